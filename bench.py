@@ -1,0 +1,394 @@
+"""Benchmark: residues/s of Angles2Backbone forward+backward on one GB300.
+
+Workload (the large-scale Angles2Backbone sweep configuration): 4096 chains of
+1000 residues, float32 angles [4096, 3, 1000] with phi, psi ~ U[-pi, pi) and
+omega = pi, upstream gradient ~ N(0, 1) of the coordinates' shape.  Synthetic,
+seeded; inputs (49 MB angles + 147 MB upstream gradient) and outputs (147 MB
+coordinates + 49 MB gradient) exceed the 129 MB L2, so no L2 flush is needed
+between steps.
+
+One step = forward (angles -> N, CA, C coordinates) + backward (dL/dcoords ->
+dL/dangles) of the batched FP32 kernels, replayed from a CUDA graph.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line.  `--impl reference` times the reference's CPU algorithm
+for the same workload on a bounded sample of chains per step, on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_CHAINS, L_RES = 4096, 1000
+FWD_BYTES_PER_RES = 12 + 36          # angles in, N/CA/C coordinates out (FP32)
+BWD_BYTES_PER_RES = 12 + 36 + 12     # angles + dL/dcoords in, dL/dangles out
+WORKLOAD = "Angles2Backbone fwd+bwd, 4096 chains x 1000 residues, FP32"
+
+
+def make_inputs(seed=1005):
+    g = np.random.default_rng(seed)
+    ang = g.uniform(-np.pi, np.pi, (B_CHAINS, 3, L_RES)).astype(np.float32)
+    ang[:, 2] = np.float32(np.pi)
+    up = g.standard_normal((B_CHAINS, 9 * L_RES), dtype=np.float32)
+    lengths = np.full(B_CHAINS, L_RES, dtype=np.int32)
+    return ang, lengths, up
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def traffic_from_profiles():
+    p = os.path.join(ROOT, "profiles", "a2b_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return None
+    return None
+
+
+# ----------------------------------------------------------------- CPU baseline
+def cpu_reference_rate(sample_chains=None, threads=None, use_port=None):
+    """Reference CPU algorithm (O(L^2) Jacobian backward) on `sample_chains` chains of
+    the workload, one chain per host thread.  Returns (residues/s, cores, kind, sample)."""
+    import oracle
+
+    kind = "reference" if (use_port is False or (use_port is None and oracle.ref_available())) else "port"
+    threads = threads or os.cpu_count() or 1
+    n = sample_chains or threads
+    ang, lengths, up = make_inputs()
+    ang = ang[:n].astype(np.float64)
+    lengths = lengths[:n]
+    up = up[:n].astype(np.float64)
+    t0 = time.perf_counter()
+    if kind == "reference":
+        c, A = oracle.a2b_forward(ang, lengths, impl="ref", threads=threads)
+        oracle.a2b_backward(up, ang, lengths, A, impl="ref", threads=threads)
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+
+        def one(b):
+            c, A = oracle.a2b_forward(ang[b:b + 1], lengths[b:b + 1])
+            oracle.a2b_backward(up[b:b + 1], ang[b:b + 1], lengths[b:b + 1], A)
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(one, range(n)))
+    dt = time.perf_counter() - t0
+    return n * L_RES / dt, threads, kind, f"{n} chains x {L_RES} residues (FP64 fwd+bwd), {threads} threads"
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build(os.environ.get("TPL_REFERENCE_DIR", "/root/reference"))
+    threads = os.cpu_count() or 1
+    for _ in range(max(0, args.warmup)):
+        cpu_reference_rate(sample_chains=threads, threads=threads)
+    rates = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, cores, kind, sample = cpu_reference_rate(sample_chains=threads, threads=threads)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    value = statistics.median(rates)
+    line = {"metric": "residues/sec fwd+bwd", "value": value, "unit": "residues/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": "residues/s", "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "residues/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------- ours
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from torchproteinlibrary_gb300 import load_extension
+    from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+
+    rm = load_extension("_ReducedModel")
+    ang_np, len_np, up_np = make_inputs(seed=1005 + rank)  # weak scaling: a full batch per GPU
+    ang = torch.from_numpy(ang_np).to(dev)
+    lengths = torch.from_numpy(len_np).to(dev)
+    up = torch.from_numpy(up_np).to(dev)
+    B, L = B_CHAINS, L_RES
+    ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+    coords = torch.empty(B, 9 * L, device=dev)
+    gang = torch.empty(B, 3, L, device=dev)
+    none = torch.empty(0, device=dev)
+
+    def fwd():
+        rm.Angles2BackboneGPU_forward(ang, coords, lengths, ws)
+
+    def bwd():
+        rm.Angles2BackboneGPU_backward(gang, up, ang, lengths, ws, none)
+
+    # warm-up (eager), then capture one step per graph for per-kernel events
+    s = torch.cuda.Stream(device=dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(s):
+        for _ in range(max(3, args.warmup)):
+            fwd(); bwd()
+    torch.cuda.current_stream(dev).wait_stream(s)
+    torch.cuda.synchronize(dev)
+    g_f, g_b = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_f):
+        fwd()
+    with torch.cuda.graph(g_b):
+        bwd()
+    for _ in range(args.warmup):
+        g_f.replay(); g_b.replay()
+    torch.cuda.synchronize(dev)
+
+    stream = torch.cuda.current_stream(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            g_f.replay()
+            ev[i][1].record(stream)
+            g_b.replay()
+            ev[i][2].record(stream)
+        end.record(stream)
+        torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    ms = start.elapsed_time(end)
+    t_f = [e[0].elapsed_time(e[1]) for e in ev]
+    t_b = [e[1].elapsed_time(e[2]) for e in ev]
+    ms_t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    residues = B * L * args.steps * world
+    value = residues / (ms / 1e3)
+
+    # correctness of this very run against the FP64 plain form on a slice
+    check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
+
+    # plain FP64 form on the same workload (the drop-in denominator)
+    plain = time_plain_fp64(rm, ang, lengths, up, dev, steps=max(1, min(3, args.steps)))
+
+    # e2e: public autograd layer, host (pinned) inputs in, results back to the host
+    e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(1, min(5, args.steps)))
+
+    peak, peak_kind = peaks()
+    fwd_ms, bwd_ms = statistics.mean(t_f), statistics.mean(t_b)
+    dom = "backward" if bwd_ms >= fwd_ms else "forward"
+    dom_ms = max(fwd_ms, bwd_ms)
+    dom_bytes = B * L * (BWD_BYTES_PER_RES if dom == "backward" else FWD_BYTES_PER_RES)
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    tr = traffic_from_profiles()
+    traffic = None
+    if tr and dom in tr:
+        traffic = tr[dom]
+    line = {
+        "metric": "residues/sec fwd+bwd", "value": value, "unit": "residues/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "global_batch_chains": B * world, "residues_per_chain": L,
+                   "l2": "inputs and outputs larger than L2; no flush", "launch": "CUDA graph per pass",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": f"a2b_{'bwd' if dom == 'backward' else 'fwd'}_f32",
+                     "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": dom_bytes},
+        "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
+        "gpu_launches": 2 * args.steps,
+        "e2e": e2e,
+        "plain_fp64": plain,
+        "accuracy_vs_fp64": check,
+    }
+    if rank == 0:
+        line["clocks"] = clk.summary()
+        line["cpu_baseline"] = cpu_baseline_entry()
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev, n=256):
+    import torch
+
+    a64 = ang[:n].double().contiguous()
+    ln = lengths[:n].contiguous()
+    c64 = torch.empty(n, 9 * L_RES, dtype=torch.float64, device=dev)
+    g64 = torch.empty(n, 3, L_RES, dtype=torch.float64, device=dev)
+    ws = torch.zeros(rm.workspace_bytes(n, L_RES), dtype=torch.uint8, device=dev)
+    rm.Angles2BackboneGPU_forward(a64, c64, ln, ws)
+    rm.Angles2BackboneGPU_backward(g64, up[:n].double().contiguous(), a64, ln, ws, torch.empty(0, device=dev))
+    d = (coords[:n].double() - c64).view(n, -1, 3).norm(dim=-1)
+    ge = (gang[:n].double() - g64).abs().max() / g64.abs().max()
+    return {"chains": n, "coord_max_A": float(d.max()), "coord_rms_A": float(d.pow(2).mean().sqrt()),
+            "grad_max_rel": float(ge), "reference": "plain FP64 form on the same float32 angles"}
+
+
+def time_plain_fp64(rm, ang, lengths, up, dev, steps):
+    import torch
+
+    a64 = ang.double()
+    u64 = up.double()
+    B = a64.shape[0]
+    c = torch.empty(B, 9 * L_RES, dtype=torch.float64, device=dev)
+    g = torch.empty(B, 3, L_RES, dtype=torch.float64, device=dev)
+    ws = torch.zeros(rm.workspace_bytes(B, L_RES), dtype=torch.uint8, device=dev)
+    none = torch.empty(0, device=dev)
+    rm.Angles2BackboneGPU_forward(a64, c, lengths, ws)
+    rm.Angles2BackboneGPU_backward(g, u64, a64, lengths, ws, none)
+    torch.cuda.synchronize(dev)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        rm.Angles2BackboneGPU_forward(a64, c, lengths, ws)
+        rm.Angles2BackboneGPU_backward(g, u64, a64, lengths, ws, none)
+    e.record()
+    torch.cuda.synchronize(dev)
+    ms = s.elapsed_time(e) / steps
+    return {"value": B * L_RES / (ms / 1e3), "unit": "residues/s", "ms_per_step": ms, "steps": steps,
+            "dtype": "f64", "form": "one chain per CTA, FP64, one launch per pass"}
+
+
+def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
+    import torch
+
+    ang_h = torch.from_numpy(ang_np).pin_memory()
+    len_h = torch.from_numpy(len_np).pin_memory()
+    up_h = torch.from_numpy(up_np).pin_memory()
+    out_c = torch.empty(ang_np.shape[0], 9 * L_RES).pin_memory()
+    out_g = torch.empty(ang_np.shape).pin_memory()
+
+    def step():
+        a = ang_h.to(dev, non_blocking=True).requires_grad_()
+        ln = len_h.to(dev, non_blocking=True)
+        u = up_h.to(dev, non_blocking=True)
+        c = layer(a, ln)
+        c.backward(u)
+        out_c.copy_(c.detach(), non_blocking=True)
+        out_g.copy_(a.grad, non_blocking=True)
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize(dev)
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    h2d = ang_np.nbytes + len_np.nbytes + up_np.nbytes
+    d2h = out_c.numel() * 4 + out_g.numel() * 4
+    return {"value": ang_np.shape[0] * L_RES / (ms / 1e3), "unit": "residues/s", "ms_per_step": ms,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "api": "torchproteinlibrary_gb300.ReducedModel.Angles2Backbone (autograd), pinned host buffers"}
+
+
+def cpu_baseline_entry():
+    try:
+        import oracle
+
+        oracle.build(os.environ.get("TPL_REFERENCE_DIR", "/root/reference"))
+        threads = os.cpu_count() or 1
+        r, cores, kind, sample = cpu_reference_rate(sample_chains=threads, threads=threads)
+        return {"value": r, "unit": "residues/s", "cores": cores, "kind": kind, "sample": sample}
+    except Exception as e:  # the baseline is reported, never required
+        return {"value": None, "unit": "residues/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup) if args.impl == "ours" else args.warmup
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

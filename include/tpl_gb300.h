@@ -1,0 +1,116 @@
+/*
+ * tpl_gb300.h -- C ABI of the GB300 (sm_103a) chain-kinematics library
+ * (libtpl_gb300.so).
+ *
+ * The library replaces the compute behind TorchProteinLibrary's two
+ * internal-coordinate layers:
+ *   ReducedModel.Angles2Backbone  (phi, psi, omega + lengths -> N, CA, C coords)
+ *   FullAtomModel.Angles2Coords   (8 angles + sequences -> heavy-atom coords)
+ * Each entry point below names the reference interface it stands in for
+ * (paths relative to the reference project).
+ *
+ * Conventions
+ *   - Plain pointers, sizes and a CUDA stream passed as `void *` (a cudaStream_t;
+ *     NULL = legacy default stream).  No torch types.
+ *   - Every pointer argument is a DEVICE pointer unless stated otherwise.
+ *   - Layouts are the reference's: angles [batch, rows, max_len] row-major,
+ *     coordinates [batch, 3 * atoms] with xyz interleaved, lengths int32.
+ *   - The caller owns every buffer, including the workspace.  Entry points are
+ *     asynchronous: they enqueue work on `stream` and return a tpl_status that
+ *     covers argument checks and the launch itself.  Errors the kernels detect
+ *     (a length outside [0, max_len], a look-back wait that timed out) are
+ *     recorded in the workspace; tpl_workspace_status() reads them back.
+ *   - No entry point allocates device memory or synchronises the stream,
+ *     except tpl_workspace_status().
+ */
+#ifndef TPL_GB300_H
+#define TPL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tpl_status {
+    TPL_OK = 0,
+    TPL_ERR_ARGUMENT = -1,          /* null pointer, negative size, bad option */
+    TPL_ERR_WORKSPACE = -2,         /* workspace missing or too small */
+    TPL_ERR_LAUNCH = -3,            /* CUDA reported an error at launch */
+    TPL_ERR_LENGTH = -4,            /* a chain length outside [0, max_len] (device-detected) */
+    TPL_ERR_SEQUENCE = -5,          /* a residue letter outside the 20 standard ones */
+    TPL_ERR_LOOKBACK_TIMEOUT = -6,  /* a bounded inter-tile wait gave up (device-detected) */
+    TPL_ERR_ATOMS = -7,             /* a chain needs more atom slots than max_atoms */
+    TPL_ERR_UNSUPPORTED = -8        /* option combination without a compiled kernel */
+} tpl_status;
+
+/* Tuning knobs.  A NULL options pointer, or a zero field, selects the tuned default. */
+typedef struct tpl_options {
+    int residues_per_thread;   /* residues each thread scans serially: 1, 2, 4 or 8 */
+    int threads_per_cta;       /* 64, 128 or 256 */
+    int fp64_carry_min_len;    /* chains at least this long compose inter-tile carries in FP64;
+                                  0 = default (always), -1 = never */
+    int renormalize;           /* 0 = default (on), 1 = on, -1 = off: Newton-Schulz renormalisation
+                                  of scan aggregates */
+    int max_ctas;              /* cap on persistent CTAs; 0 = occupancy-derived */
+} tpl_options;
+
+/* Human-readable text for a tpl_status value (host). */
+const char *tpl_status_string(int status);
+
+/* Library version, major * 10000 + minor * 100 + patch (host). */
+int tpl_version(void);
+
+/* Bytes of workspace the Angles2Backbone FP32 entry points need for a batch of
+ * `batch` chains stored with stride `max_len` (host). */
+size_t tpl_a2b_workspace_bytes(int batch, int max_len, const tpl_options *opt);
+
+/* Zero a workspace before its first use, or after an error (enqueued on stream). */
+int tpl_workspace_init(void *workspace, size_t workspace_bytes, void *stream);
+
+/* Synchronise `stream`, then return the first error the kernels recorded in
+ * `workspace` (TPL_OK if none) through *status_out.  The recorded error is cleared. */
+int tpl_workspace_status(void *workspace, void *stream, int *status_out);
+
+/* Angles2Backbone forward, batched FP32.
+ * Replaces Angles2BackboneGPU_forward (Layers/ReducedModel/Angles2Backbone/
+ * angles2backbone_interface.cpp:7-26, kernel cBackboneProteinCUDAKernels.cu:6-41).
+ *   angles  [batch, 3, max_len]  rows phi, psi, omega (radians)
+ *   lengths [batch] int32        residues per chain, 0 <= lengths[b] <= max_len
+ *   coords  [batch, 9 * max_len] N, CA, C xyz per residue; zero past 9 * lengths[b]
+ * The workspace (the reference's `A` buffer) keeps one carry transform per tile
+ * for the backward; it must be passed unchanged to tpl_a2b_backward_f32. */
+int tpl_a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, void *workspace,
+                        size_t workspace_bytes, int batch, int max_len, const tpl_options *opt, void *stream);
+
+/* Angles2Backbone backward, batched FP32 adjoint.
+ * Replaces Angles2BackboneGPU_backward (angles2backbone_interface.cpp:27-56,
+ * kernels cBackboneProteinCUDAKernels.cu:84-163).  Writes dL/dangles
+ * [batch, 3, max_len] (overwritten, zero past each length) from dL/dcoords
+ * [batch, 9 * max_len].  No per-atom Jacobian (the reference's dr_dangle) is formed.
+ * omega of each chain's last residue moves no atom; its gradient is 0 (the
+ * reference reads one transform past the chain there). */
+int tpl_a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles,
+                         const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         const tpl_options *opt, void *stream);
+
+/* Angles2Backbone forward, plain FP64 form: one chain per CTA, one launch.
+ * Same contract as tpl_a2b_forward_f32 in double precision; replaces
+ * Angles2BackboneCPU_forward (angles2backbone_interface.cpp:60-80) on the GPU.
+ * Needs no workspace. */
+int tpl_a2b_forward_f64(const double *angles, const int32_t *lengths, double *coords, int batch, int max_len,
+                        void *stream);
+
+/* Angles2Backbone backward, plain FP64 form (replaces Angles2BackboneCPU_backward,
+ * angles2backbone_interface.cpp:82-111).  The workspace needs
+ * tpl_a2b_workspace_bytes(batch, max_len, NULL) bytes. */
+int tpl_a2b_backward_f64(double *grad_angles, const double *grad_coords, const double *angles,
+                         const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TPL_GB300_H */

@@ -1,0 +1,172 @@
+"""ORACLE -- test infrastructure only.
+
+CPU checkers for the internal-coordinate chain kinematics path:
+
+* ``port``: ``oracle/tpl_oracle.c``, a plain-C FP64 restatement of the reference
+  algorithms (Angles2Backbone: Layers/ReducedModel/cBackboneProteinCPUKernels.cpp:14-145;
+  Angles2Coords: Layers/FullAtomModel/cConformation.cpp:30-211 with the residue
+  templates of cConformationAA.cpp and cRigidGroup.cpp).
+* ``ref``: the reference's own CPU kinematics sources compiled unmodified into
+  ``oracle/_ref/libtplref.so`` (``make -C oracle ref``), when they were built.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its CPU-baseline
+leg and ``--impl reference``) may import this package.  The product path
+(``torchproteinlibrary_gb300``) never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_PORT = None
+_REF = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_up = ctypes.POINTER(ctypes.c_ubyte)
+
+
+def build(ref_dir: str | None = None) -> None:
+    """Compile the C restatement, and the reference sources when ``ref_dir`` exists."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if ref_dir and os.path.isdir(ref_dir):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True)
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+def port():
+    global _PORT
+    if _PORT is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        lib = ctypes.CDLL(path)
+        lib.oracle_a2b_forward.argtypes = [_dp, _ip, _dp, _dp, ctypes.c_int, ctypes.c_int]
+        lib.oracle_a2b_backward.argtypes = [_dp, _dp, _dp, _ip, _dp, ctypes.c_int, ctypes.c_int]
+        lib.oracle_num_atoms.argtypes = [ctypes.c_char_p]
+        lib.oracle_a2c_forward.argtypes = [_up, ctypes.c_int, _dp, _dp, _up, _up, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int]
+        lib.oracle_a2c_backward.argtypes = [_dp, _dp, _up, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int]
+        _PORT = lib
+    return _PORT
+
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libtplref.so"))
+
+
+def ref():
+    global _REF
+    if _REF is None:
+        path = os.path.join(HERE, "_ref", "libtplref.so")
+        lib = ctypes.CDLL(path)
+        i = ctypes.c_int
+        lib.ref_a2b_forward.argtypes = [_dp, _ip, _dp, _dp, i, i, i]
+        lib.ref_a2b_backward.argtypes = [_dp, _dp, _dp, _ip, _dp, _dp, i, i, i]
+        lib.ref_a2c_forward.argtypes = [_up, i, _dp, _dp, _up, _up, i, i, i, i]
+        lib.ref_a2c_backward.argtypes = [_dp, _dp, _up, i, _dp, i, i, i, i]
+        _REF = lib
+    return _REF
+
+
+# ----------------------------------------------------------------- helpers
+def seq_bytes(seqs: list[str]) -> np.ndarray:
+    """NUL-terminated byte rows, as TorchProteinLibrary/FullAtomModel/Angles2Coords/Angles2Coords.py:12-26."""
+    width = max(len(s) for s in seqs) + 1 if seqs else 1
+    out = np.zeros((len(seqs), width), dtype=np.uint8)
+    for i, s in enumerate(seqs):
+        out[i, : len(s)] = np.frombuffer(s.encode("ascii"), dtype=np.uint8)
+    return out
+
+
+def num_atoms(seq: str) -> int:
+    n = port().oracle_num_atoms(seq.encode("ascii"))
+    if n < 0:
+        raise ValueError(f"unknown residue letter in {seq!r}")
+    return n
+
+
+def a2b_forward(angles: np.ndarray, lengths: np.ndarray, impl: str = "port", threads: int = 1):
+    """angles [B,3,L] f64, lengths [B] int32 -> (coords [B,9L], A [B,48L])."""
+    angles = np.ascontiguousarray(angles, dtype=np.float64)
+    lengths = np.ascontiguousarray(lengths, dtype=np.int32)
+    B, _, L = angles.shape
+    coords = np.zeros((B, 9 * L))
+    A = np.zeros((B, 48 * L))
+    if impl == "ref":
+        rc = ref().ref_a2b_forward(_ptr(angles, _dp), _ptr(lengths, _ip), _ptr(coords, _dp), _ptr(A, _dp), B, L,
+                                   threads)
+    else:
+        rc = port().oracle_a2b_forward(_ptr(angles, _dp), _ptr(lengths, _ip), _ptr(coords, _dp), _ptr(A, _dp), B, L)
+    if rc != 0:
+        raise RuntimeError(f"a2b_forward failed ({rc})")
+    return coords, A
+
+
+def a2b_backward(grad_coords: np.ndarray, angles: np.ndarray, lengths: np.ndarray, A: np.ndarray,
+                 impl: str = "port", threads: int = 1) -> np.ndarray:
+    """Returns dL/dangles [B,3,L].  impl='ref' returns the reference's raw values
+    (including its omega[len-1] entry, which reads one matrix past the chain)."""
+    angles = np.ascontiguousarray(angles, dtype=np.float64)
+    lengths = np.ascontiguousarray(lengths, dtype=np.int32)
+    grad_coords = np.ascontiguousarray(grad_coords, dtype=np.float64)
+    B, _, L = angles.shape
+    out = np.zeros((B, 3, L))
+    if impl == "ref":
+        dr = np.zeros(27 * L * L * max(1, threads))
+        rc = ref().ref_a2b_backward(_ptr(out, _dp), _ptr(grad_coords, _dp), _ptr(angles, _dp), _ptr(lengths, _ip),
+                                    _ptr(A, _dp), _ptr(dr, _dp), B, L, threads)
+    else:
+        rc = port().oracle_a2b_backward(_ptr(out, _dp), _ptr(grad_coords, _dp), _ptr(angles, _dp),
+                                        _ptr(lengths, _ip), _ptr(A, _dp), B, L)
+    if rc != 0:
+        raise RuntimeError(f"a2b_backward failed ({rc})")
+    return out
+
+
+def a2c_forward(angles: np.ndarray, seqs: list[str], impl: str = "port", threads: int = 1):
+    """angles [B,8,L] f64 -> (coords [B,3*maxA], res_names u8 [B,maxA,4], atom_names u8 [B,maxA,4], num_atoms)."""
+    angles = np.ascontiguousarray(angles, dtype=np.float64)
+    B, _, L = angles.shape
+    sb = seq_bytes(seqs)
+    na = np.array([num_atoms(s) for s in seqs], dtype=np.int32)
+    maxA = int(na.max()) if B else 0
+    coords = np.zeros((B, 3 * maxA))
+    rn = np.zeros((B, maxA, 4), dtype=np.uint8)
+    an = np.zeros((B, maxA, 4), dtype=np.uint8)
+    if impl == "ref":
+        rc = ref().ref_a2c_forward(_ptr(sb, _up), sb.shape[1], _ptr(angles, _dp), _ptr(coords, _dp), _ptr(rn, _up),
+                                   _ptr(an, _up), B, L, maxA, threads)
+    else:
+        rc = port().oracle_a2c_forward(_ptr(sb, _up), sb.shape[1], _ptr(angles, _dp), _ptr(coords, _dp),
+                                       _ptr(rn, _up), _ptr(an, _up), B, L, maxA)
+    if rc != 0:
+        raise RuntimeError(f"a2c_forward failed ({rc})")
+    return coords, rn, an, na
+
+
+def a2c_backward(grad_coords: np.ndarray, angles: np.ndarray, seqs: list[str], impl: str = "port",
+                 threads: int = 1) -> np.ndarray:
+    angles = np.ascontiguousarray(angles, dtype=np.float64)
+    grad_coords = np.ascontiguousarray(grad_coords, dtype=np.float64)
+    B, _, L = angles.shape
+    sb = seq_bytes(seqs)
+    maxA = grad_coords.shape[1] // 3
+    out = np.zeros((B, 8, L))
+    if impl == "ref":
+        rc = ref().ref_a2c_backward(_ptr(grad_coords, _dp), _ptr(out, _dp), _ptr(sb, _up), sb.shape[1],
+                                    _ptr(angles, _dp), B, L, maxA, threads)
+    else:
+        rc = port().oracle_a2c_backward(_ptr(grad_coords, _dp), _ptr(out, _dp), _ptr(sb, _up), sb.shape[1],
+                                        _ptr(angles, _dp), B, L, maxA)
+    if rc != 0:
+        raise RuntimeError(f"a2c_backward failed ({rc})")
+    return out

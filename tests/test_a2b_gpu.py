@@ -1,0 +1,295 @@
+"""Angles2Backbone on the GPU against the oracle (FP64 restatement of the
+reference CPU path, itself pinned to the reference in test_oracle_pin.py).
+
+Tolerances (stated here, used below):
+  * FP64 plain form vs oracle: coordinates 1e-9 A, gradients 1e-9 x max|grad|.
+  * FP32 batched form vs oracle on the same float32 angles: coordinates 1e-3 A
+    (the target for chains up to 1000 residues), gradients 1e-4 x max|grad|.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+COORD_TOL_F32 = 1e-3
+GRAD_TOL_F32 = 1e-4
+COORD_TOL_F64 = 1e-9
+GRAD_TOL_F64 = 1e-9
+
+
+@pytest.fixture(scope="module")
+def rm(built):
+    from torchproteinlibrary_gb300 import load_extension
+    m = load_extension("_ReducedModel")
+    m.set_options(0, 0, 0, 0)
+    yield m
+    m.set_options(0, 0, 0, 0)
+
+
+def make_case(B, L, seed, lengths=None, omega="pi"):
+    rng = np.random.default_rng(seed)
+    ang = rng.uniform(-np.pi, np.pi, (B, 3, L))
+    if omega == "pi":
+        ang[:, 2] = np.pi
+    else:
+        ang[:, 2] = rng.normal(np.pi, 0.05, (B, L))
+    if lengths is None:
+        lengths = rng.integers(0, L + 1, B)
+    lengths = np.asarray(lengths, dtype=np.int32)
+    g = rng.standard_normal((B, 9 * L))
+    return ang, lengths, g
+
+
+def run_gpu(rm, ang, lengths, g, dtype):
+    dev = torch.device("cuda")
+    a = torch.tensor(ang, dtype=dtype, device=dev)
+    ln = torch.tensor(lengths, dtype=torch.int32, device=dev)
+    B, _, L = a.shape
+    ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+    coords = torch.full((B, 9 * L), float("nan"), dtype=dtype, device=dev)
+    rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
+    gi = torch.full((B, 3, L), float("nan"), dtype=dtype, device=dev)
+    gt = torch.tensor(g, dtype=dtype, device=dev)
+    rm.Angles2BackboneGPU_backward(gi, gt, a, ln, ws, torch.empty(0, device=dev))
+    assert rm.workspace_status(ws) == 0
+    return coords.double().cpu().numpy(), gi.double().cpu().numpy()
+
+
+def oracle_ref(ang, lengths, g, as_float32):
+    a = ang.astype(np.float32).astype(np.float64) if as_float32 else ang
+    c, A = oracle.a2b_forward(a, lengths)
+    return c, oracle.a2b_backward(g if not as_float32 else g.astype(np.float32).astype(np.float64), a, lengths, A)
+
+
+def check(got_c, got_g, ref_c, ref_g, lengths, L, ctol, gtol):
+    B = len(lengths)
+    for b in range(B):
+        n = lengths[b]
+        assert np.all(got_c[b, 9 * n:] == 0.0), "coordinates past the chain must be exactly zero"
+        assert np.all(got_g[b, :, n:] == 0.0), "gradients past the chain must be exactly zero"
+    d = np.abs(got_c - ref_c).reshape(B, -1, 3)
+    err = np.sqrt((d ** 2).sum(-1)).max()
+    assert err <= ctol, f"max coordinate error {err:.3e} A"
+    scale = max(1.0, np.abs(ref_g).max())
+    gerr = np.abs(got_g - ref_g).max() / scale
+    assert gerr <= gtol, f"max gradient error {gerr:.3e} of max|grad|"
+    return err, gerr
+
+
+@pytest.mark.parametrize("B,L,seed", [(16, 50, 1), (5, 7, 2), (3, 130, 3), (9, 257, 4)])
+def test_fp32_matches_oracle(rm, B, L, seed):
+    ang, lengths, g = make_case(B, L, seed)
+    lengths[0] = L
+    c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+@pytest.mark.parametrize("B,L,seed", [(16, 50, 1), (3, 300, 5), (2, 513, 6)])
+def test_fp64_plain_matches_oracle(rm, B, L, seed):
+    ang, lengths, g = make_case(B, L, seed, omega="noise")
+    lengths[0] = L
+    c, gi = run_gpu(rm, ang, lengths, g, torch.float64)
+    rc, rg = oracle_ref(ang, lengths, g, False)
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F64, GRAD_TOL_F64)
+
+
+@pytest.mark.parametrize("rpt", [1, 2, 4, 8])
+def test_tile_shapes_and_lookback(rm, rpt):
+    """Chains of 1000 residues split into 8 (R=1, 128-residue tiles) down to one
+    (R=8, 1024-residue tiles) look-back tiles; all within tolerance of the oracle."""
+    B, L = 6, 1000
+    ang, lengths, g = make_case(B, L, 40 + rpt, lengths=[1000, 999, 129, 128, 127, 1])
+    rm.set_options(rpt, 0, 0, 0)
+    try:
+        c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+    finally:
+        rm.set_options(0, 0, 0, 0)
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def test_fp64_carry_threshold_and_renorm_off(rm):
+    B, L = 4, 600
+    ang, lengths, g = make_case(B, L, 77, lengths=[600, 450, 300, 20])
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    for carry, renorm in [(-1, 0), (256, 0), (0, -1)]:
+        rm.set_options(1, carry, renorm, 0)
+        try:
+            c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+        finally:
+            rm.set_options(0, 0, 0, 0)
+        check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def test_padding_nan_does_not_leak(rm):
+    B, L = 4, 64
+    ang, lengths, g = make_case(B, L, 9, lengths=[64, 30, 1, 0])
+    for b, n in enumerate(lengths):
+        ang[b, :, n:] = np.nan
+        g[b, 9 * n:] = np.nan
+    ang[1, 2, 29] = np.nan  # omega of the last residue is never used
+    c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+    a2 = np.nan_to_num(ang, nan=0.0)
+    g2 = np.nan_to_num(g, nan=0.0)
+    rc, rg = oracle_ref(a2, lengths, g2, True)
+    assert np.isfinite(c).all() and np.isfinite(gi).all()
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def test_empty_inputs(rm):
+    dev = torch.device("cuda")
+    for B, L in [(0, 10), (3, 0)]:
+        a = torch.zeros(B, 3, L, device=dev)
+        ln = torch.zeros(B, dtype=torch.int32, device=dev)
+        ws = torch.zeros(max(64, rm.workspace_bytes(B, L)), dtype=torch.uint8, device=dev)
+        out = torch.zeros(B, 9 * L, device=dev)
+        rm.Angles2BackboneGPU_forward(a, out, ln, ws)
+    c, gi = run_gpu(rm, np.zeros((3, 3, 5)), np.zeros(3, np.int32), np.ones((3, 45)), torch.float32)
+    assert np.all(c == 0) and np.all(gi == 0)
+
+
+def test_errors_raise(rm):
+    dev = torch.device("cuda")
+    a = torch.zeros(2, 3, 8, device=dev)
+    ln = torch.full((2,), 8, dtype=torch.int32, device=dev)
+    out = torch.zeros(2, 72, device=dev)
+    ws = torch.zeros(rm.workspace_bytes(2, 8), dtype=torch.uint8, device=dev)
+    with pytest.raises(RuntimeError):
+        rm.Angles2BackboneGPU_forward(a.cpu(), out.cpu(), ln.cpu(), ws.cpu())
+    with pytest.raises(RuntimeError):
+        rm.Angles2BackboneGPU_forward(a, out, ln.long(), ws)
+    with pytest.raises(RuntimeError):
+        rm.Angles2BackboneGPU_forward(a, out, ln, ws[:10])
+    # a length beyond max_len is clamped on the device and reported
+    bad = torch.tensor([8, 9], dtype=torch.int32, device=dev)
+    rm.Angles2BackboneGPU_forward(a, out, bad, ws)
+    assert rm.workspace_status(ws) == -4
+    assert rm.workspace_status(ws) == 0  # reading clears it
+
+
+def test_lookback_timeout_is_reported(rm, built):
+    """Fault injection on the host side of the kernel: the first tile of chain 0
+    never publishes, so the next tile's bounded wait runs out.  The kernel ends,
+    records TPL_ERR_LOOKBACK_TIMEOUT, and the context stays usable."""
+    from torchproteinlibrary_gb300 import capi
+    dev = torch.device("cuda")
+    B, L = 2, 300
+    a = torch.rand(B, 3, L, device=dev)
+    ln = torch.full((B,), L, dtype=torch.int32, device=dev)
+    out = torch.zeros(B, 9 * L, device=dev)
+    rm.set_options(1, 0, 0, 0)  # 128-residue tiles: 3 tiles per chain
+    try:
+        ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+        ws[4 * 8:4 * 9].view(torch.int32).fill_(1)  # WsHeader.test_skip_publish
+        rm.Angles2BackboneGPU_forward(a, out, ln, ws)
+        assert rm.workspace_status(ws) == -6
+        ws.zero_()
+        rm.Angles2BackboneGPU_forward(a, out, ln, ws)
+        assert rm.workspace_status(ws) == 0
+    finally:
+        rm.set_options(0, 0, 0, 0)
+    assert torch.isfinite(out).all()
+
+
+def test_c_abi_direct_matches_extension(rm, built):
+    from torchproteinlibrary_gb300 import capi
+    lib = capi.lib()
+    ang, lengths, g = make_case(7, 90, 21)
+    c_ext, g_ext = run_gpu(rm, ang, lengths, g, torch.float32)
+    dev = torch.device("cuda")
+    a = torch.tensor(ang, dtype=torch.float32, device=dev)
+    ln = torch.tensor(lengths, device=dev)
+    n = lib.tpl_a2b_workspace_bytes(7, 90, None)
+    ws = torch.zeros(n, dtype=torch.uint8, device=dev)
+    coords = torch.empty(7, 810, device=dev)
+    st = capi.stream_ptr()
+    capi.check(lib.tpl_a2b_forward_f32(a.data_ptr(), ln.data_ptr(), coords.data_ptr(), ws.data_ptr(), n, 7, 90,
+                                       None, st))
+    gi = torch.empty(7, 3, 90, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    capi.check(lib.tpl_a2b_backward_f32(gi.data_ptr(), gt.data_ptr(), a.data_ptr(), ln.data_ptr(), ws.data_ptr(), n,
+                                        7, 90, None, st))
+    status = ctypes.c_int(123)
+    capi.check(lib.tpl_workspace_status(ws.data_ptr(), st, ctypes.byref(status)))
+    assert status.value == 0
+    assert np.array_equal(coords.double().cpu().numpy(), c_ext)
+    assert np.array_equal(gi.double().cpu().numpy(), g_ext)
+
+
+def test_autograd_layer_and_gradcheck(built):
+    from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+    layer = Angles2Backbone()
+    dev = torch.device("cuda")
+    # reference test setup (UnitTests/ReducedModel/Angles2Backbone/test.py:72-82), here in FP64
+    torch.manual_seed(0)
+    x = torch.randn(8, 3, 8, dtype=torch.float64, device=dev, requires_grad=True)
+    n = torch.randint(4, 8, (8,), dtype=torch.int32, device=dev)
+    assert torch.autograd.gradcheck(layer, (x, n), eps=1e-6, atol=1e-6, rtol=1e-5)
+    # FP32 with the reference's own tolerances
+    x32 = x.detach().float().requires_grad_()
+    assert torch.autograd.gradcheck(layer, (x32, n), eps=1e-3, atol=1e-2, rtol=0.01)
+    with pytest.raises(RuntimeError):
+        layer(x.detach().cpu(), n.cpu())
+
+
+def test_cuda_graph_replay(rm):
+    """Persistent launches reset their tickets/epochs themselves, so a captured
+    forward+backward replays correctly without memsets."""
+    dev = torch.device("cuda")
+    B, L = 64, 400
+    ang, lengths, g = make_case(B, L, 5)
+    a = torch.tensor(ang, dtype=torch.float32, device=dev)
+    ln = torch.tensor(lengths, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+    coords = torch.empty(B, 9 * L, device=dev)
+    gi = torch.empty(B, 3, L, device=dev)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
+        rm.Angles2BackboneGPU_backward(gi, gt, a, ln, ws, torch.empty(0, device=dev))
+    torch.cuda.current_stream().wait_stream(s)
+    ref_c, ref_g = coords.clone(), gi.clone()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
+        rm.Angles2BackboneGPU_backward(gi, gt, a, ln, ws, torch.empty(0, device=dev))
+    for _ in range(3):
+        coords.zero_(); gi.zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(coords, ref_c) and torch.equal(gi, ref_g)
+    assert rm.workspace_status(ws) == 0
+
+
+def _ragged_config3(seed=1003):
+    rng = np.random.default_rng(seed)
+    B, L = 1024, 700
+    lengths = rng.integers(20, 701, B).astype(np.int32)
+    ang = rng.uniform(-np.pi, np.pi, (B, 3, L))
+    ang[:, 2] = rng.normal(np.pi, 0.05, (B, L))
+    for b, n in enumerate(lengths):
+        ang[b, :, n:] = 0.0
+    g = rng.standard_normal((B, 9 * L))
+    return ang, lengths, g
+
+
+def test_config3_full_size_against_fp64_form(rm):
+    """1024 ragged chains of 20..700 residues: the FP32 batched path agrees with the
+    FP64 plain form (pinned to the oracle above) within the stated tolerances, and
+    a few chains are checked against the CPU oracle directly."""
+    ang, lengths, g = _ragged_config3()
+    c32, g32 = run_gpu(rm, ang, lengths, g.astype(np.float32).astype(np.float64), torch.float32)
+    a32 = ang.astype(np.float32).astype(np.float64)
+    c64, g64 = run_gpu(rm, a32, lengths, g.astype(np.float32).astype(np.float64), torch.float64)
+    check(c32, g32, c64, g64, lengths, 700, COORD_TOL_F32, GRAD_TOL_F32)
+    idx = np.argsort(lengths)[-2:]
+    rc, rg = oracle_ref(ang[idx], lengths[idx], g[idx], True)
+    check(c64[idx], g64[idx], rc, rg, lengths[idx], 700, COORD_TOL_F64, GRAD_TOL_F64)

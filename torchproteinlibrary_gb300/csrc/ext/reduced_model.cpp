@@ -1,0 +1,140 @@
+// _ReducedModel extension module: the reference's entry points
+// (Layers/ReducedModel/main.cpp:4-9, Layers/ReducedModel/Angles2Backbone/
+// angles2backbone_interface.cpp) over the libtpl_gb300 C ABI.
+//
+// Differences from the reference, all deliberate:
+//  * CUDA tensors of float32 run the batched FP32 kernels, float64 the plain FP64
+//    form; the CPU entry points raise (this build has no CPU path).
+//  * `A` is the caller-owned workspace (any dtype, at least
+//    workspace_bytes(batch, max_len) bytes, zeroed before its first use).  It
+//    carries per-tile transforms from the forward to the backward.
+//  * `dr_dangle` is accepted and ignored: the adjoint forms no Jacobian.
+//  * Errors raise RuntimeError instead of passing silently (the reference's
+//    ERROR() is a no-op, Math/nUtil.h:48).
+#include <c10/cuda/CUDAGuard.h>
+#include <c10/cuda/CUDAStream.h>
+#include <torch/extension.h>
+
+#include "../../../include/tpl_gb300.h"
+
+namespace {
+
+tpl_options g_opt = {0, 0, 0, 0, 0};
+
+void check_status(int s, const char *what) {
+    TORCH_CHECK(s == TPL_OK, what, ": ", tpl_status_string(s), " (", s, ")");
+}
+
+void check_cuda(const torch::Tensor &t, const char *name) {
+    TORCH_CHECK(t.is_cuda(), name, " must be a CUDA tensor (this build has no CPU path)");
+    TORCH_CHECK(t.is_contiguous(), name, " must be contiguous");
+}
+
+void *stream_of(const torch::Tensor &t) {
+    return (void *)c10::cuda::getCurrentCUDAStream(t.device().index()).stream();
+}
+
+size_t ws_bytes(int64_t B, int64_t L) { return tpl_a2b_workspace_bytes((int)B, (int)L, &g_opt); }
+
+void Angles2BackboneGPU_forward(torch::Tensor input_angles, torch::Tensor output_coords,
+                                torch::Tensor angles_length, torch::Tensor A) {
+    check_cuda(input_angles, "input_angles");
+    check_cuda(output_coords, "output_coords");
+    check_cuda(angles_length, "angles_length");
+    check_cuda(A, "A");
+    TORCH_CHECK(input_angles.dim() == 3 && input_angles.size(1) == 3, "input_angles must be [batch, 3, max_len]");
+    TORCH_CHECK(angles_length.scalar_type() == torch::kInt, "angles_length must be int32");
+    const int64_t B = input_angles.size(0), L = input_angles.size(2);
+    TORCH_CHECK(angles_length.numel() == B, "angles_length must have one entry per chain");
+    TORCH_CHECK(output_coords.numel() == B * 9 * L, "output_coords must hold batch * 9 * max_len values");
+    TORCH_CHECK(output_coords.scalar_type() == input_angles.scalar_type(), "output_coords dtype must match angles");
+    const at::cuda::CUDAGuard guard(input_angles.device());
+    void *st = stream_of(input_angles);
+    int s;
+    if (input_angles.scalar_type() == torch::kFloat) {
+        s = tpl_a2b_forward_f32(input_angles.data_ptr<float>(), angles_length.data_ptr<int32_t>(),
+                                output_coords.data_ptr<float>(), A.data_ptr(), A.nbytes(), (int)B, (int)L, &g_opt,
+                                st);
+    } else if (input_angles.scalar_type() == torch::kDouble) {
+        s = tpl_a2b_forward_f64(input_angles.data_ptr<double>(), angles_length.data_ptr<int32_t>(),
+                                output_coords.data_ptr<double>(), (int)B, (int)L, st);
+    } else {
+        TORCH_CHECK(false, "input_angles must be float32 or float64");
+    }
+    check_status(s, "Angles2BackboneGPU_forward");
+}
+
+void Angles2BackboneGPU_backward(torch::Tensor gradInput, torch::Tensor gradOutput, torch::Tensor input_angles,
+                                 torch::Tensor angles_length, torch::Tensor A, torch::Tensor dr_dangle) {
+    (void)dr_dangle;
+    check_cuda(gradInput, "gradInput");
+    check_cuda(gradOutput, "gradOutput");
+    check_cuda(input_angles, "input_angles");
+    check_cuda(angles_length, "angles_length");
+    check_cuda(A, "A");
+    TORCH_CHECK(input_angles.dim() == 3 && input_angles.size(1) == 3, "input_angles must be [batch, 3, max_len]");
+    TORCH_CHECK(angles_length.scalar_type() == torch::kInt, "angles_length must be int32");
+    const int64_t B = input_angles.size(0), L = input_angles.size(2);
+    TORCH_CHECK(gradOutput.numel() == B * 9 * L, "gradOutput must hold batch * 9 * max_len values");
+    TORCH_CHECK(gradInput.numel() == B * 3 * L, "gradInput must hold batch * 3 * max_len values");
+    TORCH_CHECK(gradInput.scalar_type() == input_angles.scalar_type() &&
+                    gradOutput.scalar_type() == input_angles.scalar_type(),
+                "gradient dtypes must match angles");
+    const at::cuda::CUDAGuard guard(input_angles.device());
+    void *st = stream_of(input_angles);
+    int s;
+    if (input_angles.scalar_type() == torch::kFloat) {
+        s = tpl_a2b_backward_f32(gradInput.data_ptr<float>(), gradOutput.data_ptr<float>(),
+                                 input_angles.data_ptr<float>(), angles_length.data_ptr<int32_t>(), A.data_ptr(),
+                                 A.nbytes(), (int)B, (int)L, &g_opt, st);
+    } else if (input_angles.scalar_type() == torch::kDouble) {
+        s = tpl_a2b_backward_f64(gradInput.data_ptr<double>(), gradOutput.data_ptr<double>(),
+                                 input_angles.data_ptr<double>(), angles_length.data_ptr<int32_t>(), A.data_ptr(),
+                                 A.nbytes(), (int)B, (int)L, st);
+    } else {
+        TORCH_CHECK(false, "input_angles must be float32 or float64");
+    }
+    check_status(s, "Angles2BackboneGPU_backward");
+}
+
+void no_cpu_path(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
+    TORCH_CHECK(false, "Angles2Backbone: this build has no CPU path; move the tensors to a CUDA device");
+}
+void no_cpu_path_bwd(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
+    TORCH_CHECK(false, "Angles2Backbone: this build has no CPU path; move the tensors to a CUDA device");
+}
+
+int64_t workspace_bytes(int64_t B, int64_t L) { return (int64_t)ws_bytes(B, L); }
+
+int64_t workspace_status(torch::Tensor A) {
+    check_cuda(A, "A");
+    const at::cuda::CUDAGuard guard(A.device());
+    int st = 0;
+    check_status(tpl_workspace_status(A.data_ptr(), stream_of(A), &st), "workspace_status");
+    return st;
+}
+
+void set_options(int64_t residues_per_thread, int64_t fp64_carry_min_len, int64_t renormalize, int64_t max_ctas) {
+    tpl_options o = {(int)residues_per_thread, 0, (int)fp64_carry_min_len, (int)renormalize, (int)max_ctas};
+    TORCH_CHECK(o.residues_per_thread == 0 || o.residues_per_thread == 1 || o.residues_per_thread == 2 ||
+                    o.residues_per_thread == 4 || o.residues_per_thread == 8,
+                "residues_per_thread must be 0, 1, 2, 4 or 8");
+    g_opt = o;
+}
+
+std::vector<int64_t> get_options() {
+    return {g_opt.residues_per_thread, g_opt.fp64_carry_min_len, g_opt.renormalize, g_opt.max_ctas};
+}
+
+}  // namespace
+
+PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
+    m.def("Angles2BackboneGPU_forward", &Angles2BackboneGPU_forward, "Angles2Backbone gpu forward");
+    m.def("Angles2BackboneGPU_backward", &Angles2BackboneGPU_backward, "Angles2Backbone gpu backward");
+    m.def("Angles2BackboneCPU_forward", &no_cpu_path, "not available: no CPU path");
+    m.def("Angles2BackboneCPU_backward", &no_cpu_path_bwd, "not available: no CPU path");
+    m.def("workspace_bytes", &workspace_bytes, "bytes of the A workspace for (batch, max_len)");
+    m.def("workspace_status", &workspace_status, "synchronise and read the first device-detected error");
+    m.def("set_options", &set_options, "tuning knobs: residues_per_thread, fp64_carry_min_len, renormalize, max_ctas");
+    m.def("get_options", &get_options, "current tuning knobs");
+}

@@ -1,0 +1,910 @@
+// Angles2Backbone kernels for sm_103a.
+//
+// Forward (reference: Layers/ReducedModel/cBackboneProteinCUDAKernels.cu:6-41 runs
+// one thread per chain over 3L serial 4x4 products).  Here the chain of bond
+// transforms is a parallel scan:
+//   * work item = (chain, tile of R*NT residues), handed out by an atomic ticket
+//     counter to a persistent grid, tiles of a chain in order;
+//   * each thread composes the 3R joints of its R residues from identity (walk 1),
+//     warps scan the per-thread transforms with shuffles, warp totals are scanned
+//     in shared memory;
+//   * chains longer than a tile get the carry from earlier tiles by decoupled
+//     look-back on per-tile records (aggregate / inclusive prefix), composed in
+//     FP64 for chains of at least fp64_carry_min_len residues;
+//   * each thread re-walks its residues from its world prefix (walk 2) and the
+//     tile's N, CA, C positions are staged in shared memory and written with
+//     coalesced float4 stores, zeros past the chain length.
+//
+// Backward (reference: computeGradientsOptimizedBackbone + backwardFromCoordinates-
+// Backbone, cBackboneProteinCUDAKernels.cu:84-163, which materialise dR/dangle of
+// size 27 L^2 per chain).  Here the adjoint is a reverse suffix scan: with u_m the
+// rotation axis of joint m (x-axis of frame m) and x_m its origin,
+//     dL/dtheta_m = u_m . sum_{i>m} (x_i - x_m) x g_i = u_m . (S_m - x_m x G_m),
+// G_m = sum_{i>m} g_i, S_m = sum_{i>m} x_i x g_i.  The kernel recomputes the
+// forward positions (angles are 3x smaller than coordinates), scans (G, S)
+// backwards over threads, warps and tiles (tiles handed out last-first), and
+// evaluates the three joint gradients of each residue.
+#include <cstdio>
+
+#include "tpl_common.cuh"
+#include "tpl_internal.h"
+
+namespace tpl {
+
+constexpr unsigned kSpinLimit = 1u << 22;  // ~0.5 s of 100 ns sleeps
+
+struct A2bArgs {
+    const float *angles;
+    const int *lengths;
+    float *coords;
+    float *grad_angles;
+    const float *grad_coords;
+    WsHeader *hdr;
+    TileRecord *rec;
+    int L, ntiles, total;
+    int fp64_min_len;
+    int renorm;
+    BondConsts bc;
+};
+
+__device__ __forceinline__ void record_error(WsHeader *h, int code) {
+    atomicCAS(&h->status, 0u, (unsigned)code);
+}
+
+// Write n_total floats to global dst: src[i] (shared) for i < n_valid, 0 after.
+// 16-byte aligned body as float4, scalar head/tail.
+template <int NT>
+__device__ __forceinline__ void store_floats(float *dst, const float *src, int n_valid, int n_total) {
+    const int tid = threadIdx.x;
+    int head = (int)(((16u - ((unsigned)(uintptr_t)dst & 15u)) & 15u) >> 2);
+    head = min(head, n_total);
+    for (int i = tid; i < head; i += NT) dst[i] = i < n_valid ? src[i] : 0.f;
+    const int nvec = (n_total - head) >> 2;
+    float4 *d4 = reinterpret_cast<float4 *>(dst + head);
+    for (int v = tid; v < nvec; v += NT) {
+        const int i = head + 4 * v;
+        float4 x;
+        x.x = i < n_valid ? src[i] : 0.f;
+        x.y = i + 1 < n_valid ? src[i + 1] : 0.f;
+        x.z = i + 2 < n_valid ? src[i + 2] : 0.f;
+        x.w = i + 3 < n_valid ? src[i + 3] : 0.f;
+        d4[v] = x;
+    }
+    for (int i = head + 4 * nvec + tid; i < n_total; i += NT) dst[i] = i < n_valid ? src[i] : 0.f;
+}
+
+// Load n floats from global src into shared dst (coalesced).
+template <int NT>
+__device__ __forceinline__ void load_floats(float *dst, const float *src, int n) {
+    const int tid = threadIdx.x;
+    int head = (int)(((16u - ((unsigned)(uintptr_t)src & 15u)) & 15u) >> 2);
+    head = min(head, n);
+    for (int i = tid; i < head; i += NT) dst[i] = __ldg(src + i);
+    const int nvec = (n - head) >> 2;
+    const float4 *s4 = reinterpret_cast<const float4 *>(src + head);
+    for (int v = tid; v < nvec; v += NT) {
+        float4 x = __ldg(s4 + v);
+        const int i = head + 4 * v;
+        dst[i] = x.x; dst[i + 1] = x.y; dst[i + 2] = x.z; dst[i + 3] = x.w;
+    }
+    for (int i = head + 4 * nvec + tid; i < n; i += NT) dst[i] = __ldg(src + i);
+}
+
+__device__ __forceinline__ void round_to_float(Frame<double> &f) {
+#pragma unroll
+    for (int i = 0; i < 9; i++) f.r[i] = (double)(float)f.r[i];
+#pragma unroll
+    for (int i = 0; i < 3; i++) f.p[i] = (double)(float)f.p[i];
+}
+
+__device__ __forceinline__ void store_frame_d(double *dst, const Frame<double> &f) { frame_store(dst, f); }
+
+// Spin (bounded) until the record flag carries this launch's epoch and a state.
+__device__ __forceinline__ unsigned wait_flag(const unsigned *flag, unsigned epoch_bits, WsHeader *h, bool &ok) {
+    unsigned f = 0;
+    for (unsigned spins = 0;; spins++) {
+        f = ld_acquire(flag);
+        if ((f & ~3u) == epoch_bits && (f & 3u)) return f;
+        if (spins >= kSpinLimit) {
+            record_error(h, TPL_ERR_LOOKBACK_TIMEOUT);
+            ok = false;
+            return 0;
+        }
+        __nanosleep(100);
+    }
+}
+
+// Tile scan shared by forward and backward: thread aggregates of R residues,
+// warp scan, warp totals in shared memory.  Returns the thread's exclusive prefix
+// inside its warp; s_wtot receives the warp totals.
+template <int R, int NT>
+__device__ __forceinline__ Frame<float> tile_local_scan(const A2bArgs &a, const float (*s_ang)[R * NT], int nreal,
+                                                        bool last_in_tile_is_chain_end, float (&cs)[R][3],
+                                                        float (&sn)[R][3], Frame<float> *s_wtot) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int j0 = tid * R;
+    Frame<float> agg;
+    frame_identity(agg);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int j = j0 + r;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            cs[r][k] = 1.f;
+            sn[r][k] = 0.f;
+        }
+        if (j < nreal) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (k == 2 && last_in_tile_is_chain_end && j == nreal - 1) break;  // omega[len-1] moves nothing
+                sincosf(s_ang[k][j], &sn[r][k], &cs[r][k]);
+                apply_joint(agg, a.bc.cb[k], a.bc.sb[k], a.bc.d[k], cs[r][k], sn[r][k]);
+            }
+        }
+    }
+    if (a.renorm) renormalize(agg);
+    Frame<float> inc = warp_scan_frames(agg, lane);
+    Frame<float> exc = shfl_up_frame(inc, 1);
+    if (lane == 0) frame_identity(exc);
+    if (lane == 31) s_wtot[w] = inc;
+    return exc;
+}
+
+// Forward inter-tile carry by decoupled look-back (thread 0 only).
+// Returns the transform of the chain frame at the start of tile t (FP64).
+__device__ Frame<double> forward_carry(const A2bArgs &a, int b, int t, bool more, const Frame<float> &tile_agg,
+                                       unsigned epoch_bits, bool use64) {
+    TileRecord *rc = a.rec + (size_t)b * a.ntiles + t;
+    Frame<double> agg64 = frame_cast<double>(tile_agg);
+    Frame<double> carry;
+    frame_identity(carry);
+    if (t == 0) {
+        // test hook: leave the first tile of chain 0 unpublished so that its
+        // successor's bounded wait runs out (tpl_workspace_status reports it)
+        if (more && !(b == 0 && a.hdr->test_skip_publish)) {
+            store_frame_d(rc->finc, agg64);
+            st_release(&rc->fflag, epoch_bits | kFlagInc);
+        }
+        return carry;
+    }
+    if (more) {
+        store_frame_d(rc->fagg, agg64);
+        st_release(&rc->fflag, epoch_bits | kFlagAgg);
+    }
+    Frame<double> acc;
+    frame_identity(acc);
+    bool ok = true;
+    for (int tt = t - 1; tt >= 0; tt--) {
+        const TileRecord *q = a.rec + (size_t)b * a.ntiles + tt;
+        unsigned f = wait_flag(&q->fflag, epoch_bits, a.hdr, ok);
+        if (!ok) break;
+        Frame<double> x;
+        if ((f & 3u) == kFlagInc) {
+            frame_load(x, q->finc);
+            carry = compose(x, acc);
+            if (!use64) round_to_float(carry);
+            break;
+        }
+        frame_load(x, q->fagg);
+        acc = compose(x, acc);
+        if (!use64) round_to_float(acc);
+    }
+    if (!ok) frame_identity(carry);
+    if (a.renorm) renormalize(carry);
+    frame_store(rc->fexc, carry);
+    if (more) {
+        Frame<double> incl = compose(carry, agg64);
+        if (!use64) round_to_float(incl);
+        if (a.renorm) renormalize(incl);
+        store_frame_d(rc->finc, incl);
+        st_release(&rc->fflag, epoch_bits | kFlagInc);
+    }
+    return carry;
+}
+
+__device__ __forceinline__ void finish_launch(unsigned *ticket, unsigned *done, unsigned *epoch) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(done, 1u);
+        if (prev == gridDim.x - 1) {
+            atomicExch(ticket, 0u);
+            atomicExch(done, 0u);
+            __threadfence();
+            atomicAdd(epoch, 1u);
+        }
+    }
+}
+
+template <int R, int NT>
+__global__ void __launch_bounds__(NT) a2b_fwd_f32_kernel(A2bArgs a) {
+    constexpr int TILE = R * NT;
+    constexpr int NW = NT / 32;
+    __shared__ float s_ang[3][TILE];
+    __shared__ float s_out[9 * TILE];
+    __shared__ Frame<float> s_wtot[NW];
+    __shared__ Frame<float> s_wpre[NW];
+    __shared__ float s_org[3];
+    __shared__ int s_item;
+    __shared__ unsigned s_epoch;
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) s_epoch = (*(volatile unsigned *)&a.hdr->fwd_epoch & 0x3fffffffu) << 2;
+
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(&a.hdr->fwd_ticket, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.total) break;
+        const int b = item / a.ntiles, t = item - b * a.ntiles;
+        int len = a.lengths[b];
+        if (len < 0 || len > a.L) {
+            if (tid == 0) record_error(a.hdr, TPL_ERR_LENGTH);
+            len = max(0, min(len, a.L));
+        }
+        const int s0 = t * TILE;
+        const int ntile = min(TILE, a.L - s0);
+        const int nreal = max(0, min(ntile, len - s0));
+        float *out = a.coords + (size_t)b * 9 * a.L + (size_t)9 * s0;
+        if (nreal == 0) {
+            store_floats<NT>(out, s_out, 0, 9 * ntile);
+            __syncthreads();
+            continue;
+        }
+        const float *ang = a.angles + (size_t)b * 3 * a.L + s0;
+        load_floats<NT>(s_ang[0], ang, nreal);
+        load_floats<NT>(s_ang[1], ang + a.L, nreal);
+        load_floats<NT>(s_ang[2], ang + 2 * a.L, nreal);
+        __syncthreads();
+
+        const bool chain_end = (s0 + nreal == len);
+        float cs[R][3], sn[R][3];
+        Frame<float> exc = tile_local_scan<R, NT>(a, s_ang, nreal, chain_end, cs, sn, s_wtot);
+        __syncthreads();
+
+        if (tid == 0) {
+            Frame<float> run;
+            frame_identity(run);
+            Frame<float> pre[NW];
+#pragma unroll
+            for (int ww = 0; ww < NW; ww++) {
+                pre[ww] = run;
+                run = compose(run, s_wtot[ww]);
+                if (a.renorm) renormalize(run);
+            }
+            const bool more = s0 + TILE < len;
+            const bool use64 = a.fp64_min_len >= 0 && len >= a.fp64_min_len;
+            Frame<double> carry = forward_carry(a, b, t, more, run, s_epoch, use64);
+            Frame<float> c32 = frame_cast<float>(carry);
+            s_org[0] = c32.p[0]; s_org[1] = c32.p[1]; s_org[2] = c32.p[2];
+            c32.p[0] = c32.p[1] = c32.p[2] = 0.f;  // positions relative to the tile origin
+#pragma unroll
+            for (int ww = 0; ww < NW; ww++) s_wpre[ww] = compose(c32, pre[ww]);
+        }
+        __syncthreads();
+
+        Frame<float> P = compose(s_wpre[w], exc);
+        if (a.renorm) renormalize(P);
+        const float o0 = s_org[0], o1 = s_org[1], o2 = s_org[2];
+        const int j0 = tid * R;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int j = j0 + r;
+            if (j < nreal) {
+                float *o = s_out + 9 * j;
+                o[0] = P.p[0] + o0; o[1] = P.p[1] + o1; o[2] = P.p[2] + o2;
+                apply_joint(P, a.bc.cb[0], a.bc.sb[0], a.bc.d[0], cs[r][0], sn[r][0]);
+                o[3] = P.p[0] + o0; o[4] = P.p[1] + o1; o[5] = P.p[2] + o2;
+                apply_joint(P, a.bc.cb[1], a.bc.sb[1], a.bc.d[1], cs[r][1], sn[r][1]);
+                o[6] = P.p[0] + o0; o[7] = P.p[1] + o1; o[8] = P.p[2] + o2;
+                apply_joint(P, a.bc.cb[2], a.bc.sb[2], a.bc.d[2], cs[r][2], sn[r][2]);
+            }
+        }
+        (void)lane;
+        __syncthreads();
+        store_floats<NT>(out, s_out, 9 * nreal, 9 * ntile);
+        __syncthreads();
+    }
+    finish_launch(&a.hdr->fwd_ticket, &a.hdr->fwd_done, &a.hdr->fwd_epoch);
+}
+
+// ------------------------------------------------------------------ backward
+// Suffix look-back over later tiles of the chain (thread 0 only).  own = this
+// tile's (G, S) with S about the world origin.  Returns the sums over all later
+// tiles.
+__device__ void backward_suffix(const A2bArgs &a, int b, int t, int t_last, const double own[6],
+                                unsigned epoch_bits, double carry[6]) {
+    TileRecord *rc = a.rec + (size_t)b * a.ntiles + t;
+    for (int i = 0; i < 6; i++) carry[i] = 0.0;
+    if (t == t_last) {
+        if (t > 0) {
+            for (int i = 0; i < 6; i++) rc->binc[i] = own[i];
+            st_release(&rc->bflag, epoch_bits | kFlagInc);
+        }
+        return;
+    }
+    if (t > 0) {
+        for (int i = 0; i < 6; i++) rc->bagg[i] = own[i];
+        st_release(&rc->bflag, epoch_bits | kFlagAgg);
+    }
+    bool ok = true;
+    for (int tt = t + 1; tt <= t_last; tt++) {
+        const TileRecord *q = a.rec + (size_t)b * a.ntiles + tt;
+        unsigned f = wait_flag(&q->bflag, epoch_bits, a.hdr, ok);
+        if (!ok) break;
+        if ((f & 3u) == kFlagInc) {
+            for (int i = 0; i < 6; i++) carry[i] += q->binc[i];
+            break;
+        }
+        for (int i = 0; i < 6; i++) carry[i] += q->bagg[i];
+    }
+    if (!ok)
+        for (int i = 0; i < 6; i++) carry[i] = 0.0;
+    if (t > 0) {
+        for (int i = 0; i < 6; i++) rc->binc[i] = own[i] + carry[i];
+        st_release(&rc->bflag, epoch_bits | kFlagInc);
+    }
+}
+
+__device__ __forceinline__ float warp_suffix_exclusive(float v, int lane, float &total) {
+    // inclusive suffix sum: sum over lanes >= lane
+    float inc = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        float o = __shfl_down_sync(0xffffffffu, inc, off);
+        if (lane + off < 32) inc += o;
+    }
+    total = __shfl_sync(0xffffffffu, inc, 0);
+    return inc - v;
+}
+
+template <int R, int NT>
+__global__ void __launch_bounds__(NT) a2b_bwd_f32_kernel(A2bArgs a) {
+    constexpr int TILE = R * NT;
+    constexpr int NW = NT / 32;
+    __shared__ float s_ang[3][TILE];
+    __shared__ float s_g[9 * TILE];
+    __shared__ Frame<float> s_wtot[NW];
+    __shared__ Frame<float> s_wpre[NW];
+    __shared__ float s_wsum[NW][6];
+    __shared__ float s_wsuf[NW][6];
+    __shared__ int s_item;
+    __shared__ unsigned s_epoch, s_fepoch;
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) s_epoch = (*(volatile unsigned *)&a.hdr->bwd_epoch & 0x3fffffffu) << 2;
+
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(&a.hdr->bwd_ticket, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.total) break;
+        const int b = item / a.ntiles, t = a.ntiles - 1 - (item - b * a.ntiles);
+        int len = a.lengths[b];
+        if (len < 0 || len > a.L) {
+            if (tid == 0) record_error(a.hdr, TPL_ERR_LENGTH);
+            len = max(0, min(len, a.L));
+        }
+        const int s0 = t * TILE;
+        const int ntile = min(TILE, a.L - s0);
+        const int nreal = max(0, min(ntile, len - s0));
+        float *gout = a.grad_angles + (size_t)b * 3 * a.L + s0;
+        if (nreal == 0) {
+            for (int k = 0; k < 3; k++) store_floats<NT>(gout + (size_t)k * a.L, s_g, 0, ntile);
+            __syncthreads();
+            continue;
+        }
+        const float *ang = a.angles + (size_t)b * 3 * a.L + s0;
+        load_floats<NT>(s_ang[0], ang, nreal);
+        load_floats<NT>(s_ang[1], ang + a.L, nreal);
+        load_floats<NT>(s_ang[2], ang + 2 * a.L, nreal);
+        load_floats<NT>(s_g, a.grad_coords + (size_t)b * 9 * a.L + (size_t)9 * s0, 9 * nreal);
+        __syncthreads();
+
+        const bool chain_end = (s0 + nreal == len);
+        float cs[R][3], sn[R][3];
+        Frame<float> exc = tile_local_scan<R, NT>(a, s_ang, nreal, chain_end, cs, sn, s_wtot);
+        __syncthreads();
+
+        double org64[3] = {0.0, 0.0, 0.0};
+        if (tid == 0) {
+            Frame<float> run;
+            frame_identity(run);
+            Frame<float> pre[NW];
+#pragma unroll
+            for (int ww = 0; ww < NW; ww++) {
+                pre[ww] = run;
+                run = compose(run, s_wtot[ww]);
+                if (a.renorm) renormalize(run);
+            }
+            Frame<double> carry;
+            if (t == 0) frame_identity(carry);
+            else frame_load(carry, a.rec[(size_t)b * a.ntiles + t].fexc);
+            Frame<float> c32 = frame_cast<float>(carry);
+            c32.p[0] = c32.p[1] = c32.p[2] = 0.f;
+#pragma unroll
+            for (int ww = 0; ww < NW; ww++) s_wpre[ww] = compose(c32, pre[ww]);
+            // tile origin: the forward's positions are (relative position) + float(carry.p)
+            org64[0] = (double)(float)carry.p[0];
+            org64[1] = (double)(float)carry.p[1];
+            org64[2] = (double)(float)carry.p[2];
+        }
+        __syncthreads();
+
+        // walk 2: positions relative to the tile origin, joint axes, thread sums
+        Frame<float> P = compose(s_wpre[w], exc);
+        if (a.renorm) renormalize(P);
+        float x[R][3][3], u[R][3][3], xn[R][3];
+        float G[3] = {0.f, 0.f, 0.f}, S[3] = {0.f, 0.f, 0.f};
+        const int j0 = tid * R;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int j = j0 + r;
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) x[r][q][c] = u[r][q][c] = 0.f;
+                xn[r][q] = 0.f;
+            }
+            if (j < nreal) {
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) x[r][q][c] = P.p[c];
+                    apply_joint(P, a.bc.cb[q], a.bc.sb[q], a.bc.d[q], cs[r][q], sn[r][q]);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) u[r][q][c] = P.r[3 * c];
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++) xn[r][c] = P.p[c];
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    const float *g = s_g + 9 * j + 3 * q;
+                    float xg[3];
+                    cross3(x[r][q], g, xg);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += g[c];
+                        S[c] += xg[c];
+                    }
+                }
+            }
+        }
+        // block-exclusive suffix of (G, S) over threads
+        float suf[6], wt[6];
+        const float v[6] = {G[0], G[1], G[2], S[0], S[1], S[2]};
+#pragma unroll
+        for (int i = 0; i < 6; i++) suf[i] = warp_suffix_exclusive(v[i], lane, wt[i]);
+        if (lane == 0)
+#pragma unroll
+            for (int i = 0; i < 6; i++) s_wsum[w][i] = wt[i];
+        __syncthreads();
+        if (tid == 0) {
+            double tot[6] = {0, 0, 0, 0, 0, 0};
+            for (int ww = 0; ww < NW; ww++)
+                for (int i = 0; i < 6; i++) tot[i] += (double)s_wsum[ww][i];
+            // S about the world origin: S_world = S_o + o x G
+            double own[6], oxg[3];
+            cross3(org64, tot, oxg);
+            for (int i = 0; i < 3; i++) {
+                own[i] = tot[i];
+                own[3 + i] = tot[3 + i] + oxg[i];
+            }
+            const int t_last = (len - 1) / TILE;
+            double cw[6];
+            backward_suffix(a, b, t, t_last, own, s_epoch, cw);
+            // back to the tile origin: S_o = S_world - o x G
+            double oxc[3];
+            cross3(org64, cw, oxc);
+            float run[6];
+            for (int i = 0; i < 3; i++) {
+                run[i] = (float)cw[i];
+                run[3 + i] = (float)(cw[3 + i] - oxc[i]);
+            }
+            for (int ww = NW - 1; ww >= 0; ww--)
+                for (int i = 0; i < 6; i++) {
+                    s_wsuf[ww][i] = run[i];
+                    run[i] += s_wsum[ww][i];
+                }
+        }
+        __syncthreads();
+        // walk 3: residues in reverse with the running suffix (atoms after residue j)
+        float Gr[3], Sr[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            Gr[c] = suf[c] + s_wsuf[w][c];
+            Sr[c] = suf[3 + c] + s_wsuf[w][3 + c];
+        }
+        float(*s_gr)[TILE] = s_ang;  // angles are no longer needed: stage gradients there
+#pragma unroll
+        for (int r = R - 1; r >= 0; r--) {
+            const int j = j0 + r;
+            if (j < nreal) {
+                float tmp[3], cr[3];
+                // omega_j: axis u[r][2], origin = N_{j+1}
+                cross3(xn[r], Gr, cr);
+                for (int c = 0; c < 3; c++) tmp[c] = Sr[c] - cr[c];
+                const float gom = u[r][2][0] * tmp[0] + u[r][2][1] * tmp[1] + u[r][2][2] * tmp[2];
+                // psi_j: axis u[r][1], origin C_j (same atom set: everything from N_{j+1})
+                cross3(x[r][2], Gr, cr);
+                for (int c = 0; c < 3; c++) tmp[c] = Sr[c] - cr[c];
+                const float gps = u[r][1][0] * tmp[0] + u[r][1][1] * tmp[1] + u[r][1][2] * tmp[2];
+                // add C_j
+                {
+                    const float *g = s_g + 9 * j + 6;
+                    cross3(x[r][2], g, cr);
+                    for (int c = 0; c < 3; c++) {
+                        Gr[c] += g[c];
+                        Sr[c] += cr[c];
+                    }
+                }
+                // phi_j: axis u[r][0], origin CA_j
+                cross3(x[r][1], Gr, cr);
+                for (int c = 0; c < 3; c++) tmp[c] = Sr[c] - cr[c];
+                const float gph = u[r][0][0] * tmp[0] + u[r][0][1] * tmp[1] + u[r][0][2] * tmp[2];
+                // add CA_j and N_j
+                for (int q = 1; q >= 0; q--) {
+                    const float *g = s_g + 9 * j + 3 * q;
+                    cross3(x[r][q], g, cr);
+                    for (int c = 0; c < 3; c++) {
+                        Gr[c] += g[c];
+                        Sr[c] += cr[c];
+                    }
+                }
+                const bool last = chain_end && (j == nreal - 1);
+                s_gr[0][j] = gph;
+                s_gr[1][j] = last ? 0.f : gps;
+                s_gr[2][j] = last ? 0.f : gom;
+            }
+        }
+        __syncthreads();
+        for (int k = 0; k < 3; k++) store_floats<NT>(gout + (size_t)k * a.L, s_gr[k], nreal, ntile);
+        __syncthreads();
+    }
+    (void)s_fepoch;
+    finish_launch(&a.hdr->bwd_ticket, &a.hdr->bwd_done, &a.hdr->bwd_epoch);
+}
+
+// ----------------------------------------------------------- plain FP64 form
+// One chain per CTA, one residue per thread per chunk, Hillis-Steele block scan
+// of residue transforms in shared memory, carry between chunks in registers.
+constexpr int kPlainThreads = 256;
+
+struct PlainArgs {
+    const double *angles;
+    const int *lengths;
+    double *coords;
+    double *grad_angles;
+    const double *grad_coords;
+    WsHeader *hdr;
+    TileRecord *rec;
+    int L, nchunks;
+    BondConsts bc;
+};
+
+__device__ __forceinline__ Frame<double> plain_residue(const PlainArgs &a, const double *ang, int j, int len,
+                                                       double cs[3], double sn[3]) {
+    Frame<double> T;
+    frame_identity(T);
+    for (int k = 0; k < 3; k++) {
+        cs[k] = 1.0;
+        sn[k] = 0.0;
+    }
+    if (j < len) {
+        for (int k = 0; k < 3; k++) {
+            if (k == 2 && j == len - 1) break;
+            sincos(ang[(size_t)k * a.L + j], &sn[k], &cs[k]);
+            apply_joint(T, a.bc.cbd[k], a.bc.sbd[k], a.bc.dd[k], cs[k], sn[k]);
+        }
+    }
+    return T;
+}
+
+// Inclusive block scan of frames (Hillis-Steele); returns the exclusive prefix.
+__device__ __forceinline__ Frame<double> plain_block_scan(Frame<double> T, Frame<double> *s, Frame<double> &total) {
+    const int tid = threadIdx.x;
+    s[tid] = T;
+    __syncthreads();
+    for (int off = 1; off < kPlainThreads; off <<= 1) {
+        Frame<double> o;
+        if (tid >= off) o = s[tid - off];
+        __syncthreads();
+        if (tid >= off) {
+            T = compose(o, T);
+            s[tid] = T;
+        }
+        __syncthreads();
+    }
+    Frame<double> exc;
+    if (tid == 0) frame_identity(exc);
+    else exc = s[tid - 1];
+    total = s[kPlainThreads - 1];
+    __syncthreads();
+    return exc;
+}
+
+__global__ void __launch_bounds__(kPlainThreads) a2b_fwd_f64_plain_kernel(PlainArgs a) {
+    __shared__ Frame<double> s_scan[kPlainThreads];
+    const int b = blockIdx.x, tid = threadIdx.x;
+    int len = a.lengths[b];
+    if (len < 0 || len > a.L) {
+        if (tid == 0 && a.hdr) record_error(a.hdr, TPL_ERR_LENGTH);
+        len = max(0, min(len, a.L));
+    }
+    const double *ang = a.angles + (size_t)b * 3 * a.L;
+    double *out = a.coords + (size_t)b * 9 * a.L;
+    Frame<double> carry;
+    frame_identity(carry);
+    for (int s0 = 0; s0 < a.L; s0 += kPlainThreads) {
+        const int j = s0 + tid;
+        double cs[3], sn[3];
+        Frame<double> T = plain_residue(a, ang, j, len, cs, sn);
+        Frame<double> total;
+        Frame<double> exc = plain_block_scan(T, s_scan, total);
+        Frame<double> P = compose(carry, exc);
+        if (j < len) {
+            double *o = out + (size_t)9 * j;
+            for (int q = 0; q < 3; q++) {
+                o[3 * q] = P.p[0]; o[3 * q + 1] = P.p[1]; o[3 * q + 2] = P.p[2];
+                apply_joint(P, a.bc.cbd[q], a.bc.sbd[q], a.bc.dd[q], cs[q], sn[q]);
+            }
+        } else if (j < a.L) {
+            double *o = out + (size_t)9 * j;
+            for (int q = 0; q < 9; q++) o[q] = 0.0;
+        }
+        carry = compose(carry, total);
+    }
+}
+
+__global__ void __launch_bounds__(kPlainThreads) a2b_bwd_f64_plain_kernel(PlainArgs a) {
+    __shared__ Frame<double> s_scan[kPlainThreads];
+    __shared__ double s_sum[kPlainThreads][6];
+    const int b = blockIdx.x, tid = threadIdx.x;
+    int len = a.lengths[b];
+    if (len < 0 || len > a.L) {
+        if (tid == 0 && a.hdr) record_error(a.hdr, TPL_ERR_LENGTH);
+        len = max(0, min(len, a.L));
+    }
+    const double *ang = a.angles + (size_t)b * 3 * a.L;
+    const double *gc = a.grad_coords + (size_t)b * 9 * a.L;
+    double *gout = a.grad_angles + (size_t)b * 3 * a.L;
+    TileRecord *rec = a.rec + (size_t)b * a.nchunks;
+    // pass 1: chunk carries
+    Frame<double> carry;
+    frame_identity(carry);
+    for (int c = 0; c < a.nchunks; c++) {
+        if (tid == 0) frame_store(rec[c].fexc, carry);
+        const int j = c * kPlainThreads + tid;
+        double cs[3], sn[3];
+        Frame<double> T = plain_residue(a, ang, j, len, cs, sn);
+        Frame<double> total;
+        plain_block_scan(T, s_scan, total);
+        carry = compose(carry, total);
+    }
+    __syncthreads();
+    // pass 2: chunks last-first with the running suffix (G, S) about the world origin
+    double Gc[3] = {0, 0, 0}, Sc[3] = {0, 0, 0};
+    for (int c = a.nchunks - 1; c >= 0; c--) {
+        const int j = c * kPlainThreads + tid;
+        double cs[3], sn[3];
+        Frame<double> T = plain_residue(a, ang, j, len, cs, sn);
+        Frame<double> total, start;
+        Frame<double> exc = plain_block_scan(T, s_scan, total);
+        frame_load(start, rec[c].fexc);
+        Frame<double> P = compose(start, exc);
+        double x[3][3], u[3][3], xn[3];
+        double G[3] = {0, 0, 0}, S[3] = {0, 0, 0};
+        if (j < len) {
+            for (int q = 0; q < 3; q++) {
+                for (int k = 0; k < 3; k++) x[q][k] = P.p[k];
+                apply_joint(P, a.bc.cbd[q], a.bc.sbd[q], a.bc.dd[q], cs[q], sn[q]);
+                for (int k = 0; k < 3; k++) u[q][k] = P.r[3 * k];
+            }
+            for (int k = 0; k < 3; k++) xn[k] = P.p[k];
+            for (int q = 0; q < 3; q++) {
+                const double *g = gc + (size_t)9 * j + 3 * q;
+                double xg[3];
+                cross3(x[q], g, xg);
+                for (int k = 0; k < 3; k++) {
+                    G[k] += g[k];
+                    S[k] += xg[k];
+                }
+            }
+        }
+        // exclusive suffix over threads (Hillis-Steele on sums, reversed)
+        double v[6] = {G[0], G[1], G[2], S[0], S[1], S[2]};
+        for (int i = 0; i < 6; i++) s_sum[tid][i] = v[i];
+        __syncthreads();
+        for (int off = 1; off < kPlainThreads; off <<= 1) {
+            double o[6];
+            const bool has = tid + off < kPlainThreads;
+            if (has)
+                for (int i = 0; i < 6; i++) o[i] = s_sum[tid + off][i];
+            __syncthreads();
+            if (has)
+                for (int i = 0; i < 6; i++) {
+                    v[i] += o[i];
+                    s_sum[tid][i] = v[i];
+                }
+            __syncthreads();
+        }
+        double Gr[3], Sr[3], chunk_tot[6];
+        for (int i = 0; i < 6; i++) chunk_tot[i] = s_sum[0][i];
+        for (int k = 0; k < 3; k++) {
+            const double nxt_g = tid + 1 < kPlainThreads ? s_sum[tid + 1][k] : 0.0;
+            const double nxt_s = tid + 1 < kPlainThreads ? s_sum[tid + 1][3 + k] : 0.0;
+            Gr[k] = nxt_g + Gc[k];
+            Sr[k] = nxt_s + Sc[k];
+        }
+        __syncthreads();
+        if (j < len) {
+            double tmp[3], cr[3];
+            cross3(xn, Gr, cr);
+            for (int k = 0; k < 3; k++) tmp[k] = Sr[k] - cr[k];
+            const double gom = u[2][0] * tmp[0] + u[2][1] * tmp[1] + u[2][2] * tmp[2];
+            cross3(x[2], Gr, cr);
+            for (int k = 0; k < 3; k++) tmp[k] = Sr[k] - cr[k];
+            const double gps = u[1][0] * tmp[0] + u[1][1] * tmp[1] + u[1][2] * tmp[2];
+            const double *g = gc + (size_t)9 * j + 6;
+            cross3(x[2], g, cr);
+            for (int k = 0; k < 3; k++) {
+                Gr[k] += g[k];
+                Sr[k] += cr[k];
+            }
+            cross3(x[1], Gr, cr);
+            for (int k = 0; k < 3; k++) tmp[k] = Sr[k] - cr[k];
+            const double gph = u[0][0] * tmp[0] + u[0][1] * tmp[1] + u[0][2] * tmp[2];
+            const bool last = (j == len - 1);
+            gout[j] = gph;
+            gout[(size_t)a.L + j] = last ? 0.0 : gps;
+            gout[(size_t)2 * a.L + j] = last ? 0.0 : gom;
+        } else if (j < a.L) {
+            gout[j] = gout[(size_t)a.L + j] = gout[(size_t)2 * a.L + j] = 0.0;
+        }
+        for (int i = 0; i < 3; i++) {
+            Gc[i] += chunk_tot[i];
+            Sc[i] += chunk_tot[3 + i];
+        }
+    }
+}
+
+// ------------------------------------------------------------------- host side
+template <typename K>
+static int persistent_grid(K kernel, int threads, int items, int max_ctas) {
+    static int num_sms = 0;
+    if (!num_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (num_sms <= 0) num_sms = 1;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int grid = num_sms * per_sm;
+    if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+    if (grid > items) grid = items;
+    return grid < 1 ? 1 : grid;
+}
+
+struct A2bShape {
+    int R, NT;
+};
+
+// Forward: NT = 128 threads, R residues each.  Backward: same tile (it re-reads
+// the forward's per-tile carries) with half the residues per thread and twice
+// the threads, because each backward thread keeps 18 R positions and axes live.
+static A2bShape a2b_shape(const tpl_options &opt, bool backward) {
+    A2bShape s;
+    const int rf = opt.residues_per_thread > 0 ? opt.residues_per_thread : 4;
+    if (!backward || rf == 1) {
+        s.R = rf;
+        s.NT = 128;
+    } else {
+        s.R = rf / 2;
+        s.NT = 256;
+    }
+    return s;
+}
+
+int a2b_tile_for(const tpl_options &opt) {
+    A2bShape f = a2b_shape(opt, false);
+    return f.R * f.NT;
+}
+
+static A2bArgs make_args(const float *angles, const int32_t *lengths, void *ws, int B, int L, int tile,
+                         const tpl_options &opt) {
+    A2bArgs a;
+    a.angles = angles;
+    a.lengths = lengths;
+    a.coords = nullptr;
+    a.grad_angles = nullptr;
+    a.grad_coords = nullptr;
+    a.hdr = reinterpret_cast<WsHeader *>(ws);
+    a.rec = reinterpret_cast<TileRecord *>(reinterpret_cast<char *>(ws) + sizeof(WsHeader));
+    a.L = L;
+    a.ntiles = (L + tile - 1) / tile;
+    a.total = B * a.ntiles;
+    a.fp64_min_len = opt.fp64_carry_min_len == 0 ? 0 : opt.fp64_carry_min_len;
+    a.renorm = opt.renormalize >= 0 ? 1 : 0;
+    a.bc = bond_constants();
+    return a;
+}
+
+template <int R>
+static int launch_fwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
+    auto k = a2b_fwd_f32_kernel<R, 128>;
+    int grid = persistent_grid(k, 128, a.total, max_ctas);
+    k<<<grid, 128, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+template <int R, int NT>
+static int launch_bwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
+    auto k = a2b_bwd_f32_kernel<R, NT>;
+    int grid = persistent_grid(k, NT, a.total, max_ctas);
+    k<<<grid, NT, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, void *ws, int B, int L,
+                    const tpl_options &opt, cudaStream_t st) {
+    if (B == 0 || L == 0) return TPL_OK;
+    A2bShape s = a2b_shape(opt, false);
+    A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
+    a.coords = coords;
+    switch (s.R) {
+        case 1: return launch_fwd<1>(a, opt.max_ctas, st);
+        case 2: return launch_fwd<2>(a, opt.max_ctas, st);
+        case 4: return launch_fwd<4>(a, opt.max_ctas, st);
+        case 8: return launch_fwd<8>(a, opt.max_ctas, st);
+    }
+    return TPL_ERR_UNSUPPORTED;
+}
+
+int a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
+                     void *ws, int B, int L, const tpl_options &opt, cudaStream_t st) {
+    if (B == 0 || L == 0) return TPL_OK;
+    A2bShape s = a2b_shape(opt, true);
+    A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
+    a.grad_angles = grad_angles;
+    a.grad_coords = grad_coords;
+    if (s.NT == 128 && s.R == 1) return launch_bwd<1, 128>(a, opt.max_ctas, st);
+    if (s.NT == 256 && s.R == 1) return launch_bwd<1, 256>(a, opt.max_ctas, st);
+    if (s.NT == 256 && s.R == 2) return launch_bwd<2, 256>(a, opt.max_ctas, st);
+    if (s.NT == 256 && s.R == 4) return launch_bwd<4, 256>(a, opt.max_ctas, st);
+    return TPL_ERR_UNSUPPORTED;
+}
+
+int a2b_forward_f64_plain(const double *angles, const int32_t *lengths, double *coords, int B, int L,
+                          cudaStream_t st) {
+    if (B == 0 || L == 0) return TPL_OK;
+    PlainArgs a{};
+    a.angles = angles;
+    a.lengths = lengths;
+    a.coords = coords;
+    a.hdr = nullptr;
+    a.rec = nullptr;
+    a.L = L;
+    a.nchunks = (L + kPlainThreads - 1) / kPlainThreads;
+    a.bc = bond_constants();
+    a2b_fwd_f64_plain_kernel<<<B, kPlainThreads, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+int a2b_backward_f64_plain(double *grad_angles, const double *grad_coords, const double *angles,
+                           const int32_t *lengths, void *ws, int B, int L, cudaStream_t st) {
+    if (B == 0 || L == 0) return TPL_OK;
+    PlainArgs a{};
+    a.angles = angles;
+    a.lengths = lengths;
+    a.grad_angles = grad_angles;
+    a.grad_coords = grad_coords;
+    a.hdr = reinterpret_cast<WsHeader *>(ws);
+    a.rec = reinterpret_cast<TileRecord *>(reinterpret_cast<char *>(ws) + sizeof(WsHeader));
+    a.L = L;
+    a.nchunks = (L + kPlainThreads - 1) / kPlainThreads;
+    a.bc = bond_constants();
+    a2b_bwd_f64_plain_kernel<<<B, kPlainThreads, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+}  // namespace tpl

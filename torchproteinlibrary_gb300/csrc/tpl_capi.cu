@@ -1,0 +1,198 @@
+// extern "C" entry points of libtpl_gb300.so (declared in include/tpl_gb300.h).
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "tpl_internal.h"
+
+namespace tpl {
+
+// Backbone bond geometry, Layers/ReducedModel/cBackboneProteinCPUKernels.cpp:6-12:
+// joint phi:   N->CA, bond angle beta = pi - 1.9391, length 1.460
+// joint psi:   CA->C, beta = pi - 2.061,  length 1.525
+// joint omega: C->N,  beta = pi - 2.1186, length 1.330
+static const double kBeta[3] = {M_PI - 1.9391, M_PI - 2.061, M_PI - 2.1186};
+static const double kBond[3] = {1.460, 1.525, 1.330};
+
+// FP32 (cos, sin) pairs of the three backbone bond angles.
+//
+// Rounding cos(beta) and sin(beta) to FP32 independently leaves the pair's norm
+// off 1 by up to ~3e-8.  Every residue applies the same three pairs, so the
+// frames of an FP32 chain shrink or grow coherently (about -2.6e-8 per residue
+// for the nearest-rounded pairs) and positions drift by ~1e-3 A over 1000
+// residues.  Among pairs within a few ulps of (cos, sin) beta whose angle is
+// still within 4e-8 rad and whose own norm error is below 3e-8, pick the triple
+// whose norm errors cancel over a residue.
+static void pick_fp32_pairs(float cb[3], float sb[3]) {
+    struct Cand {
+        float c, s;
+        double ang_err, norm_err;
+    };
+    Cand cand[3][64];
+    int nc[3] = {0, 0, 0};
+    for (int k = 0; k < 3; k++) {
+        const double c0 = std::cos(kBeta[k]), s0 = std::sin(kBeta[k]);
+        const float cf = (float)c0, sf = (float)s0;
+        for (int i = -3; i <= 3; i++)
+            for (int j = -3; j <= 3; j++) {
+                float c = cf, s = sf;
+                for (int q = 0; q < (i < 0 ? -i : i); q++) c = std::nextafter(c, i < 0 ? -2.f : 2.f);
+                for (int q = 0; q < (j < 0 ? -j : j); q++) s = std::nextafter(s, j < 0 ? -2.f : 2.f);
+                const double ae = std::atan2((double)s, (double)c) - kBeta[k];
+                const double ne = std::hypot((double)c, (double)s) - 1.0;
+                if (std::fabs(ae) < 4e-8 && std::fabs(ne) < 3e-8 && nc[k] < 64) cand[k][nc[k]++] = {c, s, ae, ne};
+            }
+        if (nc[k] == 0) cand[k][nc[k]++] = {cf, sf, 0.0, 0.0};
+    }
+    double best = 1e30, best_ang = 1e30;
+    int bi[3] = {0, 0, 0};
+    for (int a = 0; a < nc[0]; a++)
+        for (int b = 0; b < nc[1]; b++)
+            for (int c = 0; c < nc[2]; c++) {
+                const double tot = std::fabs(cand[0][a].norm_err + cand[1][b].norm_err + cand[2][c].norm_err);
+                const double ang = std::fabs(cand[0][a].ang_err) + std::fabs(cand[1][b].ang_err) +
+                                   std::fabs(cand[2][c].ang_err);
+                if (tot < best - 1e-15 || (std::fabs(tot - best) <= 1e-15 && ang < best_ang)) {
+                    best = tot;
+                    best_ang = ang;
+                    bi[0] = a; bi[1] = b; bi[2] = c;
+                }
+            }
+    for (int k = 0; k < 3; k++) {
+        cb[k] = cand[k][bi[k]].c;
+        sb[k] = cand[k][bi[k]].s;
+    }
+}
+
+const BondConsts &bond_constants() {
+    static BondConsts bc = [] {
+        BondConsts c{};
+        pick_fp32_pairs(c.cb, c.sb);
+        for (int k = 0; k < 3; k++) {
+            c.d[k] = (float)kBond[k];
+            c.cbd[k] = std::cos(kBeta[k]);
+            c.sbd[k] = std::sin(kBeta[k]);
+            c.dd[k] = kBond[k];
+        }
+        return c;
+    }();
+    return bc;
+}
+
+static tpl_options resolve(const tpl_options *opt) {
+    tpl_options o{};
+    if (opt) o = *opt;
+    return o;
+}
+
+static bool options_ok(const tpl_options &o) {
+    const int r = o.residues_per_thread;
+    if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8)) return false;
+    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128)) return false;
+    if (o.max_ctas < 0) return false;
+    return true;
+}
+
+static size_t a2b_ws(int B, int L, const tpl_options &o) {
+    const int tile = a2b_tile_for(o);
+    const int plain_chunk = 256;
+    const int smallest = tile < plain_chunk ? tile : plain_chunk;
+    return ws_bytes_for(B, (L + smallest - 1) / smallest);
+}
+
+}  // namespace tpl
+
+using namespace tpl;
+
+extern "C" {
+
+const char *tpl_status_string(int status) {
+    switch (status) {
+        case TPL_OK: return "ok";
+        case TPL_ERR_ARGUMENT: return "invalid argument";
+        case TPL_ERR_WORKSPACE: return "workspace missing, misaligned or too small";
+        case TPL_ERR_LAUNCH: return "CUDA kernel launch failed";
+        case TPL_ERR_LENGTH: return "chain length outside [0, max_len]";
+        case TPL_ERR_SEQUENCE: return "unknown residue letter";
+        case TPL_ERR_LOOKBACK_TIMEOUT: return "inter-tile look-back wait timed out";
+        case TPL_ERR_ATOMS: return "chain has more atoms than max_atoms";
+        case TPL_ERR_UNSUPPORTED: return "unsupported option combination";
+    }
+    return "unknown status";
+}
+
+int tpl_version(void) { return 100; }
+
+size_t tpl_a2b_workspace_bytes(int batch, int max_len, const tpl_options *opt) {
+    if (batch < 0 || max_len < 0) return 0;
+    return a2b_ws(batch, max_len, resolve(opt));
+}
+
+int tpl_workspace_init(void *workspace, size_t workspace_bytes, void *stream) {
+    if (!workspace || workspace_bytes < sizeof(WsHeader)) return TPL_ERR_WORKSPACE;
+    cudaError_t e = cudaMemsetAsync(workspace, 0, workspace_bytes, (cudaStream_t)stream);
+    return e == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+int tpl_workspace_status(void *workspace, void *stream, int *status_out) {
+    if (!workspace || !status_out) return TPL_ERR_ARGUMENT;
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return TPL_ERR_LAUNCH;
+    unsigned v = 0;
+    if (cudaMemcpy(&v, workspace, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return TPL_ERR_LAUNCH;
+    if (v != 0 && cudaMemset(workspace, 0, sizeof(unsigned)) != cudaSuccess) return TPL_ERR_LAUNCH;
+    *status_out = (int)v;
+    return TPL_OK;
+}
+
+static int check_ws(const void *ws, size_t bytes, size_t need) {
+    if (!ws || bytes < need || ((uintptr_t)ws & 15u)) return TPL_ERR_WORKSPACE;
+    return TPL_OK;
+}
+
+int tpl_a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, void *workspace,
+                        size_t workspace_bytes, int batch, int max_len, const tpl_options *opt, void *stream) {
+    if (batch < 0 || max_len < 0) return TPL_ERR_ARGUMENT;
+    const tpl_options o = resolve(opt);
+    if (!options_ok(o)) return TPL_ERR_ARGUMENT;
+    if (batch == 0 || max_len == 0) return TPL_OK;
+    if (!angles || !lengths || !coords) return TPL_ERR_ARGUMENT;
+    int s = check_ws(workspace, workspace_bytes, a2b_ws(batch, max_len, o));
+    if (s) return s;
+    return a2b_forward_f32(angles, lengths, coords, workspace, batch, max_len, o, (cudaStream_t)stream);
+}
+
+int tpl_a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles,
+                         const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         const tpl_options *opt, void *stream) {
+    if (batch < 0 || max_len < 0) return TPL_ERR_ARGUMENT;
+    const tpl_options o = resolve(opt);
+    if (!options_ok(o)) return TPL_ERR_ARGUMENT;
+    if (batch == 0 || max_len == 0) return TPL_OK;
+    if (!grad_angles || !grad_coords || !angles || !lengths) return TPL_ERR_ARGUMENT;
+    int s = check_ws(workspace, workspace_bytes, a2b_ws(batch, max_len, o));
+    if (s) return s;
+    return a2b_backward_f32(grad_angles, grad_coords, angles, lengths, workspace, batch, max_len, o,
+                            (cudaStream_t)stream);
+}
+
+int tpl_a2b_forward_f64(const double *angles, const int32_t *lengths, double *coords, int batch, int max_len,
+                        void *stream) {
+    if (batch < 0 || max_len < 0) return TPL_ERR_ARGUMENT;
+    if (batch == 0 || max_len == 0) return TPL_OK;
+    if (!angles || !lengths || !coords) return TPL_ERR_ARGUMENT;
+    return a2b_forward_f64_plain(angles, lengths, coords, batch, max_len, (cudaStream_t)stream);
+}
+
+int tpl_a2b_backward_f64(double *grad_angles, const double *grad_coords, const double *angles,
+                         const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         void *stream) {
+    if (batch < 0 || max_len < 0) return TPL_ERR_ARGUMENT;
+    if (batch == 0 || max_len == 0) return TPL_OK;
+    if (!grad_angles || !grad_coords || !angles || !lengths) return TPL_ERR_ARGUMENT;
+    int s = check_ws(workspace, workspace_bytes, ws_bytes_for(batch, (max_len + 255) / 256));
+    if (s) return s;
+    return a2b_backward_f64_plain(grad_angles, grad_coords, angles, lengths, workspace, batch, max_len,
+                                  (cudaStream_t)stream);
+}
+
+}  // extern "C"

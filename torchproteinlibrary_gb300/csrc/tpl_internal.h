@@ -1,0 +1,65 @@
+// Host-side declarations shared by the C-ABI layer and the kernel files.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/tpl_gb300.h"
+
+namespace tpl {
+
+// FP32 / FP64 (cos, sin) of the three backbone bond angles plus the bond lengths,
+// in joint order phi (N->CA), psi (CA->C), omega (C->N).  The FP32 pairs are picked
+// by bond_constants() so that the rounding errors of their norms cancel over a
+// residue (see tpl_capi.cu).
+struct BondConsts {
+    float cb[3], sb[3], d[3];
+    double cbd[3], sbd[3], dd[3];
+};
+const BondConsts &bond_constants();
+
+// Workspace header, shared by all launches that use one workspace buffer.  The
+// ticket / done / epoch words make each persistent launch self-resetting, so that
+// launches can be replayed from a CUDA graph without a memset.
+struct WsHeader {
+    unsigned status;      // first error code (tpl_status), 0 = ok
+    unsigned fwd_ticket, fwd_done, fwd_epoch;
+    unsigned bwd_ticket, bwd_done, bwd_epoch;
+    unsigned tile;        // residues per tile used by the last forward
+    unsigned test_skip_publish;  // fault injection for tests: 1 = chain 0, tile 0 never publishes
+    unsigned pad[7];
+};
+static_assert(sizeof(WsHeader) == 64, "header size");
+
+// Per (chain, tile) record of the decoupled look-back.
+struct __align__(16) TileRecord {
+    unsigned fflag, bflag, atoms, pad;  // atoms: residue-atom count carried by full-atom tiles
+    double fagg[12];  // tile aggregate transform (forward)
+    double finc[12];  // inclusive prefix transform through this tile
+    double fexc[12];  // carry the forward used for this tile (read back by the backward)
+    double bagg[6];   // tile sums (G, S) of the adjoint (backward)
+    double binc[6];   // inclusive suffix sums from this tile to the chain end
+};
+
+inline size_t ws_bytes_for(int B, int ntiles) {
+    return sizeof(WsHeader) + sizeof(TileRecord) * (size_t)B * (size_t)ntiles;
+}
+
+struct LaunchShape {
+    int tile;       // residues per tile
+    int threads;    // threads per CTA
+    int grid;       // persistent CTAs
+};
+
+// Angles2Backbone launchers (tpl_a2b.cu); all return a tpl_status.
+int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, void *ws, int B, int L,
+                    const tpl_options &opt, cudaStream_t st);
+int a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
+                     void *ws, int B, int L, const tpl_options &opt, cudaStream_t st);
+int a2b_forward_f64_plain(const double *angles, const int32_t *lengths, double *coords, int B, int L,
+                          cudaStream_t st);
+int a2b_backward_f64_plain(double *grad_angles, const double *grad_coords, const double *angles,
+                           const int32_t *lengths, void *ws, int B, int L, cudaStream_t st);
+int a2b_tile_for(const tpl_options &opt);
+
+}  // namespace tpl
