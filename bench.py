@@ -68,23 +68,34 @@ class ClockSampler:
         self._t = None
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0 and out.stdout.strip():
-                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        # one streaming nvidia-smi (-lms) for the whole timed region
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        for line in self._proc.stdout:
+            if line.strip():
+                self.samples.append([x.strip() for x in line.strip().split(",")])
+            if self._stop.is_set():
+                break
 
     def __enter__(self):
+        self._proc = None
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
+        time.sleep(0.3)  # let the first sample arrive before the timed region
         return self
 
     def __exit__(self, *a):
         self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         if self._t:
             self._t.join(timeout=10)
 
@@ -94,7 +105,8 @@ class ClockSampler:
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
@@ -184,10 +196,11 @@ def run_ours(args):
 
     rm = load_extension("_ReducedModel")
     ang_np, len_np, up_np = make_inputs(seed=1005 + rank)  # weak scaling: a full batch per GPU
+    ang_np, len_np, up_np = ang_np[:args.chains], len_np[:args.chains], up_np[:args.chains]
     ang = torch.from_numpy(ang_np).to(dev)
     lengths = torch.from_numpy(len_np).to(dev)
     up = torch.from_numpy(up_np).to(dev)
-    B, L = B_CHAINS, L_RES
+    B, L = ang.shape[0], L_RES
     ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
     coords = torch.empty(B, 9 * L, device=dev)
     gang = torch.empty(B, 3, L, device=dev)
@@ -246,14 +259,15 @@ def run_ours(args):
     residues = B * L * args.steps * world
     value = residues / (ms / 1e3)
 
-    # correctness of this very run against the FP64 plain form on a slice
-    check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
-
-    # plain FP64 form on the same workload (the drop-in denominator)
-    plain = time_plain_fp64(rm, ang, lengths, up, dev, steps=max(1, min(3, args.steps)))
-
-    # e2e: public autograd layer, host (pinned) inputs in, results back to the host
-    e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(1, min(5, args.steps)))
+    if args.no_extras:
+        check = plain = e2e = None
+    else:
+        # correctness of this very run against the FP64 plain form on a slice
+        check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
+        # plain FP64 form on the same workload (the drop-in denominator)
+        plain = time_plain_fp64(rm, ang, lengths, up, dev, steps=max(1, min(3, args.steps)))
+        # e2e: public autograd layer, host (pinned) inputs in, results back to the host
+        e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(1, min(5, args.steps)))
 
     peak, peak_kind = peaks()
     fwd_ms, bwd_ms = statistics.mean(t_f), statistics.mean(t_b)
@@ -284,7 +298,7 @@ def run_ours(args):
     }
     if rank == 0:
         line["clocks"] = clk.summary()
-        line["cpu_baseline"] = cpu_baseline_entry()
+        line["cpu_baseline"] = None if args.no_extras else cpu_baseline_entry()
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
@@ -293,6 +307,7 @@ def run_ours(args):
 def accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev, n=256):
     import torch
 
+    n = min(n, ang.shape[0])
     a64 = ang[:n].double().contiguous()
     ln = lengths[:n].contiguous()
     c64 = torch.empty(n, 9 * L_RES, dtype=torch.float64, device=dev)
@@ -382,6 +397,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--chains", type=int, default=B_CHAINS,
+                    help="chains per GPU (smaller batches are for profiling; the metric uses 4096)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "ours" else args.warmup
     if args.impl == "reference":

@@ -109,6 +109,48 @@ int tpl_a2b_backward_f64(double *grad_angles, const double *grad_coords, const d
                          const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch, int max_len,
                          void *stream);
 
+/* Heavy atoms of a NUL-terminated one-letter sequence (host), or TPL_ERR_SEQUENCE
+ * for a letter outside the 20 standard residues.  Replaces getSeqNumAtoms
+ * (Layers/FullAtomModel/Angles2Coords/angles2coords_interface.cpp:139-144,
+ * Math/nUtil.cpp:174-190; no terminal OXT). */
+int tpl_num_atoms(const char *sequence);
+
+/* Workspace bytes for the Angles2Coords entry points (a status word; the
+ * full-atom kernels keep their carries on chip). */
+size_t tpl_a2c_workspace_bytes(int batch, int max_len, int max_atoms, const tpl_options *opt);
+
+/* Angles2Coords forward.  Replaces Angles2Coords_forward
+ * (Layers/FullAtomModel/Angles2Coords/angles2coords_interface.cpp:8-74) with a GPU
+ * path (the reference runs it on the CPU only).
+ *   sequences  [batch, seq_stride] uint8, one NUL-terminated one-letter sequence per
+ *              row (the chain length is the position of the NUL, at most max_len)
+ *   angles     [batch, 8, max_len] rows phi, psi, omega, chi1..chi5; omega[i] is the
+ *              dihedral between residues i and i+1
+ *   coords     [batch, 3 * max_atoms] heavy-atom xyz in the reference's atom order,
+ *              zero past each chain's atoms
+ *   res_names, atom_names  [batch, max_atoms, 4] uint8 NUL-padded names, or both NULL
+ *              to skip them (they depend on the sequences only)
+ * Unknown letters, chains longer than max_len or with more than max_atoms atoms are
+ * reported through the workspace status; such chains are zeroed. */
+int tpl_a2c_forward_f32(const uint8_t *sequences, int seq_stride, const float *angles, float *coords,
+                        uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes, int batch,
+                        int max_len, int max_atoms, const tpl_options *opt, void *stream);
+int tpl_a2c_forward_f64(const uint8_t *sequences, int seq_stride, const double *angles, double *coords,
+                        uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes, int batch,
+                        int max_len, int max_atoms, const tpl_options *opt, void *stream);
+
+/* Angles2Coords backward.  Replaces Angles2Coords_backward
+ * (angles2coords_interface.cpp:76-115, cConformation.cpp:180-211): writes
+ * dL/dangles [batch, 8, max_len] (overwritten) from dL/dcoords [batch, 3 * max_atoms].
+ * Angles without a joint (omega of the last residue, chi angles a residue does not
+ * have, Ala's chi1) and padding get 0, as in the reference. */
+int tpl_a2c_backward_f32(float *grad_angles, const float *grad_coords, const uint8_t *sequences, int seq_stride,
+                         const float *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         int max_atoms, const tpl_options *opt, void *stream);
+int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const uint8_t *sequences, int seq_stride,
+                         const double *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         int max_atoms, const tpl_options *opt, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,16 +115,19 @@ def test_tile_shapes_and_lookback(rm, rpt):
 
 
 def test_fp64_carry_threshold_and_renorm_off(rm):
+    """FP32 inter-tile carries (fp64_carry_min_len=-1) or a threshold of 256 keep the
+    1e-3 A bound; switching the Newton-Schulz renormalisation off is an ablation
+    (coherent scale drift of FP32 frames), held to 5e-3 A only."""
     B, L = 4, 600
     ang, lengths, g = make_case(B, L, 77, lengths=[600, 450, 300, 20])
     rc, rg = oracle_ref(ang, lengths, g, True)
-    for carry, renorm in [(-1, 0), (256, 0), (0, -1)]:
+    for carry, renorm, ctol in [(-1, 0, COORD_TOL_F32), (256, 0, COORD_TOL_F32), (0, -1, 5e-3)]:
         rm.set_options(1, carry, renorm, 0)
         try:
             c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
         finally:
             rm.set_options(0, 0, 0, 0)
-        check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+        check(c, gi, rc, rg, lengths, L, ctol, GRAD_TOL_F32)
 
 
 def test_padding_nan_does_not_leak(rm):

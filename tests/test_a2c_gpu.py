@@ -1,0 +1,253 @@
+"""Angles2Coords on the GPU against the oracle and the reference's golden fixtures.
+
+Tolerances (stated here, used below):
+  * FP64 kernels vs oracle / golden: coordinates 1e-9 A, gradients 1e-9 x max|grad|.
+  * FP32 kernels vs oracle on the same float32 angles: coordinates 1e-3 A,
+    gradients 1e-4 x max|grad|.
+Names and atom counts are compared bit-exactly.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+AA = "ACDEFGHIKLMNPQRSTVWY"
+COORD_TOL_F32, GRAD_TOL_F32 = 1e-3, 1e-4
+COORD_TOL_F64, GRAD_TOL_F64 = 1e-9, 1e-9
+
+
+@pytest.fixture(scope="module")
+def fm(built):
+    from torchproteinlibrary_gb300 import load_extension
+    return load_extension("_FullAtomModel")
+
+
+def run_gpu(fm, ang, seqs, g, dtype):
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+    dev = torch.device("cuda")
+    a = torch.tensor(ang, dtype=dtype, device=dev)
+    seq = convertStringList(seqs).to(dev)
+    na = [fm.getSeqNumAtoms(s) for s in seqs]
+    maxA = max(na) if na else 0
+    B = len(seqs)
+    coords = torch.full((B, 3 * maxA), float("nan"), dtype=dtype, device=dev)
+    rn = torch.full((B, maxA, 4), 255, dtype=torch.uint8, device=dev)
+    an = torch.full((B, maxA, 4), 255, dtype=torch.uint8, device=dev)
+    fm.Angles2Coords_forward(seq, a, coords, rn, an)
+    gi = torch.full_like(a, float("nan"))
+    gt = torch.tensor(g, dtype=dtype, device=dev) if g is not None else torch.zeros_like(coords)
+    fm.Angles2Coords_backward(gt, gi, seq, a)
+    assert fm.workspace_status(0) == 0
+    return (coords.double().cpu().numpy(), rn.cpu().numpy(), an.cpu().numpy(), np.array(na, np.int32),
+            gi.double().cpu().numpy())
+
+
+def check(c, gi, rc, rg, na, ctol, gtol):
+    for b, n in enumerate(na):
+        assert np.all(c[b, 3 * n:] == 0.0)
+    d = np.sqrt(((c - rc).reshape(len(na), -1, 3) ** 2).sum(-1)).max() if c.size else 0.0
+    assert d <= ctol, f"max coordinate error {d:.3e} A"
+    scale = max(1.0, np.abs(rg).max())
+    ge = np.abs(gi - rg).max() / scale
+    assert ge <= gtol, f"max gradient error {ge:.3e} of max|grad|"
+    return d, ge
+
+
+def test_golden_fp64(fm):
+    d = np.load(os.path.join(GOLD, "a2c_ref.npz"))
+    seqs = [str(s) for s in d["sequences"]]
+    c, rn, an, na, gi = run_gpu(fm, d["angles"], seqs, d["grad_coords"], torch.float64)
+    np.testing.assert_array_equal(na, d["num_atoms"])
+    np.testing.assert_array_equal(rn, d["res_names"])
+    np.testing.assert_array_equal(an, d["atom_names"])
+    check(c, gi, d["coords"], d["grad_angles"], na, COORD_TOL_F64, GRAD_TOL_F64)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_random_batch_matches_oracle(fm, dtype):
+    rng = np.random.default_rng(31)
+    seqs = ["".join(rng.choice(list(AA), rng.integers(1, 300))) for _ in range(7)] + ["G", "P", "W", AA]
+    L = 300
+    ang = rng.uniform(-np.pi, np.pi, (len(seqs), 8, L))
+    ang[:, 2] = rng.normal(np.pi, 0.05, (len(seqs), L))
+    rc, rrn, ran, na = oracle.a2c_forward(ang.astype(np.float32).astype(np.float64) if dtype == torch.float32 else ang,
+                                          seqs)
+    g = rng.standard_normal(rc.shape)
+    for b, n in enumerate(na):
+        g[b, 3 * n:] = 0
+    if dtype == torch.float32:
+        g = g.astype(np.float32).astype(np.float64)
+        a_ref = ang.astype(np.float32).astype(np.float64)
+    else:
+        a_ref = ang
+    rg = oracle.a2c_backward(g, a_ref, seqs)
+    c, rn, an, na2, gi = run_gpu(fm, ang, seqs, g, dtype)
+    np.testing.assert_array_equal(rn, rrn)
+    np.testing.assert_array_equal(an, ran)
+    tol = (COORD_TOL_F32, GRAD_TOL_F32) if dtype == torch.float32 else (COORD_TOL_F64, GRAD_TOL_F64)
+    check(c, gi, rc, rg, na, *tol)
+    # padding of the angle tensor past each chain gets zero gradient
+    for b, s in enumerate(seqs):
+        assert np.all(gi[b, :, len(s):] == 0)
+
+
+def test_config2_fd_check(fm):
+    """Full-atom config: 64 chains of 150 random residues, FP64, omega = pi; gradient
+    of 16 random angle entries per chain against central differences (h = 1e-6) of
+    the GPU forward."""
+    rng = np.random.default_rng(1002)
+    B, L = 64, 150
+    seqs = ["".join(rng.choice(list(AA), L)) for _ in range(B)]
+    ang = rng.uniform(-np.pi, np.pi, (B, 8, L))
+    ang[:, 2] = np.pi
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+    dev = torch.device("cuda")
+    c, rn, an, na, _ = run_gpu(fm, ang, seqs, None, torch.float64)
+    g = rng.standard_normal(c.shape)
+    _, _, _, _, gi = run_gpu(fm, ang, seqs, g, torch.float64)
+    # oracle on a few chains
+    idx = [0, 17, 63]
+    rc, _, _, _ = oracle.a2c_forward(ang[idx], [seqs[i] for i in idx])
+    rg = oracle.a2c_backward(g[idx][:, :rc.shape[1]], ang[idx], [seqs[i] for i in idx])
+    check(c[idx][:, :rc.shape[1]], gi[idx], rc, rg, na[idx], COORD_TOL_F64, GRAD_TOL_F64)
+    # central differences, all chains at once: perturb entry (b, k_b, j_b) of every chain
+    seq = convertStringList(seqs).to(dev)
+    maxA = int(na.max())
+    gt = torch.tensor(g, dtype=torch.float64, device=dev)
+
+    def forward(a_np):
+        a = torch.tensor(a_np, dtype=torch.float64, device=dev)
+        out = torch.empty(B, 3 * maxA, dtype=torch.float64, device=dev)
+        e = torch.empty(0, dtype=torch.uint8, device=dev)
+        fm.Angles2Coords_forward(seq, a, out, e, e)
+        return (out * gt).sum(1).cpu().numpy()
+
+    h = 1e-6
+    worst = 0.0
+    for _ in range(16):
+        k = rng.integers(0, 8, B)
+        j = rng.integers(0, L, B)
+        ap = ang.copy(); am = ang.copy()
+        ap[np.arange(B), k, j] += h
+        am[np.arange(B), k, j] -= h
+        fd = (forward(ap) - forward(am)) / (2 * h)
+        an_ = gi[np.arange(B), k, j]
+        worst = max(worst, float((np.abs(fd - an_) / np.maximum(1.0, np.abs(fd))).max()))
+    assert worst < 1e-5, worst
+
+
+def test_backbone_matches_angles2backbone(fm, built):
+    """Reference self-consistency test (UnitTests/ReducedModel/Angles2Backbone/test.py:32-70):
+    all-Gly chains through Angles2Coords give the same N, CA, C as Angles2Backbone."""
+    from torchproteinlibrary_gb300 import load_extension
+    rm = load_extension("_ReducedModel")
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(5)
+    B, L = 16, 32
+    lengths = rng.integers(L // 2, L, B).astype(np.int32)
+    # FP64: identical up to rounding.  FP32: the reference's criterion (mean error
+    # below 5e-6 A, assertAlmostEqual(places=5)) plus a 1e-4 A bound on the maximum.
+    for dtype, tol in [(torch.float64, 1e-10), (torch.float32, 1e-4)]:
+        bb = rng.standard_normal((B, 3, L))
+        a = torch.tensor(bb, dtype=dtype, device=dev)
+        ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+        cb = torch.empty(B, 9 * L, dtype=dtype, device=dev)
+        rm.Angles2BackboneGPU_forward(a, cb, torch.tensor(lengths, device=dev), ws)
+        fa = np.zeros((B, 8, L))
+        fa[:, :3] = bb
+        seqs = ["G" * n for n in lengths]
+        c, rn, an, na, _ = run_gpu(fm, fa, seqs, None, dtype)
+        cbb = cb.double().cpu().numpy()
+        err, tot, cnt = 0.0, 0.0, 0
+        for b in range(B):
+            n = lengths[b]
+            x = c[b, :3 * 4 * n].reshape(n, 4, 3)[:, :3].reshape(-1, 3)  # N, CA, C of each Gly
+            d = np.linalg.norm(x - cbb[b, :9 * n].reshape(-1, 3), axis=1)
+            err = max(err, d.max())
+            tot += d.sum()
+            cnt += d.size
+        assert err <= tol, (dtype, err)
+        assert tot / cnt < 5e-6, (dtype, tot / cnt)
+
+
+def test_edge_cases(fm):
+    dev = torch.device("cuda")
+    seqs = ["", "G", "P", "W", "GP"]
+    rng = np.random.default_rng(3)
+    ang = rng.uniform(-np.pi, np.pi, (len(seqs), 8, 4))
+    rc, rrn, ran, na = oracle.a2c_forward(ang, seqs)
+    g = rng.standard_normal(rc.shape)
+    rg = oracle.a2c_backward(g, ang, seqs)
+    c, rn, an, na2, gi = run_gpu(fm, ang, seqs, g, torch.float64)
+    np.testing.assert_array_equal(na, na2)
+    np.testing.assert_array_equal(an, ran)
+    check(c, gi, rc, rg, na, COORD_TOL_F64, GRAD_TOL_F64)
+    assert np.all(c[0] == 0) and np.all(gi[0] == 0)
+
+
+def test_unknown_letter_and_overflow_reported(fm):
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+    dev = torch.device("cuda")
+    with pytest.raises(RuntimeError):
+        fm.getSeqNumAtoms("GAXG")
+    seq = convertStringList(["GAXG", "GG"]).to(dev)
+    a = torch.zeros(2, 8, 4, device=dev)
+    out = torch.full((2, 3 * 8), 7.0, device=dev)
+    e = torch.empty(0, dtype=torch.uint8, device=dev)
+    fm.Angles2Coords_forward(seq, a, out, e, e)
+    assert fm.workspace_status(0) == -5
+    assert torch.all(out[0] == 0) and torch.all(out[1] != 7.0)
+    # more atoms than slots: clipped and reported
+    seq = convertStringList(["WWW"]).to(dev)
+    out = torch.zeros(1, 3 * 20, device=dev)
+    fm.Angles2Coords_forward(seq, torch.zeros(1, 8, 3, device=dev), out, e, e)
+    assert fm.workspace_status(0) == -7
+    # angles tensor shorter than the sequence
+    seq = convertStringList(["GGGGG"]).to(dev)
+    out = torch.zeros(1, 3 * 20, device=dev)
+    fm.Angles2Coords_forward(seq, torch.zeros(1, 8, 3, device=dev), out, e, e)
+    assert fm.workspace_status(0) == -4
+
+
+def test_layer_api_and_gradcheck(built):
+    from torchproteinlibrary_gb300.FullAtomModel import Angles2Coords
+    layer = Angles2Coords()
+    dev = torch.device("cuda")
+    seqs = ["ACDEFG", "WYP"]
+    x = torch.randn(2, 8, 6, dtype=torch.float64, device=dev, requires_grad=True)
+    coords, res, atoms, num = layer(x, seqs)
+    assert coords.shape == (2, 3 * int(num.max())) and coords.device == x.device
+    assert res.dtype == torch.uint8 and res.shape == (2, int(num.max()), 4)
+    assert num.dtype == torch.int32 and num.device.type == "cpu"
+    assert [int(v) for v in num] == [oracle.num_atoms(s) for s in seqs]
+    assert bytes(atoms[0, 1].cpu().numpy()).rstrip(b"\0") == b"CA"
+    assert bytes(res[1, 0].cpu().numpy()).rstrip(b"\0") == b"TRP"
+
+    def f(a):
+        return layer(a, seqs)[0]
+
+    assert torch.autograd.gradcheck(f, (x,), eps=1e-6, atol=1e-6, rtol=1e-5)
+    with pytest.raises(RuntimeError):
+        layer(x.detach().cpu(), seqs)
+
+
+def test_config4_ragged_fp32_vs_fp64(fm):
+    """Training-step workload shapes: 256 chains of U{50..500} random residues;
+    the FP32 kernels agree with the FP64 kernels within the stated tolerances."""
+    rng = np.random.default_rng(1004)
+    B = 256
+    lens = rng.integers(50, 501, B)
+    L = int(lens.max())
+    seqs = ["".join(rng.choice(list(AA), n)) for n in lens]
+    ang = rng.uniform(-np.pi, np.pi, (B, 8, L)).astype(np.float32).astype(np.float64)
+    c64, _, _, na, _ = run_gpu(fm, ang, seqs, None, torch.float64)
+    g = rng.standard_normal(c64.shape).astype(np.float32).astype(np.float64)
+    c64, _, _, _, g64 = run_gpu(fm, ang, seqs, g, torch.float64)
+    c32, _, _, _, g32 = run_gpu(fm, ang, seqs, g, torch.float32)
+    check(c32, g32, c64, g64, na, COORD_TOL_F32, GRAD_TOL_F32)

@@ -70,7 +70,8 @@ def _nvcc_obj(src: str) -> str:
     obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
     deps = [os.path.join(CSRC, src)] + _headers()
     if _stale(obj, deps):
-        _run([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-c",
+        _run([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+              "-I", INCLUDE, "-c",
               os.path.join(CSRC, src), "-o", obj])
     return obj
 

@@ -1,0 +1,197 @@
+// _FullAtomModel extension module: the reference's Angles2Coords entry points
+// (Layers/FullAtomModel/main.cpp:13-16, Angles2Coords/angles2coords_interface.cpp)
+// over the libtpl_gb300 C ABI.
+//
+// Differences from the reference, all deliberate:
+//  * The compute runs on CUDA tensors (float32: batched kernels, float64: FP64
+//    kernels); the reference runs on the CPU only.  A CPU `sequences` tensor is
+//    copied to the angles' device; CPU angles raise.
+//  * Unknown residue letters raise RuntimeError (the reference's getNumAtoms
+//    throws, its tree builder silently skips them, nUtil.cpp:515-516 /
+//    cConformation.cpp:60-121).
+//  * res_names / atom_names may be empty tensors to skip writing them.
+#include <c10/cuda/CUDAGuard.h>
+#include <c10/cuda/CUDAStream.h>
+#include <torch/extension.h>
+
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "../../../include/tpl_gb300.h"
+
+namespace {
+
+void check_status(int s, const char *what) {
+    TORCH_CHECK(s == TPL_OK, what, ": ", tpl_status_string(s), " (", s, ")");
+}
+
+void *stream_of(const torch::Tensor &t) {
+    return (void *)c10::cuda::getCurrentCUDAStream(t.device().index()).stream();
+}
+
+// One small status workspace per device (the reference entry points carry none).
+torch::Tensor status_ws(const torch::Device &dev) {
+    static std::mutex mu;
+    static std::map<int, torch::Tensor> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev.index());
+    if (it != cache.end()) return it->second;
+    auto t = torch::zeros({(int64_t)tpl_a2c_workspace_bytes(0, 0, 0, nullptr)},
+                          torch::TensorOptions().dtype(torch::kUInt8).device(dev));
+    cache[dev.index()] = t;
+    return t;
+}
+
+torch::Tensor seq_on(const torch::Tensor &sequences, const torch::Device &dev) {
+    TORCH_CHECK(sequences.scalar_type() == torch::kByte, "sequences must be uint8");
+    TORCH_CHECK(sequences.dim() == 2, "sequences must be [batch, max_len + 1]");
+    auto s = sequences.is_cuda() ? sequences : sequences.to(dev, /*non_blocking=*/false);
+    return s.contiguous();
+}
+
+void Angles2Coords_forward(torch::Tensor sequences, torch::Tensor input_angles, torch::Tensor output_coords,
+                           torch::Tensor res_names, torch::Tensor atom_names) {
+    TORCH_CHECK(input_angles.is_cuda(), "input_angles must be a CUDA tensor (this build has no CPU path)");
+    TORCH_CHECK(input_angles.is_contiguous() && output_coords.is_contiguous(), "tensors must be contiguous");
+    TORCH_CHECK(input_angles.dim() == 3 && input_angles.size(1) >= 8, "input_angles must be [batch, 8, max_len]");
+    TORCH_CHECK(input_angles.size(1) == 8, "input_angles must have 8 rows (phi, psi, omega, chi1..chi5)");
+    TORCH_CHECK(output_coords.is_cuda() && output_coords.scalar_type() == input_angles.scalar_type(),
+                "output_coords must be a CUDA tensor of the angles' dtype");
+    const at::cuda::CUDAGuard guard(input_angles.device());
+    const int64_t B = input_angles.size(0), L = input_angles.size(2);
+    TORCH_CHECK(output_coords.dim() == 2 && output_coords.size(0) == B && output_coords.size(1) % 3 == 0,
+                "output_coords must be [batch, 3 * max_atoms]");
+    const int64_t maxA = output_coords.size(1) / 3;
+    auto seq = seq_on(sequences, input_angles.device());
+    TORCH_CHECK(seq.size(0) == B, "one sequence per chain");
+    uint8_t *rn = nullptr, *an = nullptr;
+    if (res_names.numel() > 0 || atom_names.numel() > 0) {
+        TORCH_CHECK(res_names.is_cuda() && atom_names.is_cuda(), "names must be CUDA tensors");
+        TORCH_CHECK(res_names.scalar_type() == torch::kByte && atom_names.scalar_type() == torch::kByte,
+                    "names must be uint8");
+        TORCH_CHECK(res_names.numel() == B * maxA * 4 && atom_names.numel() == B * maxA * 4,
+                    "names must be [batch, max_atoms, 4]");
+        TORCH_CHECK(res_names.is_contiguous() && atom_names.is_contiguous(), "names must be contiguous");
+        rn = res_names.data_ptr<uint8_t>();
+        an = atom_names.data_ptr<uint8_t>();
+    }
+    auto ws = status_ws(input_angles.device());
+    void *st = stream_of(input_angles);
+    int s;
+    if (input_angles.scalar_type() == torch::kFloat) {
+        s = tpl_a2c_forward_f32(seq.data_ptr<uint8_t>(), (int)seq.size(1), input_angles.data_ptr<float>(),
+                                output_coords.data_ptr<float>(), rn, an, ws.data_ptr(), ws.nbytes(), (int)B, (int)L,
+                                (int)maxA, nullptr, st);
+    } else if (input_angles.scalar_type() == torch::kDouble) {
+        s = tpl_a2c_forward_f64(seq.data_ptr<uint8_t>(), (int)seq.size(1), input_angles.data_ptr<double>(),
+                                output_coords.data_ptr<double>(), rn, an, ws.data_ptr(), ws.nbytes(), (int)B, (int)L,
+                                (int)maxA, nullptr, st);
+    } else {
+        TORCH_CHECK(false, "input_angles must be float32 or float64");
+    }
+    check_status(s, "Angles2Coords_forward");
+}
+
+void Angles2Coords_backward(torch::Tensor grad_atoms, torch::Tensor grad_angles, torch::Tensor sequences,
+                            torch::Tensor input_angles) {
+    TORCH_CHECK(input_angles.is_cuda() && grad_atoms.is_cuda() && grad_angles.is_cuda(),
+                "tensors must be CUDA tensors (this build has no CPU path)");
+    TORCH_CHECK(input_angles.is_contiguous() && grad_atoms.is_contiguous() && grad_angles.is_contiguous(),
+                "tensors must be contiguous");
+    TORCH_CHECK(input_angles.dim() == 3 && input_angles.size(1) == 8, "input_angles must be [batch, 8, max_len]");
+    TORCH_CHECK(grad_angles.sizes() == input_angles.sizes(), "grad_angles must have the angles' shape");
+    TORCH_CHECK(grad_atoms.scalar_type() == input_angles.scalar_type() &&
+                    grad_angles.scalar_type() == input_angles.scalar_type(),
+                "gradient dtypes must match the angles");
+    const at::cuda::CUDAGuard guard(input_angles.device());
+    const int64_t B = input_angles.size(0), L = input_angles.size(2);
+    TORCH_CHECK(grad_atoms.dim() == 2 && grad_atoms.size(0) == B && grad_atoms.size(1) % 3 == 0,
+                "grad_atoms must be [batch, 3 * max_atoms]");
+    const int64_t maxA = grad_atoms.size(1) / 3;
+    auto seq = seq_on(sequences, input_angles.device());
+    auto ws = status_ws(input_angles.device());
+    void *st = stream_of(input_angles);
+    int s;
+    if (input_angles.scalar_type() == torch::kFloat) {
+        s = tpl_a2c_backward_f32(grad_angles.data_ptr<float>(), grad_atoms.data_ptr<float>(), seq.data_ptr<uint8_t>(),
+                                 (int)seq.size(1), input_angles.data_ptr<float>(), ws.data_ptr(), ws.nbytes(), (int)B,
+                                 (int)L, (int)maxA, nullptr, st);
+    } else if (input_angles.scalar_type() == torch::kDouble) {
+        s = tpl_a2c_backward_f64(grad_angles.data_ptr<double>(), grad_atoms.data_ptr<double>(),
+                                 seq.data_ptr<uint8_t>(), (int)seq.size(1), input_angles.data_ptr<double>(),
+                                 ws.data_ptr(), ws.nbytes(), (int)B, (int)L, (int)maxA, nullptr, st);
+    } else {
+        TORCH_CHECK(false, "input_angles must be float32 or float64");
+    }
+    check_status(s, "Angles2Coords_backward");
+}
+
+int64_t getSeqNumAtoms(const std::string &sequence) {
+    int n = tpl_num_atoms(sequence.c_str());
+    TORCH_CHECK(n >= 0, "Unknown atom/res names in sequence '", sequence, "'");
+    return n;
+}
+
+// Angles2Coords_save (angles2coords_interface.cpp:117-137 -> cConformation::save,
+// cConformation.cpp:228-262): PDB ATOM records of one chain, mode 'w' (overwrite)
+// or 'a' (append as a MODEL).  The coordinates come from the GPU forward.
+void Angles2Coords_save(const std::string &sequence, torch::Tensor input_angles, const std::string &output_filename,
+                        const std::string &mode) {
+    TORCH_CHECK(input_angles.dim() == 2 && input_angles.size(0) == 8, "input_angles must be [8, length]");
+    TORCH_CHECK(mode == "w" || mode == "a", "mode must be 'w' or 'a'");
+    const int64_t na = getSeqNumAtoms(sequence);
+    torch::Device dev = input_angles.is_cuda() ? input_angles.device() : torch::Device(torch::kCUDA, 0);
+    auto ang = input_angles.to(dev, torch::kDouble).contiguous().unsqueeze(0);
+    auto opts = torch::TensorOptions().device(dev);
+    auto coords = torch::empty({1, 3 * na}, opts.dtype(torch::kDouble));
+    auto rn = torch::empty({1, na, 4}, opts.dtype(torch::kByte));
+    auto an = torch::empty({1, na, 4}, opts.dtype(torch::kByte));
+    std::vector<uint8_t> sbytes(sequence.begin(), sequence.end());
+    sbytes.push_back(0);
+    auto seq = torch::from_blob(sbytes.data(), {1, (int64_t)sbytes.size()}, torch::kByte).clone();
+    Angles2Coords_forward(seq, ang, coords, rn, an);
+    auto c = coords.cpu();
+    auto r = rn.cpu();
+    auto a = an.cpu();
+    FILE *f = std::fopen(output_filename.c_str(), mode == "w" ? "w" : "a");
+    TORCH_CHECK(f != nullptr, "cannot open ", output_filename);
+    if (mode == "a") std::fprintf(f, "MODEL\n");
+    const double *x = c.data_ptr<double>();
+    const char *rnp = (const char *)r.data_ptr<uint8_t>();
+    const char *anp = (const char *)a.data_ptr<uint8_t>();
+    int res_index = -1, first_atom = 0;
+    for (int64_t i = 0; i < na; i++) {
+        std::string aname(anp + 4 * i, strnlen(anp + 4 * i, 4));
+        std::string rname(rnp + 4 * i, strnlen(rnp + 4 * i, 4));
+        if (aname == "N") {
+            res_index++;
+            first_atom = (int)i;
+        }
+        (void)first_atom;
+        std::fprintf(f, "ATOM  %5d %4s %3s A%4d    %8.3f%8.3f%8.3f\n", (int)i, aname.c_str(), rname.c_str(),
+                     res_index, x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+    }
+    if (mode == "a") std::fprintf(f, "ENDMDL\n");
+    std::fclose(f);
+}
+
+int64_t workspace_status(int64_t device) {
+    auto dev = torch::Device(torch::kCUDA, (int)device);
+    const at::cuda::CUDAGuard guard(dev);
+    auto ws = status_ws(dev);
+    int st = 0;
+    check_status(tpl_workspace_status(ws.data_ptr(), stream_of(ws), &st), "workspace_status");
+    return st;
+}
+
+}  // namespace
+
+PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
+    m.def("Angles2Coords_forward", &Angles2Coords_forward, "Angles2Coords forward");
+    m.def("Angles2Coords_backward", &Angles2Coords_backward, "Angles2Coords backward");
+    m.def("Angles2Coords_save", &Angles2Coords_save, "Angles2Coords save");
+    m.def("getSeqNumAtoms", &getSeqNumAtoms, "Get number of atoms in a sequence");
+    m.def("workspace_status", &workspace_status, "synchronise and read the first device-detected error");
+}

@@ -28,6 +28,7 @@
 
 #include "tpl_common.cuh"
 #include "tpl_internal.h"
+#include "tpl_topology.cuh"
 
 namespace tpl {
 
@@ -67,7 +68,7 @@ __device__ __forceinline__ void store_floats(float *dst, const float *src, int n
         x.x = i < n_valid ? src[i] : 0.f;
         x.y = i + 1 < n_valid ? src[i + 1] : 0.f;
         x.z = i + 2 < n_valid ? src[i + 2] : 0.f;
-        x.w = i + 3 < n_valid ? src[i + 3] : 0.f;
+        x.w = i + 3 < n_valid ? src[i + 3] : 0.f;  // src is only read below n_valid
         d4[v] = x;
     }
     for (int i = head + 4 * nvec + tid; i < n_total; i += NT) dst[i] = i < n_valid ? src[i] : 0.f;
@@ -114,35 +115,51 @@ __device__ __forceinline__ unsigned wait_flag(const unsigned *flag, unsigned epo
     }
 }
 
-// Tile scan shared by forward and backward: thread aggregates of R residues,
-// warp scan, warp totals in shared memory.  Returns the thread's exclusive prefix
-// inside its warp; s_wtot receives the warp totals.
+__device__ const SinCosTableC g_sincos_tab = make_sincos_table();
+
+template <int NT>
+__device__ __forceinline__ void load_sincos_table(float4 *s_tab) {
+    const float4 *src = reinterpret_cast<const float4 *>(&g_sincos_tab);
+    for (int i = threadIdx.x; i < 65; i += NT) s_tab[i] = src[i];
+}
+
+// Walk 1 of a tile: each thread composes the joints of its R residues from
+// identity, recording the thread-local positions of N, CA and C in shared memory
+// (s_loc[(9 r + c) * NT + tid], conflict-free).  Returns the thread's aggregate
+// transform.  omega of the chain's last residue moves nothing and is skipped.
 template <int R, int NT>
-__device__ __forceinline__ Frame<float> tile_local_scan(const A2bArgs &a, const float (*s_ang)[R * NT], int nreal,
-                                                        bool last_in_tile_is_chain_end, float (&cs)[R][3],
-                                                        float (&sn)[R][3], Frame<float> *s_wtot) {
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int j0 = tid * R;
+__device__ __forceinline__ Frame<float> walk_local(const A2bArgs &a, const float4 *s_tab, const float *ang0,
+                                                   const float *ang1, const float *ang2, int j0, int nreal,
+                                                   bool chain_end, float *s_loc) {
     Frame<float> agg;
     frame_identity(agg);
+    float *l = s_loc + threadIdx.x;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int j = j0 + r;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            cs[r][k] = 1.f;
-            sn[r][k] = 0.f;
-        }
         if (j < nreal) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                if (k == 2 && last_in_tile_is_chain_end && j == nreal - 1) break;  // omega[len-1] moves nothing
-                sincosf(s_ang[k][j], &sn[r][k], &cs[r][k]);
-                apply_joint(agg, a.bc.cb[k], a.bc.sb[k], a.bc.d[k], cs[r][k], sn[r][k]);
+            float s, c;
+            l[(9 * r + 0) * NT] = agg.p[0]; l[(9 * r + 1) * NT] = agg.p[1]; l[(9 * r + 2) * NT] = agg.p[2];
+            sincos_tab(s_tab, ang0[j], &s, &c);
+            apply_joint(agg, a.bc.cb[0], a.bc.sb[0], a.bc.d[0], c, s);
+            l[(9 * r + 3) * NT] = agg.p[0]; l[(9 * r + 4) * NT] = agg.p[1]; l[(9 * r + 5) * NT] = agg.p[2];
+            sincos_tab(s_tab, ang1[j], &s, &c);
+            apply_joint(agg, a.bc.cb[1], a.bc.sb[1], a.bc.d[1], c, s);
+            l[(9 * r + 6) * NT] = agg.p[0]; l[(9 * r + 7) * NT] = agg.p[1]; l[(9 * r + 8) * NT] = agg.p[2];
+            if (!(chain_end && j == nreal - 1)) {
+                sincos_tab(s_tab, ang2[j], &s, &c);
+                apply_joint(agg, a.bc.cb[2], a.bc.sb[2], a.bc.d[2], c, s);
             }
         }
     }
-    if (a.renorm) renormalize(agg);
+    return agg;
+}
+
+// Warp scan of the thread aggregates; returns the exclusive prefix inside the
+// warp and leaves the warp totals in s_wtot.
+__device__ __forceinline__ Frame<float> warp_exclusive(Frame<float> agg, bool renorm, Frame<float> *s_wtot) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (renorm) renormalize(agg);
     Frame<float> inc = warp_scan_frames(agg, lane);
     Frame<float> exc = shfl_up_frame(inc, 1);
     if (lane == 0) frame_identity(exc);
@@ -150,56 +167,113 @@ __device__ __forceinline__ Frame<float> tile_local_scan(const A2bArgs &a, const 
     return exc;
 }
 
-// Forward inter-tile carry by decoupled look-back (thread 0 only).
-// Returns the transform of the chain frame at the start of tile t (FP64).
-__device__ Frame<double> forward_carry(const A2bArgs &a, int b, int t, bool more, const Frame<float> &tile_agg,
-                                       unsigned epoch_bits, bool use64) {
+// Warp 0: exclusive scan of the NW warp totals across lanes 0..NW-1 (log2 NW
+// shuffle steps).  Lane l < NW gets the prefix of warps < l; every lane gets the
+// tile aggregate.
+template <int NW>
+__device__ __forceinline__ Frame<float> warp_totals_scan(const Frame<float> *s_wtot, bool renorm, Frame<float> &tile) {
+    const int lane = threadIdx.x & 31;
+    Frame<float> f;
+    if (lane < NW) f = s_wtot[lane];
+    else frame_identity(f);
+#pragma unroll
+    for (int off = 1; off < NW; off <<= 1) {
+        Frame<float> o = shfl_up_frame(f, off);
+        if (lane >= off) f = compose(o, f);
+    }
+    if (renorm) renormalize(f);
+    Frame<float> exc = shfl_up_frame(f, 1);
+    if (lane == 0) frame_identity(exc);
+#pragma unroll
+    for (int i = 0; i < 9; i++) tile.r[i] = __shfl_sync(0xffffffffu, f.r[i], NW - 1);
+#pragma unroll
+    for (int i = 0; i < 3; i++) tile.p[i] = __shfl_sync(0xffffffffu, f.p[i], NW - 1);
+    return exc;
+}
+
+// FP64 frame arithmetic on 12-double arrays (rotation row-major, translation),
+// used by the single look-back thread; kept out of line and in memory so that
+// the kernels' register budget is set by their parallel parts.
+__device__ __noinline__ void compose_d(double *c, const double *a, const double *b) {
+#pragma unroll 1
+    for (int i = 0; i < 3; i++) {
+        const double a0 = a[3 * i], a1 = a[3 * i + 1], a2 = a[3 * i + 2];
+        c[3 * i] = fma(a0, b[0], fma(a1, b[3], a2 * b[6]));
+        c[3 * i + 1] = fma(a0, b[1], fma(a1, b[4], a2 * b[7]));
+        c[3 * i + 2] = fma(a0, b[2], fma(a1, b[5], a2 * b[8]));
+        c[9 + i] = fma(a0, b[9], fma(a1, b[10], fma(a2, b[11], a[9 + i])));
+    }
+}
+__device__ __noinline__ void renormalize_d(double *f) {
+    Frame<double> x;
+    frame_load(x, f);
+    renormalize(x);
+    frame_store(f, x);
+}
+__device__ __noinline__ void round_to_float_d(double *f) {
+#pragma unroll 1
+    for (int i = 0; i < 12; i++) f[i] = (double)(float)f[i];
+}
+__device__ __forceinline__ void identity_d(double *f) {
+#pragma unroll 1
+    for (int i = 0; i < 12; i++) f[i] = (i < 9 && i % 4 == 0) ? 1.0 : 0.0;
+}
+__device__ __forceinline__ void copy_d(double *d, const double *s) {
+#pragma unroll 1
+    for (int i = 0; i < 12; i++) d[i] = s[i];
+}
+
+// Forward inter-tile carry by decoupled look-back (thread 0 only).  Publishes this
+// tile's aggregate (and inclusive prefix when a later tile exists), waits on the
+// predecessors, and returns in `carry` the chain frame at the start of tile t.
+// `scratch` holds 3 x 12 doubles of shared memory.
+__device__ __noinline__ void forward_carry(const A2bArgs &a, int b, int t, bool more, const Frame<float> &tile_agg,
+                                           unsigned epoch_bits, bool use64, double *carry, double *scratch) {
     TileRecord *rc = a.rec + (size_t)b * a.ntiles + t;
-    Frame<double> agg64 = frame_cast<double>(tile_agg);
-    Frame<double> carry;
-    frame_identity(carry);
+    double *acc = scratch, *agg = scratch + 12, *tmp = scratch + 24;
+#pragma unroll 1
+    for (int i = 0; i < 9; i++) agg[i] = (double)tile_agg.r[i];
+#pragma unroll 1
+    for (int i = 0; i < 3; i++) agg[9 + i] = (double)tile_agg.p[i];
+    identity_d(carry);
     if (t == 0) {
         // test hook: leave the first tile of chain 0 unpublished so that its
         // successor's bounded wait runs out (tpl_workspace_status reports it)
         if (more && !(b == 0 && a.hdr->test_skip_publish)) {
-            store_frame_d(rc->finc, agg64);
+            copy_d(rc->finc, agg);
             st_release(&rc->fflag, epoch_bits | kFlagInc);
         }
-        return carry;
+        return;
     }
     if (more) {
-        store_frame_d(rc->fagg, agg64);
+        copy_d(rc->fagg, agg);
         st_release(&rc->fflag, epoch_bits | kFlagAgg);
     }
-    Frame<double> acc;
-    frame_identity(acc);
+    identity_d(acc);
     bool ok = true;
     for (int tt = t - 1; tt >= 0; tt--) {
         const TileRecord *q = a.rec + (size_t)b * a.ntiles + tt;
         unsigned f = wait_flag(&q->fflag, epoch_bits, a.hdr, ok);
         if (!ok) break;
-        Frame<double> x;
         if ((f & 3u) == kFlagInc) {
-            frame_load(x, q->finc);
-            carry = compose(x, acc);
-            if (!use64) round_to_float(carry);
+            compose_d(carry, q->finc, acc);
+            if (!use64) round_to_float_d(carry);
             break;
         }
-        frame_load(x, q->fagg);
-        acc = compose(x, acc);
-        if (!use64) round_to_float(acc);
+        compose_d(tmp, q->fagg, acc);
+        copy_d(acc, tmp);
+        if (!use64) round_to_float_d(acc);
     }
-    if (!ok) frame_identity(carry);
-    if (a.renorm) renormalize(carry);
-    frame_store(rc->fexc, carry);
+    if (!ok) identity_d(carry);
+    if (a.renorm) renormalize_d(carry);
+    copy_d(rc->fexc, carry);
     if (more) {
-        Frame<double> incl = compose(carry, agg64);
-        if (!use64) round_to_float(incl);
-        if (a.renorm) renormalize(incl);
-        store_frame_d(rc->finc, incl);
+        compose_d(tmp, carry, agg);
+        if (!use64) round_to_float_d(tmp);
+        if (a.renorm) renormalize_d(tmp);
+        copy_d(rc->finc, tmp);
         st_release(&rc->fflag, epoch_bits | kFlagInc);
     }
-    return carry;
 }
 
 __device__ __forceinline__ void finish_launch(unsigned *ticket, unsigned *done, unsigned *epoch) {
@@ -216,19 +290,24 @@ __device__ __forceinline__ void finish_launch(unsigned *ticket, unsigned *done, 
 }
 
 template <int R, int NT>
-__global__ void __launch_bounds__(NT) a2b_fwd_f32_kernel(A2bArgs a) {
+__global__ void __launch_bounds__(NT, 5) a2b_fwd_f32_kernel(A2bArgs a) {
     constexpr int TILE = R * NT;
     constexpr int NW = NT / 32;
-    __shared__ float s_ang[3][TILE];
-    __shared__ float s_out[9 * TILE];
+    extern __shared__ __align__(16) float s_dyn[];
+    float(*s_ang)[TILE] = reinterpret_cast<float(*)[TILE]>(s_dyn);  // [3][TILE]
+    float *s_loc = s_dyn + 3 * TILE;                                 // [9 * TILE]
+    __shared__ float4 s_tab[65];
     __shared__ Frame<float> s_wtot[NW];
     __shared__ Frame<float> s_wpre[NW];
+    __shared__ Frame<float> s_carry;
+    __shared__ double s_fcarry[12], s_fscratch[36];
     __shared__ float s_org[3];
     __shared__ int s_item;
     __shared__ unsigned s_epoch;
 
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int tid = threadIdx.x, w = tid >> 5;
     if (tid == 0) s_epoch = (*(volatile unsigned *)&a.hdr->fwd_epoch & 0x3fffffffu) << 2;
+    load_sincos_table<NT>(s_tab);
 
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(&a.hdr->fwd_ticket, 1u);
@@ -245,8 +324,8 @@ __global__ void __launch_bounds__(NT) a2b_fwd_f32_kernel(A2bArgs a) {
         const int ntile = min(TILE, a.L - s0);
         const int nreal = max(0, min(ntile, len - s0));
         float *out = a.coords + (size_t)b * 9 * a.L + (size_t)9 * s0;
+        if (nreal < ntile) store_floats<NT>(out + 9 * nreal, nullptr, 0, 9 * (ntile - nreal));
         if (nreal == 0) {
-            store_floats<NT>(out, s_out, 0, 9 * ntile);
             __syncthreads();
             continue;
         }
@@ -257,51 +336,52 @@ __global__ void __launch_bounds__(NT) a2b_fwd_f32_kernel(A2bArgs a) {
         __syncthreads();
 
         const bool chain_end = (s0 + nreal == len);
-        float cs[R][3], sn[R][3];
-        Frame<float> exc = tile_local_scan<R, NT>(a, s_ang, nreal, chain_end, cs, sn, s_wtot);
+        const int j0 = tid * R;
+        Frame<float> agg = walk_local<R, NT>(a, s_tab, s_ang[0], s_ang[1], s_ang[2], j0, nreal, chain_end, s_loc);
+        Frame<float> exc = warp_exclusive(agg, a.renorm, s_wtot);
         __syncthreads();
 
-        if (tid == 0) {
-            Frame<float> run;
-            frame_identity(run);
-            Frame<float> pre[NW];
-#pragma unroll
-            for (int ww = 0; ww < NW; ww++) {
-                pre[ww] = run;
-                run = compose(run, s_wtot[ww]);
-                if (a.renorm) renormalize(run);
+        if (w == 0) {
+            Frame<float> tile;
+            Frame<float> wexc = warp_totals_scan<NW>(s_wtot, a.renorm, tile);
+            if (tid == 0) {
+                const bool more = s0 + TILE < len;
+                const bool use64 = a.fp64_min_len >= 0 && len >= a.fp64_min_len;
+                forward_carry(a, b, t, more, tile, s_epoch, use64, s_fcarry, s_fscratch);
+                Frame<float> c32;
+                frame_load(c32, s_fcarry);
+                s_org[0] = c32.p[0]; s_org[1] = c32.p[1]; s_org[2] = c32.p[2];
+                c32.p[0] = c32.p[1] = c32.p[2] = 0.f;  // positions relative to the tile origin
+                s_carry = c32;
             }
-            const bool more = s0 + TILE < len;
-            const bool use64 = a.fp64_min_len >= 0 && len >= a.fp64_min_len;
-            Frame<double> carry = forward_carry(a, b, t, more, run, s_epoch, use64);
-            Frame<float> c32 = frame_cast<float>(carry);
-            s_org[0] = c32.p[0]; s_org[1] = c32.p[1]; s_org[2] = c32.p[2];
-            c32.p[0] = c32.p[1] = c32.p[2] = 0.f;  // positions relative to the tile origin
-#pragma unroll
-            for (int ww = 0; ww < NW; ww++) s_wpre[ww] = compose(c32, pre[ww]);
+            __syncwarp();
+            if (tid < NW) s_wpre[tid] = compose(s_carry, wexc);
         }
         __syncthreads();
 
+        // walk 2: world position = P (x) local position, written straight to HBM
         Frame<float> P = compose(s_wpre[w], exc);
         if (a.renorm) renormalize(P);
-        const float o0 = s_org[0], o1 = s_org[1], o2 = s_org[2];
-        const int j0 = tid * R;
+        const float t0 = P.p[0] + s_org[0], t1 = P.p[1] + s_org[1], t2 = P.p[2] + s_org[2];
+        float *dst = out + (size_t)9 * j0;
+        const bool vec = (R % 4 == 0) && (j0 + R <= nreal) && ((((uintptr_t)dst) & 15u) == 0);
+        const float *l = s_loc + tid;
+        auto world = [&](int e) {  // element e = 9 r + 3 q + c of this thread's output
+            const int r = e / 9, q = (e % 9) / 3, c = e % 3;
+            const float x = l[(9 * r + 3 * q) * NT], y = l[(9 * r + 3 * q + 1) * NT], z = l[(9 * r + 3 * q + 2) * NT];
+            const float tc = c == 0 ? t0 : (c == 1 ? t1 : t2);
+            return fmaf(P.r[3 * c], x, fmaf(P.r[3 * c + 1], y, fmaf(P.r[3 * c + 2], z, tc)));
+        };
+        if (vec) {
+            float4 *d4 = reinterpret_cast<float4 *>(dst);
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int j = j0 + r;
-            if (j < nreal) {
-                float *o = s_out + 9 * j;
-                o[0] = P.p[0] + o0; o[1] = P.p[1] + o1; o[2] = P.p[2] + o2;
-                apply_joint(P, a.bc.cb[0], a.bc.sb[0], a.bc.d[0], cs[r][0], sn[r][0]);
-                o[3] = P.p[0] + o0; o[4] = P.p[1] + o1; o[5] = P.p[2] + o2;
-                apply_joint(P, a.bc.cb[1], a.bc.sb[1], a.bc.d[1], cs[r][1], sn[r][1]);
-                o[6] = P.p[0] + o0; o[7] = P.p[1] + o1; o[8] = P.p[2] + o2;
-                apply_joint(P, a.bc.cb[2], a.bc.sb[2], a.bc.d[2], cs[r][2], sn[r][2]);
-            }
+            for (int i = 0; i < 9 * R / 4; i++)
+                d4[i] = make_float4(world(4 * i), world(4 * i + 1), world(4 * i + 2), world(4 * i + 3));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 9 * R; e++)
+                if (j0 + e / 9 < nreal) dst[e] = world(e);
         }
-        (void)lane;
-        __syncthreads();
-        store_floats<NT>(out, s_out, 9 * nreal, 9 * ntile);
         __syncthreads();
     }
     finish_launch(&a.hdr->fwd_ticket, &a.hdr->fwd_done, &a.hdr->fwd_epoch);
@@ -311,7 +391,7 @@ __global__ void __launch_bounds__(NT) a2b_fwd_f32_kernel(A2bArgs a) {
 // Suffix look-back over later tiles of the chain (thread 0 only).  own = this
 // tile's (G, S) with S about the world origin.  Returns the sums over all later
 // tiles.
-__device__ void backward_suffix(const A2bArgs &a, int b, int t, int t_last, const double own[6],
+__device__ __noinline__ void backward_suffix(const A2bArgs &a, int b, int t, int t_last, const double own[6],
                                 unsigned epoch_bits, double carry[6]) {
     TileRecord *rc = a.rec + (size_t)b * a.ntiles + t;
     for (int i = 0; i < 6; i++) carry[i] = 0.0;
@@ -357,21 +437,44 @@ __device__ __forceinline__ float warp_suffix_exclusive(float v, int lane, float 
     return inc - v;
 }
 
+// Rotate a vector by R^T (into a frame's local coordinates) and by R.
+__device__ __forceinline__ void rot_t(const Frame<float> &f, const float *v, float *o) {
+    o[0] = fmaf(f.r[0], v[0], fmaf(f.r[3], v[1], f.r[6] * v[2]));
+    o[1] = fmaf(f.r[1], v[0], fmaf(f.r[4], v[1], f.r[7] * v[2]));
+    o[2] = fmaf(f.r[2], v[0], fmaf(f.r[5], v[1], f.r[8] * v[2]));
+}
+__device__ __forceinline__ void rot(const Frame<float> &f, const float *v, float *o) {
+    o[0] = fmaf(f.r[0], v[0], fmaf(f.r[1], v[1], f.r[2] * v[2]));
+    o[1] = fmaf(f.r[3], v[0], fmaf(f.r[4], v[1], f.r[5] * v[2]));
+    o[2] = fmaf(f.r[6], v[0], fmaf(f.r[7], v[1], f.r[8] * v[2]));
+}
+
+// The adjoint is evaluated in each thread's local frame (the frame its walk
+// started from): for a rigid motion (R, p), u . sum (x_i - x_m) x g_i is
+// unchanged when u and x are replaced by their local coordinates and g by
+// R^T g.  Each thread therefore only rotates its upstream gradients (27 FMA per
+// residue); joint axes are its local bond directions.
 template <int R, int NT>
-__global__ void __launch_bounds__(NT) a2b_bwd_f32_kernel(A2bArgs a) {
+__global__ void __launch_bounds__(NT, 5) a2b_bwd_f32_kernel(A2bArgs a) {
     constexpr int TILE = R * NT;
     constexpr int NW = NT / 32;
-    __shared__ float s_ang[3][TILE];
-    __shared__ float s_g[9 * TILE];
+    extern __shared__ __align__(16) float s_dyn[];
+    float(*s_ang)[TILE] = reinterpret_cast<float(*)[TILE]>(s_dyn);  // [3][TILE]
+    float *s_g = s_dyn + 3 * TILE;                                   // [9 * TILE]
+    float *s_loc = s_dyn + 12 * TILE;                                // [9 * TILE]
+    __shared__ float4 s_tab[65];
     __shared__ Frame<float> s_wtot[NW];
     __shared__ Frame<float> s_wpre[NW];
     __shared__ float s_wsum[NW][6];
     __shared__ float s_wsuf[NW][6];
+    __shared__ float s_org[3];
     __shared__ int s_item;
-    __shared__ unsigned s_epoch, s_fepoch;
+    __shared__ unsigned s_epoch;
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     if (tid == 0) s_epoch = (*(volatile unsigned *)&a.hdr->bwd_epoch & 0x3fffffffu) << 2;
+    load_sincos_table<NT>(s_tab);
+    const float inv_d0 = 1.f / a.bc.d[0], inv_d1 = 1.f / a.bc.d[1], inv_d2 = 1.f / a.bc.d[2];
 
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(&a.hdr->bwd_ticket, 1u);
@@ -389,7 +492,7 @@ __global__ void __launch_bounds__(NT) a2b_bwd_f32_kernel(A2bArgs a) {
         const int nreal = max(0, min(ntile, len - s0));
         float *gout = a.grad_angles + (size_t)b * 3 * a.L + s0;
         if (nreal == 0) {
-            for (int k = 0; k < 3; k++) store_floats<NT>(gout + (size_t)k * a.L, s_g, 0, ntile);
+            for (int k = 0; k < 3; k++) store_floats<NT>(gout + (size_t)k * a.L, nullptr, 0, ntile);
             __syncthreads();
             continue;
         }
@@ -401,88 +504,73 @@ __global__ void __launch_bounds__(NT) a2b_bwd_f32_kernel(A2bArgs a) {
         __syncthreads();
 
         const bool chain_end = (s0 + nreal == len);
-        float cs[R][3], sn[R][3];
-        Frame<float> exc = tile_local_scan<R, NT>(a, s_ang, nreal, chain_end, cs, sn, s_wtot);
+        const int j0 = tid * R;
+        Frame<float> agg = walk_local<R, NT>(a, s_tab, s_ang[0], s_ang[1], s_ang[2], j0, nreal, chain_end, s_loc);
+        const float nx = agg.p[0], ny = agg.p[1], nz = agg.p[2];  // N after the thread's last residue
+        Frame<float> exc = warp_exclusive(agg, a.renorm, s_wtot);
         __syncthreads();
 
-        double org64[3] = {0.0, 0.0, 0.0};
-        if (tid == 0) {
-            Frame<float> run;
-            frame_identity(run);
-            Frame<float> pre[NW];
-#pragma unroll
-            for (int ww = 0; ww < NW; ww++) {
-                pre[ww] = run;
-                run = compose(run, s_wtot[ww]);
-                if (a.renorm) renormalize(run);
+        if (w == 0) {
+            Frame<float> tile;
+            Frame<float> wexc = warp_totals_scan<NW>(s_wtot, a.renorm, tile);
+            Frame<float> c32;
+            if (t == 0) frame_identity(c32);
+            else frame_load(c32, a.rec[(size_t)b * a.ntiles + t].fexc);
+            if (tid == 0) {
+                s_org[0] = c32.p[0]; s_org[1] = c32.p[1]; s_org[2] = c32.p[2];
             }
-            Frame<double> carry;
-            if (t == 0) frame_identity(carry);
-            else frame_load(carry, a.rec[(size_t)b * a.ntiles + t].fexc);
-            Frame<float> c32 = frame_cast<float>(carry);
             c32.p[0] = c32.p[1] = c32.p[2] = 0.f;
-#pragma unroll
-            for (int ww = 0; ww < NW; ww++) s_wpre[ww] = compose(c32, pre[ww]);
-            // tile origin: the forward's positions are (relative position) + float(carry.p)
-            org64[0] = (double)(float)carry.p[0];
-            org64[1] = (double)(float)carry.p[1];
-            org64[2] = (double)(float)carry.p[2];
+            if (tid < NW) s_wpre[tid] = compose(c32, wexc);
         }
         __syncthreads();
 
-        // walk 2: positions relative to the tile origin, joint axes, thread sums
         Frame<float> P = compose(s_wpre[w], exc);
         if (a.renorm) renormalize(P);
-        float x[R][3][3], u[R][3][3], xn[R][3];
-        float G[3] = {0.f, 0.f, 0.f}, S[3] = {0.f, 0.f, 0.f};
-        const int j0 = tid * R;
+        // rotate this thread's upstream gradients into its local frame (in place)
+        // and sum G' = sum g', S' = sum x_local x g'
+        float Gl[3] = {0.f, 0.f, 0.f}, Sl[3] = {0.f, 0.f, 0.f};
+        const float *lp = s_loc + tid;
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const int j = j0 + r;
-#pragma unroll
-            for (int q = 0; q < 3; q++) {
-#pragma unroll
-                for (int c = 0; c < 3; c++) x[r][q][c] = u[r][q][c] = 0.f;
-                xn[r][q] = 0.f;
-            }
             if (j < nreal) {
 #pragma unroll
                 for (int q = 0; q < 3; q++) {
-#pragma unroll
-                    for (int c = 0; c < 3; c++) x[r][q][c] = P.p[c];
-                    apply_joint(P, a.bc.cb[q], a.bc.sb[q], a.bc.d[q], cs[r][q], sn[r][q]);
-#pragma unroll
-                    for (int c = 0; c < 3; c++) u[r][q][c] = P.r[3 * c];
-                }
-#pragma unroll
-                for (int c = 0; c < 3; c++) xn[r][c] = P.p[c];
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    const float *g = s_g + 9 * j + 3 * q;
-                    float xg[3];
-                    cross3(x[r][q], g, xg);
+                    float *gp = s_g + 9 * j + 3 * q;
+                    float gw[3] = {gp[0], gp[1], gp[2]}, gl[3], xg[3];
+                    rot_t(P, gw, gl);
+                    gp[0] = gl[0]; gp[1] = gl[1]; gp[2] = gl[2];
+                    const float xq[3] = {lp[(9 * r + 3 * q) * NT], lp[(9 * r + 3 * q + 1) * NT],
+                                         lp[(9 * r + 3 * q + 2) * NT]};
+                    cross3(xq, gl, xg);
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
-                        G[c] += g[c];
-                        S[c] += xg[c];
+                        Gl[c] += gl[c];
+                        Sl[c] += xg[c];
                     }
                 }
             }
         }
-        // block-exclusive suffix of (G, S) over threads
-        float suf[6], wt[6];
-        const float v[6] = {G[0], G[1], G[2], S[0], S[1], S[2]};
+        // thread totals in the tile frame: G = R G', S = R S' + p x G
+        float Gt[3], St[3], pxg[3];
+        rot(P, Gl, Gt);
+        rot(P, Sl, St);
+        cross3(P.p, Gt, pxg);
 #pragma unroll
-        for (int i = 0; i < 6; i++) suf[i] = warp_suffix_exclusive(v[i], lane, wt[i]);
+        for (int c = 0; c < 3; c++) St[c] += pxg[c];
+        float suf[6], wt[6];
+        const float v6[6] = {Gt[0], Gt[1], Gt[2], St[0], St[1], St[2]};
+#pragma unroll
+        for (int i = 0; i < 6; i++) suf[i] = warp_suffix_exclusive(v6[i], lane, wt[i]);
         if (lane == 0)
 #pragma unroll
             for (int i = 0; i < 6; i++) s_wsum[w][i] = wt[i];
         __syncthreads();
         if (tid == 0) {
+            const double org64[3] = {(double)s_org[0], (double)s_org[1], (double)s_org[2]};
             double tot[6] = {0, 0, 0, 0, 0, 0};
             for (int ww = 0; ww < NW; ww++)
                 for (int i = 0; i < 6; i++) tot[i] += (double)s_wsum[ww][i];
-            // S about the world origin: S_world = S_o + o x G
             double own[6], oxg[3];
             cross3(org64, tot, oxg);
             for (int i = 0; i < 3; i++) {
@@ -492,7 +580,6 @@ __global__ void __launch_bounds__(NT) a2b_bwd_f32_kernel(A2bArgs a) {
             const int t_last = (len - 1) / TILE;
             double cw[6];
             backward_suffix(a, b, t, t_last, own, s_epoch, cw);
-            // back to the tile origin: S_o = S_world - o x G
             double oxc[3];
             cross3(org64, cw, oxc);
             float run[6];
@@ -507,60 +594,88 @@ __global__ void __launch_bounds__(NT) a2b_bwd_f32_kernel(A2bArgs a) {
                 }
         }
         __syncthreads();
-        // walk 3: residues in reverse with the running suffix (atoms after residue j)
-        float Gr[3], Sr[3];
+        // incoming suffix (atoms after this thread) in the thread's local frame:
+        // G' = R^T G, S' = R^T (S - p x G)
+        float Gw[3], Sw[3], G[3], S[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            Gr[c] = suf[c] + s_wsuf[w][c];
-            Sr[c] = suf[3 + c] + s_wsuf[w][3 + c];
+            Gw[c] = suf[c] + s_wsuf[w][c];
+            Sw[c] = suf[3 + c] + s_wsuf[w][3 + c];
         }
+        cross3(P.p, Gw, pxg);
+#pragma unroll
+        for (int c = 0; c < 3; c++) Sw[c] -= pxg[c];
+        rot_t(P, Gw, G);
+        rot_t(P, Sw, S);
+
         float(*s_gr)[TILE] = s_ang;  // angles are no longer needed: stage gradients there
+        float nxt[3] = {nx, ny, nz};
 #pragma unroll
         for (int r = R - 1; r >= 0; r--) {
             const int j = j0 + r;
+            float xN[3], xA[3], xC[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                xN[c] = lp[(9 * r + c) * NT];
+                xA[c] = lp[(9 * r + 3 + c) * NT];
+                xC[c] = lp[(9 * r + 6 + c) * NT];
+            }
             if (j < nreal) {
-                float tmp[3], cr[3];
-                // omega_j: axis u[r][2], origin = N_{j+1}
-                cross3(xn[r], Gr, cr);
-                for (int c = 0; c < 3; c++) tmp[c] = Sr[c] - cr[c];
-                const float gom = u[r][2][0] * tmp[0] + u[r][2][1] * tmp[1] + u[r][2][2] * tmp[2];
-                // psi_j: axis u[r][1], origin C_j (same atom set: everything from N_{j+1})
-                cross3(x[r][2], Gr, cr);
-                for (int c = 0; c < 3; c++) tmp[c] = Sr[c] - cr[c];
-                const float gps = u[r][1][0] * tmp[0] + u[r][1][1] * tmp[1] + u[r][1][2] * tmp[2];
-                // add C_j
-                {
-                    const float *g = s_g + 9 * j + 6;
-                    cross3(x[r][2], g, cr);
-                    for (int c = 0; c < 3; c++) {
-                        Gr[c] += g[c];
-                        Sr[c] += cr[c];
-                    }
+                const float *g = s_g + 9 * j;
+                float u[3], tmp[3], cr[3];
+                // omega_j: axis C -> N_{j+1}, origin N_{j+1}; subtree = atoms from N_{j+1} on
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (nxt[c] - xC[c]) * inv_d2;
+                cross3(nxt, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                const float gom = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                // psi_j: axis CA -> C, origin C; same subtree
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xC[c] - xA[c]) * inv_d1;
+                cross3(xC, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                const float gps = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                // C_j joins the subtree of phi_j
+                cross3(xC, g + 6, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += g[6 + c];
+                    S[c] += cr[c];
                 }
-                // phi_j: axis u[r][0], origin CA_j
-                cross3(x[r][1], Gr, cr);
-                for (int c = 0; c < 3; c++) tmp[c] = Sr[c] - cr[c];
-                const float gph = u[r][0][0] * tmp[0] + u[r][0][1] * tmp[1] + u[r][0][2] * tmp[2];
-                // add CA_j and N_j
-                for (int q = 1; q >= 0; q--) {
-                    const float *g = s_g + 9 * j + 3 * q;
-                    cross3(x[r][q], g, cr);
-                    for (int c = 0; c < 3; c++) {
-                        Gr[c] += g[c];
-                        Sr[c] += cr[c];
-                    }
+                // phi_j: axis N -> CA, origin CA
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xA[c] - xN[c]) * inv_d0;
+                cross3(xA, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                const float gph = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                // CA_j and N_j join the suffix of residue j-1
+                cross3(xA, g + 3, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += g[3 + c];
+                    S[c] += cr[c];
+                }
+                cross3(xN, g, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += g[c];
+                    S[c] += cr[c];
                 }
                 const bool last = chain_end && (j == nreal - 1);
                 s_gr[0][j] = gph;
                 s_gr[1][j] = last ? 0.f : gps;
                 s_gr[2][j] = last ? 0.f : gom;
             }
+#pragma unroll
+            for (int c = 0; c < 3; c++) nxt[c] = xN[c];
         }
         __syncthreads();
         for (int k = 0; k < 3; k++) store_floats<NT>(gout + (size_t)k * a.L, s_gr[k], nreal, ntile);
         __syncthreads();
     }
-    (void)s_fepoch;
     finish_launch(&a.hdr->bwd_ticket, &a.hdr->bwd_done, &a.hdr->bwd_epoch);
 }
 
@@ -769,7 +884,7 @@ __global__ void __launch_bounds__(kPlainThreads) a2b_bwd_f64_plain_kernel(PlainA
 
 // ------------------------------------------------------------------- host side
 template <typename K>
-static int persistent_grid(K kernel, int threads, int items, int max_ctas) {
+static int persistent_grid(K kernel, int threads, int items, int max_ctas, int dyn_smem = 0) {
     static int num_sms = 0;
     if (!num_sms) {
         int dev = 0;
@@ -778,7 +893,8 @@ static int persistent_grid(K kernel, int threads, int items, int max_ctas) {
         if (num_sms <= 0) num_sms = 1;
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem) != cudaSuccess ||
+        per_sm < 1)
         per_sm = 1;
     int grid = num_sms * per_sm;
     if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
@@ -790,19 +906,13 @@ struct A2bShape {
     int R, NT;
 };
 
-// Forward: NT = 128 threads, R residues each.  Backward: same tile (it re-reads
-// the forward's per-tile carries) with half the residues per thread and twice
-// the threads, because each backward thread keeps 18 R positions and axes live.
+// Forward and backward share the tile (the backward re-reads the forward's
+// per-tile carries): NT = 128 threads of R residues.
 static A2bShape a2b_shape(const tpl_options &opt, bool backward) {
+    (void)backward;
     A2bShape s;
-    const int rf = opt.residues_per_thread > 0 ? opt.residues_per_thread : 4;
-    if (!backward || rf == 1) {
-        s.R = rf;
-        s.NT = 128;
-    } else {
-        s.R = rf / 2;
-        s.NT = 256;
-    }
+    s.R = opt.residues_per_thread > 0 ? opt.residues_per_thread : 4;
+    s.NT = 128;
     return s;
 }
 
@@ -833,15 +943,21 @@ static A2bArgs make_args(const float *angles, const int32_t *lengths, void *ws, 
 template <int R>
 static int launch_fwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
     auto k = a2b_fwd_f32_kernel<R, 128>;
-    int grid = persistent_grid(k, 128, a.total, max_ctas);
-    k<<<grid, 128, 0, st>>>(a);
+    const int smem = 12 * R * 128 * (int)sizeof(float);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return TPL_ERR_LAUNCH;
+    int grid = persistent_grid(k, 128, a.total, max_ctas, smem);
+    k<<<grid, 128, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 template <int R, int NT>
 static int launch_bwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
     auto k = a2b_bwd_f32_kernel<R, NT>;
-    int grid = persistent_grid(k, NT, a.total, max_ctas);
-    k<<<grid, NT, 0, st>>>(a);
+    const int smem = 21 * R * NT * (int)sizeof(float);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return TPL_ERR_LAUNCH;
+    int grid = persistent_grid(k, NT, a.total, max_ctas, smem);
+    k<<<grid, NT, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
@@ -867,10 +983,12 @@ int a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.grad_angles = grad_angles;
     a.grad_coords = grad_coords;
-    if (s.NT == 128 && s.R == 1) return launch_bwd<1, 128>(a, opt.max_ctas, st);
-    if (s.NT == 256 && s.R == 1) return launch_bwd<1, 256>(a, opt.max_ctas, st);
-    if (s.NT == 256 && s.R == 2) return launch_bwd<2, 256>(a, opt.max_ctas, st);
-    if (s.NT == 256 && s.R == 4) return launch_bwd<4, 256>(a, opt.max_ctas, st);
+    switch (s.R) {
+        case 1: return launch_bwd<1, 128>(a, opt.max_ctas, st);
+        case 2: return launch_bwd<2, 128>(a, opt.max_ctas, st);
+        case 4: return launch_bwd<4, 128>(a, opt.max_ctas, st);
+        case 8: return launch_bwd<8, 128>(a, opt.max_ctas, st);
+    }
     return TPL_ERR_UNSUPPORTED;
 }
 

@@ -1,0 +1,671 @@
+// Angles2Coords kernels for sm_103a (the reference has no GPU path here: it
+// builds one heap-allocated node graph per chain on the CPU,
+// Layers/FullAtomModel/cConformation.cpp:30-211, OpenMP over chains in
+// Angles2Coords/angles2coords_interface.cpp:27,92).
+//
+// One CTA per chain, looping over tiles of R*NT residues with the carry (frame
+// and atom offset) kept in shared memory.  Inside a tile the backbone is the
+// same parallel scan as Angles2Backbone (per-thread joint products, warp
+// shuffles, shared-memory warp totals); the atom offsets of the residues are an
+// integer scan of per-residue atom counts carried alongside.  Each thread then
+// walks its residues from its world frame and places every atom of each residue
+// (backbone, Pro ring, side-chain joints below the dummy transform, carbonyl),
+// stages them in shared memory and the tile's contiguous atom range is written
+// with coalesced stores.
+//
+// The backward is the adjoint of the same tree: for a joint with axis u and
+// origin o, dL/dalpha = u . sum over its subtree of (x - o) x g.  Subtrees of the
+// backbone joints are "everything after" in atom order (plus the residue's own
+// side chain for phi), so the kernel scans (G, S) = (sum g, sum x x g) backwards
+// over tiles, threads and residues; side-chain joints use prefix sums over the
+// side-chain path of their residue.  Complexity O(atoms) per chain instead of
+// the reference's O(nodes x subtree).
+#include <cstdio>
+
+#include "tpl_common.cuh"
+#include "tpl_internal.h"
+#include "tpl_topology.cuh"
+
+namespace tpl {
+
+__device__ const Topology<float> g_topo_f32 = make_topology<float>();
+__device__ const Topology<double> g_topo_f64 = make_topology<double>();
+
+template <typename T>
+__device__ __forceinline__ const Topology<T> &topo_global();
+template <>
+__device__ __forceinline__ const Topology<float> &topo_global<float>() { return g_topo_f32; }
+template <>
+__device__ __forceinline__ const Topology<double> &topo_global<double>() { return g_topo_f64; }
+
+template <typename T>
+struct A2cArgs {
+    const unsigned char *seq;
+    int seq_stride;
+    const T *angles;
+    T *coords;
+    uint32_t *res_names;
+    uint32_t *atom_names;
+    T *grad_angles;
+    const T *grad_coords;
+    WsHeader *hdr;
+    int L, maxA;
+};
+
+__device__ __forceinline__ void a2c_error(WsHeader *h, int code) {
+    if (h) atomicCAS(&h->status, 0u, (unsigned)code);
+}
+
+template <typename T>
+__device__ __forceinline__ void sc(T a, T *s, T *c) { sincos_t(a, s, c); }
+
+template <typename T>
+__device__ __forceinline__ void renorm_if(Frame<T> &f, bool on) {
+    if (on) renormalize(f);
+}
+
+// Shared-memory layout of the tile buffers (dynamic).
+template <typename T, int TILE>
+struct A2cSmem {
+    Topology<T> topo;
+    T ang[8][TILE];
+    T xyz[TILE * kMaxResAtoms * 3];
+    signed char type[TILE];
+    signed char lut[256];
+};
+
+template <typename T, int TILE>
+struct A2cSmemBwd {
+    A2cSmem<T, TILE> f;
+    T g[TILE * kMaxResAtoms * 3];
+};
+
+// Copy the topology to shared memory and build the letter -> type table.
+template <typename T, int NT>
+__device__ __forceinline__ void load_topology(Topology<T> &dst, signed char *lut) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&topo_global<T>());
+    uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
+    constexpr int n = sizeof(Topology<T>) / 4;
+    static_assert(sizeof(Topology<T>) % 4 == 0, "topology size");
+    for (int i = threadIdx.x; i < n; i += NT) d[i] = src[i];
+    for (int i = threadIdx.x; i < 256; i += NT) lut[i] = (signed char)residue_type((unsigned char)i);
+}
+
+// Chain length = index of the first NUL of the sequence row (at most the row
+// stride); every letter before it must be one of the 20 residues.
+template <int NT>
+__device__ __forceinline__ int chain_length(const unsigned char *row, int stride, const signed char *lut, int *s_len,
+                                            int *s_bad) {
+    if (threadIdx.x == 0) {
+        *s_len = stride;
+        *s_bad = 0;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < stride; j += NT)
+        if (row[j] == 0) atomicMin(s_len, j);
+    __syncthreads();
+    const int len = *s_len;
+    for (int j = threadIdx.x; j < len; j += NT)
+        if (lut[row[j]] < 0) *s_bad = 1;
+    __syncthreads();
+    return len;
+}
+
+// Per-thread scan state for one tile: backbone aggregate of the thread's
+// residues, its exclusive prefix inside the warp, atom counts.
+template <typename T, int R, int NT>
+struct TileScan {
+    T cs[R][3], sn[R][3];
+    Frame<T> exc;     // exclusive prefix inside the warp
+    int cnt_exc;      // atoms before this thread inside the warp
+    int cnt_own;      // atoms of this thread
+};
+
+template <typename T, int R, int NT>
+__device__ __forceinline__ void a2c_tile_scan(const Topology<T> &tp, const T (*ang)[R * NT],
+                                              const signed char *type, int n, bool chain_end, bool renorm,
+                                              TileScan<T, R, NT> &ts, Frame<T> *s_wtot, int *s_wcnt) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    Frame<T> agg;
+    frame_identity(agg);
+    int cnt = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int j = tid * R + r;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            ts.cs[r][k] = T(1);
+            ts.sn[r][k] = T(0);
+        }
+        if (j < n) {
+            cnt += tp.natoms[type[j]];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (k == 2 && chain_end && j == n - 1) break;
+                sc(ang[k][j], &ts.sn[r][k], &ts.cs[r][k]);
+                apply_joint(agg, tp.bb_cb[k], tp.bb_sb[k], tp.bb_d[k], ts.cs[r][k], ts.sn[r][k]);
+            }
+        }
+    }
+    renorm_if(agg, renorm);
+    Frame<T> inc = warp_scan_frames(agg, lane);
+    ts.exc = shfl_up_frame(inc, 1);
+    if (lane == 0) frame_identity(ts.exc);
+    int ci = cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int o = __shfl_up_sync(0xffffffffu, ci, off);
+        if (lane >= off) ci += o;
+    }
+    ts.cnt_exc = ci - cnt;
+    ts.cnt_own = cnt;
+    if (lane == 31) {
+        s_wtot[w] = inc;
+        s_wcnt[w] = ci;
+    }
+}
+
+// Thread 0: warp prefixes with the tile carry folded in (rotation only: positions
+// are relative to the tile origin), the tile aggregate and the tile atom count.
+template <typename T, int NW>
+__device__ __forceinline__ void a2c_tile_prefix(const Frame<T> &carry, const Frame<T> *s_wtot, const int *s_wcnt,
+                                                bool renorm, Frame<T> *s_wpre, int *s_wcpre, Frame<T> &tile_agg,
+                                                int &tile_cnt) {
+    Frame<T> run;
+    frame_identity(run);
+    Frame<T> c0 = carry;
+    c0.p[0] = c0.p[1] = c0.p[2] = T(0);
+    int cr = 0;
+    for (int w = 0; w < NW; w++) {
+        s_wpre[w] = compose(c0, run);
+        s_wcpre[w] = cr;
+        run = compose(run, s_wtot[w]);
+        renorm_if(run, renorm);
+        cr += s_wcnt[w];
+    }
+    tile_agg = run;
+    tile_cnt = cr;
+}
+
+// All atoms of residue j (type ty) from the frame P at its N atom.  emit(slot, xyz)
+// receives positions in P's coordinates; returns the frame at the next N.
+template <typename T, typename Emit>
+__device__ __forceinline__ void residue_atoms(const Topology<T> &tp, int ty, Frame<T> &P, const T cs[3],
+                                              const T sn[3], const T *chi_ang, int chi_stride, Emit emit) {
+    emit(0, P.p);
+    Frame<T> F = P;
+    apply_joint(F, tp.bb_cb[0], tp.bb_sb[0], tp.bb_d[0], cs[0], sn[0]);
+    emit(1, F.p);
+    const int na = tp.natoms[ty];
+    if (tp.pro[ty]) {
+        for (int a = 0; a < 3; a++) {
+            T x[3];
+            frame_point(F, tp.pro_local[a][0], tp.pro_local[a][1], tp.pro_local[a][2], x);
+            emit(2 + a, x);
+        }
+    }
+    const int nj = tp.njoints[ty];
+    if (nj > 0) {
+        Frame<T> S = F;
+        apply_rx(S, tp.dummy_c, tp.dummy_s);
+        for (int k = 0; k < nj; k++) {
+            const int chi = tp.jchi[ty][k];
+            T c = T(1), s = T(0);
+            if (chi >= 0) sc(chi_ang[(size_t)chi * chi_stride], &s, &c);
+            apply_joint(S, tp.jcb[ty][k], tp.jsb[ty][k], tp.jd[ty][k], c, s);
+            const int f0 = tp.jfirst[ty][k];
+            for (int a = 0; a < tp.jna[ty][k]; a++) {
+                T x[3];
+                frame_point(S, tp.sc[ty][f0 + a][0], tp.sc[ty][f0 + a][1], tp.sc[ty][f0 + a][2], x);
+                emit(2 + f0 + a, x);
+            }
+        }
+    }
+    Frame<T> C = F;
+    apply_joint(C, tp.bb_cb[1], tp.bb_sb[1], tp.bb_d[1], cs[1], sn[1]);
+    emit(na - 2, C.p);
+    {
+        T x[3];
+        frame_point(C, tp.o_local[0], tp.o_local[1], tp.o_local[2], x);
+        emit(na - 1, x);
+    }
+    P = C;
+    apply_joint(P, tp.bb_cb[2], tp.bb_sb[2], tp.bb_d[2], cs[2], sn[2]);
+}
+
+template <typename T, int NT>
+__device__ __forceinline__ void store_tile_atoms(T *dst, const T *src, const T org[3], int n_atoms) {
+    // dst: global coords of the tile's first atom (3 * n_atoms values, xyz interleaved)
+    for (int i = threadIdx.x; i < 3 * n_atoms; i += NT) dst[i] = src[i] + org[i % 3];
+}
+
+template <typename T, int R, int NT>
+__global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
+    constexpr int TILE = R * NT, NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    A2cSmem<T, TILE> &sm = *reinterpret_cast<A2cSmem<T, TILE> *>(smem_raw);
+    __shared__ Frame<T> s_wtot[NW], s_wpre[NW];
+    __shared__ int s_wcnt[NW], s_wcpre[NW];
+    __shared__ Frame<T> s_carry;
+    __shared__ T s_org[3];
+    __shared__ int s_len, s_bad, s_abase, s_tcnt;
+
+    const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    load_topology<T, NT>(sm.topo, sm.lut);
+    const unsigned char *row = a.seq + (size_t)b * a.seq_stride;
+    int len = chain_length<NT>(row, a.seq_stride, sm.lut, &s_len, &s_bad);
+    T *out = a.coords + (size_t)b * 3 * a.maxA;
+    uint32_t *rn = a.res_names ? a.res_names + (size_t)b * a.maxA : nullptr;
+    uint32_t *an = a.atom_names ? a.atom_names + (size_t)b * a.maxA : nullptr;
+    bool ok = true;
+    if (s_bad) {
+        if (tid == 0) a2c_error(a.hdr, TPL_ERR_SEQUENCE);
+        ok = false;
+    }
+    if (len > a.L) {
+        if (tid == 0) a2c_error(a.hdr, TPL_ERR_LENGTH);
+        ok = false;
+    }
+    if (tid == 0) {
+        frame_identity(s_carry);
+        s_abase = 0;
+    }
+    __syncthreads();
+    const T *ang_b = a.angles + (size_t)b * 8 * a.L;
+    for (int s0 = 0; ok && s0 < len; s0 += TILE) {
+        const int n = min(TILE, len - s0);
+        for (int k = 0; k < 8; k++)
+            for (int i = tid; i < n; i += NT) sm.ang[k][i] = ang_b[(size_t)k * a.L + s0 + i];
+        for (int i = tid; i < n; i += NT) sm.type[i] = sm.lut[row[s0 + i]];
+        __syncthreads();
+        const bool chain_end = (s0 + n == len);
+        TileScan<T, R, NT> ts;
+        a2c_tile_scan<T, R, NT>(sm.topo, sm.ang, sm.type, n, chain_end, renorm, ts, s_wtot, s_wcnt);
+        __syncthreads();
+        if (tid == 0) {
+            Frame<T> agg;
+            int tcnt;
+            a2c_tile_prefix<T, NW>(s_carry, s_wtot, s_wcnt, renorm, s_wpre, s_wcpre, agg, tcnt);
+            s_org[0] = s_carry.p[0]; s_org[1] = s_carry.p[1]; s_org[2] = s_carry.p[2];
+            s_tcnt = tcnt;
+            Frame<T> nc = compose(s_carry, agg);
+            renorm_if(nc, renorm);
+            s_carry = nc;
+        }
+        __syncthreads();
+        Frame<T> P = compose(s_wpre[w], ts.exc);
+        renorm_if(P, renorm);
+        int aoff = s_wcpre[w] + ts.cnt_exc;  // first atom of this thread inside the tile
+        const int abase = s_abase;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int j = tid * R + r;
+            if (j < n) {
+                const int ty = sm.type[j];
+                T *dst = sm.xyz + 3 * aoff;
+                const int gatom = abase + aoff;
+                residue_atoms<T>(sm.topo, ty, P, ts.cs[r], ts.sn[r], &sm.ang[3][j], TILE,
+                                 [&](int slot, const T *x) {
+                                     dst[3 * slot] = x[0];
+                                     dst[3 * slot + 1] = x[1];
+                                     dst[3 * slot + 2] = x[2];
+                                 });
+                if (rn && an) {
+                    const int na = sm.topo.natoms[ty];
+                    for (int k = 0; k < na && gatom + k < a.maxA; k++) {
+                        rn[gatom + k] = sm.topo.res_name[ty];
+                        an[gatom + k] = sm.topo.atom_name[ty][k];
+                    }
+                }
+                aoff += sm.topo.natoms[ty];
+            }
+        }
+        __syncthreads();
+        const int tcnt = s_tcnt;
+        const int nstore = max(0, min(tcnt, a.maxA - abase));
+        const T org[3] = {s_org[0], s_org[1], s_org[2]};
+        store_tile_atoms<T, NT>(out + (size_t)3 * abase, sm.xyz, org, nstore);
+        __syncthreads();
+        if (tid == 0) s_abase = abase + tcnt;
+        __syncthreads();
+    }
+    int total = ok ? s_abase : 0;
+    if (total > a.maxA) {
+        if (tid == 0) a2c_error(a.hdr, TPL_ERR_ATOMS);
+        total = a.maxA;
+    }
+    for (int i = 3 * total + tid; i < 3 * a.maxA; i += NT) out[i] = T(0);
+    if (rn && an)
+        for (int i = total + tid; i < a.maxA; i += NT) rn[i] = an[i] = 0u;
+    (void)lane;
+}
+
+// ------------------------------------------------------------------ backward
+template <typename T, int R, int NT>
+__global__ void __launch_bounds__(NT) a2c_bwd_kernel(A2cArgs<T> a, int renorm, int max_tiles) {
+    constexpr int TILE = R * NT, NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    A2cSmemBwd<T, TILE> &sm = *reinterpret_cast<A2cSmemBwd<T, TILE> *>(smem_raw);
+    Frame<T> *s_carries = reinterpret_cast<Frame<T> *>(smem_raw + sizeof(A2cSmemBwd<T, TILE>));
+    int *s_tbase = reinterpret_cast<int *>(s_carries + max_tiles);
+    __shared__ Frame<T> s_wtot[NW], s_wpre[NW];
+    __shared__ int s_wcnt[NW], s_wcpre[NW];
+    __shared__ T s_wsum[NW][6], s_wsuf[NW][6];
+    __shared__ double s_tail[6];
+    __shared__ int s_len, s_bad;
+
+    const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    load_topology<T, NT>(sm.f.topo, sm.f.lut);
+    const Topology<T> &tp = sm.f.topo;
+    const unsigned char *row = a.seq + (size_t)b * a.seq_stride;
+    int len = chain_length<NT>(row, a.seq_stride, sm.f.lut, &s_len, &s_bad);
+    T *gout = a.grad_angles + (size_t)b * 8 * a.L;
+    const T *gin = a.grad_coords + (size_t)b * 3 * a.maxA;
+    const T *ang_b = a.angles + (size_t)b * 8 * a.L;
+    bool ok = !s_bad && len <= a.L;
+    if (tid == 0) {
+        if (s_bad) a2c_error(a.hdr, TPL_ERR_SEQUENCE);
+        if (len > a.L) a2c_error(a.hdr, TPL_ERR_LENGTH);
+    }
+    const int ntiles = ok ? (len + TILE - 1) / TILE : 0;
+    if (ntiles > max_tiles) {
+        if (tid == 0) a2c_error(a.hdr, TPL_ERR_ARGUMENT);
+        ok = false;
+    }
+    // sweep 1: tile carries and atom bases
+    if (tid == 0) {
+        frame_identity(s_carries[0]);
+        s_tbase[0] = 0;
+    }
+    __syncthreads();
+    for (int t = 0; ok && t < ntiles; t++) {
+        const int s0 = t * TILE, n = min(TILE, len - s0);
+        for (int k = 0; k < 3; k++)
+            for (int i = tid; i < n; i += NT) sm.f.ang[k][i] = ang_b[(size_t)k * a.L + s0 + i];
+        for (int i = tid; i < n; i += NT) sm.f.type[i] = sm.f.lut[row[s0 + i]];
+        __syncthreads();
+        TileScan<T, R, NT> ts;
+        a2c_tile_scan<T, R, NT>(tp, sm.f.ang, sm.f.type, n, s0 + n == len, renorm, ts, s_wtot, s_wcnt);
+        __syncthreads();
+        if (tid == 0) {
+            Frame<T> agg;
+            int tcnt;
+            a2c_tile_prefix<T, NW>(s_carries[t], s_wtot, s_wcnt, renorm, s_wpre, s_wcpre, agg, tcnt);
+            if (t + 1 < max_tiles) {
+                Frame<T> nc = compose(s_carries[t], agg);
+                renorm_if(nc, renorm);
+                s_carries[t + 1] = nc;
+                s_tbase[t + 1] = s_tbase[t] + tcnt;
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0)
+        for (int i = 0; i < 6; i++) s_tail[i] = 0.0;
+    __syncthreads();
+    // sweep 2: tiles last-first
+    for (int t = ntiles - 1; ok && t >= 0; t--) {
+        const int s0 = t * TILE, n = min(TILE, len - s0);
+        const int abase = s_tbase[t];
+        for (int k = 0; k < 8; k++)
+            for (int i = tid; i < n; i += NT) sm.f.ang[k][i] = ang_b[(size_t)k * a.L + s0 + i];
+        for (int i = tid; i < n; i += NT) sm.f.type[i] = sm.f.lut[row[s0 + i]];
+        __syncthreads();
+        TileScan<T, R, NT> ts;
+        a2c_tile_scan<T, R, NT>(tp, sm.f.ang, sm.f.type, n, s0 + n == len, renorm, ts, s_wtot, s_wcnt);
+        __syncthreads();
+        if (tid == 0) {
+            Frame<T> agg;
+            int tcnt;
+            a2c_tile_prefix<T, NW>(s_carries[t], s_wtot, s_wcnt, renorm, s_wpre, s_wcpre, agg, tcnt);
+            s_wcnt[0] = tcnt;  // reuse: tile atom count
+        }
+        __syncthreads();
+        const int tcnt = s_wcnt[0];
+        const int nload = max(0, min(tcnt, a.maxA - abase));
+        for (int i = tid; i < 3 * tcnt; i += NT) sm.g[i] = i < 3 * nload ? gin[(size_t)3 * abase + i] : T(0);
+        Frame<T> P = compose(s_wpre[w], ts.exc);
+        renorm_if(P, renorm);
+        Frame<T> start[R];
+        int roff[R];
+        int aoff = s_wcpre[w] + ts.cnt_exc;
+        __syncthreads();  // sm.g complete
+        T G[3] = {0, 0, 0}, S[3] = {0, 0, 0};
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int j = tid * R + r;
+            start[r] = P;
+            roff[r] = aoff;
+            if (j < n) {
+                const int ty = sm.f.type[j];
+                T *dst = sm.f.xyz + 3 * aoff;
+                const T *gg = sm.g + 3 * aoff;
+                residue_atoms<T>(tp, ty, P, ts.cs[r], ts.sn[r], &sm.f.ang[3][j], TILE, [&](int slot, const T *x) {
+                    dst[3 * slot] = x[0];
+                    dst[3 * slot + 1] = x[1];
+                    dst[3 * slot + 2] = x[2];
+                    T xg[3];
+                    cross3(x, gg + 3 * slot, xg);
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += gg[3 * slot + c];
+                        S[c] += xg[c];
+                    }
+                });
+                aoff += tp.natoms[ty];
+            }
+        }
+        // block-exclusive suffix over threads, plus the carry from later tiles
+        T suf[6];
+        const T v[6] = {G[0], G[1], G[2], S[0], S[1], S[2]};
+        for (int i = 0; i < 6; i++) {
+            T inc = v[i];
+            for (int off = 1; off < 32; off <<= 1) {
+                T o = __shfl_down_sync(0xffffffffu, inc, off);
+                if (lane + off < 32) inc += o;
+            }
+            T tot = __shfl_sync(0xffffffffu, inc, 0);
+            suf[i] = inc - v[i];
+            if (lane == 0) s_wsum[w][i] = tot;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            // later tiles' (G, S) are kept about the world origin in FP64; move them
+            // to this tile's origin o: S_o = S_world - o x G
+            const double o[3] = {(double)s_carries[t].p[0], (double)s_carries[t].p[1], (double)s_carries[t].p[2]};
+            double ox[3];
+            cross3(o, s_tail, ox);
+            double run[6];
+            for (int i = 0; i < 3; i++) {
+                run[i] = s_tail[i];
+                run[3 + i] = s_tail[3 + i] - ox[i];
+            }
+            double tot[6] = {0, 0, 0, 0, 0, 0};
+            for (int ww = NW - 1; ww >= 0; ww--)
+                for (int i = 0; i < 6; i++) {
+                    s_wsuf[ww][i] = (T)run[i];
+                    run[i] += (double)s_wsum[ww][i];
+                    tot[i] += (double)s_wsum[ww][i];
+                }
+            double ot[3];
+            cross3(o, tot, ot);
+            for (int i = 0; i < 3; i++) {
+                s_tail[i] += tot[i];
+                s_tail[3 + i] += tot[3 + i] + ot[i];
+            }
+        }
+        __syncthreads();
+        T Gn[3], Sn[3];
+        for (int c = 0; c < 3; c++) {
+            Gn[c] = suf[c] + s_wsuf[w][c];
+            Sn[c] = suf[3 + c] + s_wsuf[w][3 + c];
+        }
+        T(*s_gr)[TILE] = sm.f.ang;  // angles of this tile stay in registers (ts) / are re-read below
+#pragma unroll
+        for (int r = R - 1; r >= 0; r--) {
+            const int j = tid * R + r;
+            if (j >= n) continue;
+            const int ty = sm.f.type[j];
+            const int na = tp.natoms[ty], nj = tp.njoints[ty];
+            const T *X = sm.f.xyz + 3 * roff[r];
+            const T *Gg = sm.g + 3 * roff[r];
+            // per-group sums of this residue
+            auto acc = [&](int lo, int hi, T *gs, T *ss) {
+                for (int c = 0; c < 3; c++) gs[c] = ss[c] = T(0);
+                for (int q = lo; q < hi; q++) {
+                    T xg[3];
+                    cross3(X + 3 * q, Gg + 3 * q, xg);
+                    for (int c = 0; c < 3; c++) {
+                        gs[c] += Gg[3 * q + c];
+                        ss[c] += xg[c];
+                    }
+                }
+            };
+            T Gco[3], Sco[3], Gmid[3], Smid[3], Gn0[3], Sn0[3];
+            acc(na - 2, na, Gco, Sco);
+            acc(1, na - 2, Gmid, Smid);   // CA, Pro ring / side chain
+            acc(0, 1, Gn0, Sn0);          // N
+            // frames of the residue
+            Frame<T> F = start[r];
+            apply_joint(F, tp.bb_cb[0], tp.bb_sb[0], tp.bb_d[0], ts.cs[r][0], ts.sn[r][0]);
+            Frame<T> C = F;
+            apply_joint(C, tp.bb_cb[1], tp.bb_sb[1], tp.bb_d[1], ts.cs[r][1], ts.sn[r][1]);
+            Frame<T> Nn = C;
+            apply_joint(Nn, tp.bb_cb[2], tp.bb_sb[2], tp.bb_d[2], ts.cs[r][2], ts.sn[r][2]);
+            T tmp[3], cr[3];
+            auto gradient = [&](const Frame<T> &J, const T *Gs, const T *Ss) {
+                cross3(J.p, Gs, cr);
+                for (int c = 0; c < 3; c++) tmp[c] = Ss[c] - cr[c];
+                return J.r[0] * tmp[0] + J.r[3] * tmp[1] + J.r[6] * tmp[2];
+            };
+            const bool last = (s0 + j == len - 1);
+            const T g_om = last ? T(0) : gradient(Nn, Gn, Sn);
+            T Gc[3], Sc[3];
+            for (int c = 0; c < 3; c++) {
+                Gc[c] = Gn[c] + Gco[c];
+                Sc[c] = Sn[c] + Sco[c];
+            }
+            const T g_ps = gradient(C, Gc, Sc);
+            for (int c = 0; c < 3; c++) {
+                Gc[c] += Gmid[c];
+                Sc[c] += Smid[c];
+            }
+            const T g_ph = gradient(F, Gc, Sc);
+            // side-chain joints: subtree of joint k = its group and all later groups
+            T g_chi[5] = {0, 0, 0, 0, 0};
+            if (nj > 0) {
+                T Gsc[3], Ssc[3];
+                acc(2, na - 2, Gsc, Ssc);
+                Frame<T> Sf = F;
+                apply_rx(Sf, tp.dummy_c, tp.dummy_s);
+                for (int k = 0; k < nj; k++) {
+                    const int chi = tp.jchi[ty][k];
+                    T c = T(1), s = T(0);
+                    if (chi >= 0) sc(sm.f.ang[3 + chi][j], &s, &c);
+                    apply_joint(Sf, tp.jcb[ty][k], tp.jsb[ty][k], tp.jd[ty][k], c, s);
+                    if (chi >= 0) g_chi[chi] = gradient(Sf, Gsc, Ssc);
+                    const int f0 = 2 + tp.jfirst[ty][k];
+                    T Gk[3], Sk[3];
+                    acc(f0, f0 + tp.jna[ty][k], Gk, Sk);
+                    for (int q = 0; q < 3; q++) {
+                        Gsc[q] -= Gk[q];
+                        Ssc[q] -= Sk[q];
+                    }
+                }
+            }
+            // suffix for the previous residue: this residue's atoms join it
+            for (int c = 0; c < 3; c++) {
+                Gn[c] = Gc[c] + Gn0[c];
+                Sn[c] = Sc[c] + Sn0[c];
+            }
+            // chi angles are read from shared memory above, so stage gradients in
+            // registers until every thread has finished with the angle rows
+            start[r].r[0] = g_ph; start[r].r[1] = g_ps; start[r].r[2] = g_om;
+            for (int q = 0; q < 5; q++) start[r].r[3 + q] = g_chi[q];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int j = tid * R + r;
+            if (j < n)
+                for (int q = 0; q < 8; q++) s_gr[q][j] = start[r].r[q];
+        }
+        __syncthreads();
+        for (int k = 0; k < 8; k++)
+            for (int i = tid; i < n; i += NT) gout[(size_t)k * a.L + s0 + i] = s_gr[k][i];
+        __syncthreads();
+    }
+    // zeros past the chain (and everywhere when the chain was rejected)
+    const int from = ok ? len : 0;
+    for (int k = 0; k < 8; k++)
+        for (int i = from + tid; i < a.L; i += NT) gout[(size_t)k * a.L + i] = T(0);
+}
+
+// ------------------------------------------------------------------ host side
+template <typename T, int R, int NT>
+static int launch_a2c_fwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t st) {
+    constexpr int TILE = R * NT;
+    const size_t smem = sizeof(A2cSmem<T, TILE>);
+    auto k = a2c_fwd_kernel<T, R, NT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return TPL_ERR_LAUNCH;
+    k<<<B, NT, smem, st>>>(a, renorm);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+template <typename T, int R, int NT>
+static int launch_a2c_bwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t st) {
+    constexpr int TILE = R * NT;
+    const int max_tiles = (a.L + TILE - 1) / TILE + 1;
+    const size_t smem = sizeof(A2cSmemBwd<T, TILE>) + (sizeof(Frame<T>) + sizeof(int)) * max_tiles;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((int)smem > optin) return TPL_ERR_UNSUPPORTED;
+    auto k = a2c_bwd_kernel<T, R, NT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return TPL_ERR_LAUNCH;
+    k<<<B, NT, smem, st>>>(a, renorm, max_tiles);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *angles, void *coords,
+                uint32_t *res_names, uint32_t *atom_names, void *ws, int B, int L, int maxA,
+                const tpl_options &opt, cudaStream_t st) {
+    if (B == 0) return TPL_OK;
+    const int renorm = opt.renormalize >= 0 ? 1 : 0;
+    if (f64) {
+        A2cArgs<double> a{seq, seq_stride, (const double *)angles, (double *)coords, res_names, atom_names,
+                          nullptr, nullptr, (WsHeader *)ws, L, maxA};
+        return launch_a2c_fwd<double, 1, 128>(a, B, renorm, st);
+    }
+    A2cArgs<float> a{seq, seq_stride, (const float *)angles, (float *)coords, res_names, atom_names,
+                     nullptr, nullptr, (WsHeader *)ws, L, maxA};
+    return launch_a2c_fwd<float, 2, 128>(a, B, renorm, st);
+}
+
+int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const unsigned char *seq, int seq_stride,
+                 const void *angles, void *ws, int B, int L, int maxA, const tpl_options &opt, cudaStream_t st) {
+    if (B == 0) return TPL_OK;
+    const int renorm = opt.renormalize >= 0 ? 1 : 0;
+    if (f64) {
+        A2cArgs<double> a{seq, seq_stride, (const double *)angles, nullptr, nullptr, nullptr,
+                          (double *)grad_angles, (const double *)grad_coords, (WsHeader *)ws, L, maxA};
+        return launch_a2c_bwd<double, 1, 128>(a, B, renorm, st);
+    }
+    A2cArgs<float> a{seq, seq_stride, (const float *)angles, nullptr, nullptr, nullptr, (float *)grad_angles,
+                     (const float *)grad_coords, (WsHeader *)ws, L, maxA};
+    return launch_a2c_bwd<float, 2, 128>(a, B, renorm, st);
+}
+
+int num_atoms_host(const char *seq) {
+    static constexpr Topology<double> tp = make_topology<double>();
+    int n = 0;
+    for (const char *p = seq; *p; p++) {
+        int t = residue_type((unsigned char)*p);
+        if (t < 0) return -1;
+        n += tp.natoms[t];
+    }
+    return n;
+}
+
+}  // namespace tpl

@@ -195,4 +195,74 @@ int tpl_a2b_backward_f64(double *grad_angles, const double *grad_coords, const d
                                   (cudaStream_t)stream);
 }
 
+int tpl_num_atoms(const char *sequence) {
+    if (!sequence) return TPL_ERR_ARGUMENT;
+    int n = num_atoms_host(sequence);
+    return n < 0 ? TPL_ERR_SEQUENCE : n;
+}
+
+size_t tpl_a2c_workspace_bytes(int batch, int max_len, int max_atoms, const tpl_options *opt) {
+    (void)batch; (void)max_len; (void)max_atoms; (void)opt;
+    return sizeof(WsHeader);
+}
+
+static int a2c_fwd_common(bool f64, const uint8_t *sequences, int seq_stride, const void *angles, void *coords,
+                          uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes,
+                          int batch, int max_len, int max_atoms, const tpl_options *opt, void *stream) {
+    if (batch < 0 || max_len < 0 || max_atoms < 0 || seq_stride <= 0) return TPL_ERR_ARGUMENT;
+    const tpl_options o = resolve(opt);
+    if (!options_ok(o)) return TPL_ERR_ARGUMENT;
+    if (batch == 0) return TPL_OK;
+    if (!sequences || (!angles && max_len > 0) || (!coords && max_atoms > 0)) return TPL_ERR_ARGUMENT;
+    if ((res_names == nullptr) != (atom_names == nullptr)) return TPL_ERR_ARGUMENT;
+    if (((uintptr_t)res_names & 3u) || ((uintptr_t)atom_names & 3u)) return TPL_ERR_ARGUMENT;
+    int s = check_ws(workspace, workspace_bytes, sizeof(WsHeader));
+    if (s) return s;
+    return a2c_forward(f64, sequences, seq_stride, angles, coords, (uint32_t *)res_names, (uint32_t *)atom_names,
+                       workspace, batch, max_len, max_atoms, o, (cudaStream_t)stream);
+}
+
+static int a2c_bwd_common(bool f64, void *grad_angles, const void *grad_coords, const uint8_t *sequences,
+                          int seq_stride, const void *angles, void *workspace, size_t workspace_bytes, int batch,
+                          int max_len, int max_atoms, const tpl_options *opt, void *stream) {
+    if (batch < 0 || max_len < 0 || max_atoms < 0 || seq_stride <= 0) return TPL_ERR_ARGUMENT;
+    const tpl_options o = resolve(opt);
+    if (!options_ok(o)) return TPL_ERR_ARGUMENT;
+    if (batch == 0) return TPL_OK;
+    if (!sequences || ((!angles || !grad_angles) && max_len > 0) || (!grad_coords && max_atoms > 0))
+        return TPL_ERR_ARGUMENT;
+    int s = check_ws(workspace, workspace_bytes, sizeof(WsHeader));
+    if (s) return s;
+    return a2c_backward(f64, grad_angles, grad_coords, sequences, seq_stride, angles, workspace, batch, max_len,
+                        max_atoms, o, (cudaStream_t)stream);
+}
+
+int tpl_a2c_forward_f32(const uint8_t *sequences, int seq_stride, const float *angles, float *coords,
+                        uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes, int batch,
+                        int max_len, int max_atoms, const tpl_options *opt, void *stream) {
+    return a2c_fwd_common(false, sequences, seq_stride, angles, coords, res_names, atom_names, workspace,
+                          workspace_bytes, batch, max_len, max_atoms, opt, stream);
+}
+
+int tpl_a2c_forward_f64(const uint8_t *sequences, int seq_stride, const double *angles, double *coords,
+                        uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes, int batch,
+                        int max_len, int max_atoms, const tpl_options *opt, void *stream) {
+    return a2c_fwd_common(true, sequences, seq_stride, angles, coords, res_names, atom_names, workspace,
+                          workspace_bytes, batch, max_len, max_atoms, opt, stream);
+}
+
+int tpl_a2c_backward_f32(float *grad_angles, const float *grad_coords, const uint8_t *sequences, int seq_stride,
+                         const float *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         int max_atoms, const tpl_options *opt, void *stream) {
+    return a2c_bwd_common(false, grad_angles, grad_coords, sequences, seq_stride, angles, workspace,
+                          workspace_bytes, batch, max_len, max_atoms, opt, stream);
+}
+
+int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const uint8_t *sequences, int seq_stride,
+                         const double *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
+                         int max_atoms, const tpl_options *opt, void *stream) {
+    return a2c_bwd_common(true, grad_angles, grad_coords, sequences, seq_stride, angles, workspace,
+                          workspace_bytes, batch, max_len, max_atoms, opt, stream);
+}
+
 }  // extern "C"

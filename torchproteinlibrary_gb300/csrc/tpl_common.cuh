@@ -186,3 +186,39 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
 }
 
 }  // namespace tpl
+
+namespace tpl {
+
+// ---------------------------------------------------------------- sincos
+// Table-driven sin/cos for |a| <= pi (Tang's method of tabulated breakpoints
+// plus a short Taylor correction): a = k*h + r with h = pi/32, |r| <= pi/64,
+//   sin a = S_k + (S_k (cos r - 1) + C_k sin r),  cos a = C_k + (C_k (cos r - 1) - S_k sin r),
+// where (S_k, C_k) = (sin, cos)(k h) are tabulated as hi + lo float pairs, so the
+// result is within about one rounding of the FP32 sin/cos.  sin r and cos r - 1
+// are Taylor polynomials (terms below r^7/5040 ~ 1e-13 dropped).  Arguments
+// outside [-pi, pi] take sincosf.
+struct SinCosTable {
+    float4 e[65];  // (S_hi, C_hi, S_lo, C_lo) for k = -32..32
+};
+
+// Built at compile time by make_sincos_table() in tpl_topology.cuh (FP64 trig).
+__device__ __forceinline__ void sincos_tab(const float4 *tab, float a, float *s, float *c) {
+    if (fabsf(a) > 3.14159274f) {
+        sincosf(a, s, c);
+        return;
+    }
+    constexpr float kInvH = 10.185916357881302f;       // 32 / pi
+    constexpr float kHhi = 0.09817477315664291f;        // float(pi / 32)
+    constexpr float kHlo = -2.7319618e-09f;             // pi/32 - kHhi (rounded)
+    const float k = rintf(a * kInvH);
+    float r = fmaf(-k, kHhi, a);
+    r = fmaf(-k, kHlo, r);
+    const float r2 = r * r;
+    const float sr = fmaf(r * r2, fmaf(r2, 1.0f / 120.0f, -1.0f / 6.0f), r);
+    const float cm1 = r2 * fmaf(r2, 1.0f / 24.0f, -0.5f);
+    const float4 e = tab[(int)k + 32];
+    *s = e.x + fmaf(e.x, cm1, fmaf(e.y, sr, e.z));
+    *c = e.y + fmaf(e.y, cm1, fmaf(-e.x, sr, e.w));
+}
+
+}  // namespace tpl

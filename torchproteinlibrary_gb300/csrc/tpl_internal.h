@@ -62,4 +62,12 @@ int a2b_backward_f64_plain(double *grad_angles, const double *grad_coords, const
                            const int32_t *lengths, void *ws, int B, int L, cudaStream_t st);
 int a2b_tile_for(const tpl_options &opt);
 
+// Angles2Coords launchers (tpl_a2c.cu).  ws holds at least a WsHeader (status word).
+int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *angles, void *coords,
+                uint32_t *res_names, uint32_t *atom_names, void *ws, int B, int L, int maxA,
+                const tpl_options &opt, cudaStream_t st);
+int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const unsigned char *seq, int seq_stride,
+                 const void *angles, void *ws, int B, int L, int maxA, const tpl_options &opt, cudaStream_t st);
+int num_atoms_host(const char *seq);
+
 }  // namespace tpl
