@@ -206,6 +206,23 @@ def run_ours(args):
     gang = torch.empty(B, 3, L, device=dev)
     none = torch.empty(0, device=dev)
 
+    # tile shape: autotuned on this shape (outside the timed region) unless given
+    from torchproteinlibrary_gb300 import autotune
+    sweep_rows = None
+    if args.rpt:
+        rm.set_options(args.rpt, 0, 0, 0, args.cta)
+        tuned = {"residues_per_thread": args.rpt, "threads_per_cta": args.cta, "fp64_carry_min_len": 0}
+    else:
+        tuned = autotune.tune(ang, lengths, up, use_cache=False)
+        if not args.no_extras:
+            # FP64 inter-tile carry threshold sweep at the tuned tile shape (-1 = never FP64)
+            sweep_rows = autotune.sweep(ang, lengths, up,
+                                        candidates=[(tuned["residues_per_thread"], tuned["threads_per_cta"])],
+                                        carry_thresholds=(128, 256, 512, -1), steps=5)
+            rm.set_options(tuned["residues_per_thread"], tuned["fp64_carry_min_len"], 0, 0,
+                           tuned["threads_per_cta"])
+    ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)  # sized for the chosen tile
+
     def fwd():
         rm.Angles2BackboneGPU_forward(ang, coords, lengths, ws)
 
@@ -286,11 +303,14 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "global_batch_chains": B * world, "residues_per_chain": L,
                    "l2": "inputs and outputs larger than L2; no flush", "launch": "CUDA graph per pass",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": f"a2b_{'bwd' if dom == 'backward' else 'fwd'}_f32",
+        "roofline": {"bound": "hbm",
+                     "kernel": f"a2b_{'bwd' if dom == 'backward' else 'fwd'}_{'w' if tuned['threads_per_cta'] == 0 else 'f32'}",
                      "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes_per_launch": dom_bytes},
         "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
+        "tuned": tuned,
+        "fp64_carry_sweep": sweep_rows,
         "gpu_launches": 2 * args.steps,
         "e2e": e2e,
         "plain_fp64": plain,
@@ -399,6 +419,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--chains", type=int, default=B_CHAINS,
                     help="chains per GPU (smaller batches are for profiling; the metric uses 4096)")
+    ap.add_argument("--rpt", type=int, default=0,
+                    help="residues per thread; 0 = autotune (the default)")
+    ap.add_argument("--cta", type=int, default=0, help="0 = warp tiles, 128 = CTA tiles (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
     args = ap.parse_args()

@@ -99,13 +99,13 @@ def test_fp64_plain_matches_oracle(rm, B, L, seed):
     check(c, gi, rc, rg, lengths, L, COORD_TOL_F64, GRAD_TOL_F64)
 
 
-@pytest.mark.parametrize("rpt", [1, 2, 4, 8])
-def test_tile_shapes_and_lookback(rm, rpt):
-    """Chains of 1000 residues split into 8 (R=1, 128-residue tiles) down to one
-    (R=8, 1024-residue tiles) look-back tiles; all within tolerance of the oracle."""
+@pytest.mark.parametrize("rpt,cta", [(1, 0), (2, 0), (4, 0), (8, 0), (1, 128), (4, 128), (8, 128)])
+def test_tile_shapes_and_lookback(rm, rpt, cta):
+    """Chains of 1000 residues split into up to 32 warp tiles (R=1: 32-residue tiles)
+    or CTA tiles (128 R residues, one tile at R=8); all within tolerance of the oracle."""
     B, L = 6, 1000
     ang, lengths, g = make_case(B, L, 40 + rpt, lengths=[1000, 999, 129, 128, 127, 1])
-    rm.set_options(rpt, 0, 0, 0)
+    rm.set_options(rpt, 0, 0, 0, cta)
     try:
         c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
     finally:
@@ -186,7 +186,7 @@ def test_lookback_timeout_is_reported(rm, built):
     a = torch.rand(B, 3, L, device=dev)
     ln = torch.full((B,), L, dtype=torch.int32, device=dev)
     out = torch.zeros(B, 9 * L, device=dev)
-    rm.set_options(1, 0, 0, 0)  # 128-residue tiles: 3 tiles per chain
+    rm.set_options(4, 0, 0, 0)  # 128-residue warp tiles: 3 tiles per chain
     try:
         ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
         ws[4 * 8:4 * 9].view(torch.int32).fill_(1)  # WsHeader.test_skip_publish

@@ -114,8 +114,11 @@ int64_t workspace_status(torch::Tensor A) {
     return st;
 }
 
-void set_options(int64_t residues_per_thread, int64_t fp64_carry_min_len, int64_t renormalize, int64_t max_ctas) {
-    tpl_options o = {(int)residues_per_thread, 0, (int)fp64_carry_min_len, (int)renormalize, (int)max_ctas};
+void set_options(int64_t residues_per_thread, int64_t fp64_carry_min_len, int64_t renormalize, int64_t max_ctas,
+                 int64_t threads_per_cta) {
+    tpl_options o = {(int)residues_per_thread, (int)threads_per_cta, (int)fp64_carry_min_len, (int)renormalize,
+                     (int)max_ctas};
+    TORCH_CHECK(o.threads_per_cta == 0 || o.threads_per_cta == 128, "threads_per_cta must be 0 (warp tiles) or 128");
     TORCH_CHECK(o.residues_per_thread == 0 || o.residues_per_thread == 1 || o.residues_per_thread == 2 ||
                     o.residues_per_thread == 4 || o.residues_per_thread == 8,
                 "residues_per_thread must be 0, 1, 2, 4 or 8");
@@ -123,7 +126,8 @@ void set_options(int64_t residues_per_thread, int64_t fp64_carry_min_len, int64_
 }
 
 std::vector<int64_t> get_options() {
-    return {g_opt.residues_per_thread, g_opt.fp64_carry_min_len, g_opt.renormalize, g_opt.max_ctas};
+    return {g_opt.residues_per_thread, g_opt.fp64_carry_min_len, g_opt.renormalize, g_opt.max_ctas,
+            g_opt.threads_per_cta};
 }
 
 }  // namespace
@@ -135,6 +139,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Angles2BackboneCPU_backward", &no_cpu_path_bwd, "not available: no CPU path");
     m.def("workspace_bytes", &workspace_bytes, "bytes of the A workspace for (batch, max_len)");
     m.def("workspace_status", &workspace_status, "synchronise and read the first device-detected error");
-    m.def("set_options", &set_options, "tuning knobs: residues_per_thread, fp64_carry_min_len, renormalize, max_ctas");
+    m.def("set_options", &set_options, "tuning knobs", py::arg("residues_per_thread") = 0,
+          py::arg("fp64_carry_min_len") = 0, py::arg("renormalize") = 0, py::arg("max_ctas") = 0,
+          py::arg("threads_per_cta") = 0);
     m.def("get_options", &get_options, "current tuning knobs");
 }

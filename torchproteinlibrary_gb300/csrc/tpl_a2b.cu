@@ -679,6 +679,460 @@ __global__ void __launch_bounds__(NT, 5) a2b_bwd_f32_kernel(A2bArgs a) {
     finish_launch(&a.hdr->bwd_ticket, &a.hdr->bwd_done, &a.hdr->bwd_epoch);
 }
 
+// ----------------------------------------------- warp-granular tiles (default)
+// Each warp takes its own ticket for a tile of 32 R residues, so no CTA-wide
+// barrier sits on the path: angles are loaded straight into registers, the scan
+// is a warp shuffle scan, and the inter-tile carry is a warp-wide decoupled
+// look-back (every lane polls one predecessor's flag; lane 0 composes the
+// published frames in FP64).  The backward mirrors it with tiles handed out
+// last-first and a look-back over successors' (G, S) sums.
+
+template <int R>
+__device__ __forceinline__ void load_row(const float *row, int j0, int nreal, float (&v)[R]) {
+    if (R % 4 == 0 && j0 + R <= nreal && ((((uintptr_t)(row + j0)) & 15u) == 0)) {
+#pragma unroll
+        for (int i = 0; i < R / 4; i++) {
+            const float4 x = __ldg(reinterpret_cast<const float4 *>(row + j0) + i);
+            v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = (j0 + r < nreal) ? __ldg(row + j0 + r) : 0.f;
+    }
+}
+
+// Walk 1 with the thread-local N, CA, C positions kept in registers.
+template <int R>
+__device__ __forceinline__ Frame<float> walk_regs(const A2bArgs &a, const float4 *s_tab, const float (&phi)[R],
+                                                  const float (&psi)[R], const float (&om)[R], int j0, int nreal,
+                                                  bool chain_end, float (&loc)[R][9]) {
+    Frame<float> agg;
+    frame_identity(agg);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+#pragma unroll
+        for (int c = 0; c < 9; c++) loc[r][c] = 0.f;
+        if (j0 + r < nreal) {
+            float s, c;
+            loc[r][0] = agg.p[0]; loc[r][1] = agg.p[1]; loc[r][2] = agg.p[2];
+            sincos_tab(s_tab, phi[r], &s, &c);
+            apply_joint(agg, a.bc.cb[0], a.bc.sb[0], a.bc.d[0], c, s);
+            loc[r][3] = agg.p[0]; loc[r][4] = agg.p[1]; loc[r][5] = agg.p[2];
+            sincos_tab(s_tab, psi[r], &s, &c);
+            apply_joint(agg, a.bc.cb[1], a.bc.sb[1], a.bc.d[1], c, s);
+            loc[r][6] = agg.p[0]; loc[r][7] = agg.p[1]; loc[r][8] = agg.p[2];
+            if (!(chain_end && j0 + r == nreal - 1)) {
+                sincos_tab(s_tab, om[r], &s, &c);
+                apply_joint(agg, a.bc.cb[2], a.bc.sb[2], a.bc.d[2], c, s);
+            }
+        }
+    }
+    return agg;
+}
+
+__device__ __forceinline__ Frame<float> shfl_frame(const Frame<float> &f, int src) {
+    Frame<float> o;
+#pragma unroll
+    for (int i = 0; i < 9; i++) o.r[i] = __shfl_sync(0xffffffffu, f.r[i], src);
+#pragma unroll
+    for (int i = 0; i < 3; i++) o.p[i] = __shfl_sync(0xffffffffu, f.p[i], src);
+    return o;
+}
+
+// Forward look-back of one warp tile.  All lanes poll predecessor flags (lane i
+// the tile t-1-i); lane 0 folds the published frames (FP64, or rounded to FP32
+// per compose when !use64) and publishes this tile.  `carry` (12 doubles, shared)
+// receives the chain frame at the start of tile t; `scratch` holds 36 doubles.
+__device__ __noinline__ void fwd_lookback_warp(const A2bArgs &a, int b, int t, bool more,
+                                               const Frame<float> &tile_agg, unsigned epoch_bits, bool use64,
+                                               double *carry, double *scratch) {
+    const int lane = threadIdx.x & 31;
+    TileRecord *base = a.rec + (size_t)b * a.ntiles;
+    double *acc = scratch, *agg = scratch + 12, *tmp = scratch + 24;
+    if (lane == 0) {
+        for (int i = 0; i < 9; i++) agg[i] = (double)tile_agg.r[i];
+        for (int i = 0; i < 3; i++) agg[9 + i] = (double)tile_agg.p[i];
+        identity_d(acc);
+        if (t > 0 && more) {
+            copy_d(base[t].fagg, agg);
+            st_release(&base[t].fflag, epoch_bits | kFlagAgg);
+        }
+    }
+    bool ok = true;
+    for (int tt0 = t - 1; tt0 >= 0; tt0 -= 32) {
+        const int tt = tt0 - lane;
+        bool lane_ok = true;
+        unsigned f = 0;
+        if (tt >= 0) f = wait_flag(&base[tt].fflag, epoch_bits, a.hdr, lane_ok);
+        if (__ballot_sync(0xffffffffu, !lane_ok)) {
+            ok = false;
+            break;
+        }
+        const unsigned incm = __ballot_sync(0xffffffffu, tt >= 0 && (f & 3u) == kFlagInc);
+        const int stop = incm ? __ffs(incm) - 1 : min(31, tt0);
+        if (lane == 0) {
+            for (int i = 0; i <= stop; i++) {
+                const TileRecord *q = base + (tt0 - i);
+                (void)ld_acquire(&q->fflag);
+                compose_d(tmp, (incm && i == stop) ? q->finc : q->fagg, acc);
+                copy_d(acc, tmp);
+                if (!use64) round_to_float_d(acc);
+            }
+        }
+        if (incm) break;
+    }
+    if (lane == 0) {
+        if (!ok) identity_d(acc);
+        copy_d(carry, acc);
+        if (t > 0) copy_d(base[t].fexc, acc);
+        // test hook: the first tile of chain 0 stays unpublished when the workspace
+        // asks for it, so that its successor's bounded wait runs out
+        const bool skip = (t == 0 && b == 0 && a.hdr->test_skip_publish);
+        if (more && !skip) {
+            compose_d(tmp, acc, agg);
+            if (!use64) round_to_float_d(tmp);
+            copy_d(base[t].finc, tmp);
+            st_release(&base[t].fflag, epoch_bits | kFlagInc);
+        }
+    }
+    __syncwarp();
+}
+
+// Resident CTAs of 128 threads per SM the register budget is sized for.
+constexpr int warp_tile_min_blocks(int R) { return R <= 2 ? 5 : (R == 4 ? 4 : 3); }
+
+template <int R>
+__global__ void __launch_bounds__(128, warp_tile_min_blocks(R)) a2b_fwd_w_kernel(A2bArgs a) {
+    constexpr int TILE = 32 * R;
+    constexpr int NW = 4;
+    __shared__ float4 s_tab[65];
+    __shared__ double s_carry[NW][12], s_scratch[NW][36];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    load_sincos_table<128>(s_tab);
+    __syncthreads();
+    const unsigned epoch_bits = (*(volatile unsigned *)&a.hdr->fwd_epoch & 0x3fffffffu) << 2;
+
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = (int)atomicAdd(&a.hdr->fwd_ticket, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= a.total) break;
+        const int b = item / a.ntiles, t = item - b * a.ntiles;
+        int len = a.lengths[b];
+        if (len < 0 || len > a.L) {
+            if (lane == 0) record_error(a.hdr, TPL_ERR_LENGTH);
+            len = max(0, min(len, a.L));
+        }
+        const int s0 = t * TILE;
+        const int ntile = min(TILE, a.L - s0);
+        const int nreal = max(0, min(ntile, len - s0));
+        float *out = a.coords + (size_t)b * 9 * a.L + (size_t)9 * s0;
+        for (int i = 9 * nreal + lane; i < 9 * ntile; i += 32) out[i] = 0.f;
+        if (nreal == 0) continue;
+
+        const int j0 = lane * R;
+        const float *ang = a.angles + (size_t)b * 3 * a.L + s0;
+        float phi[R], psi[R], om[R];
+        load_row<R>(ang, j0, nreal, phi);
+        load_row<R>(ang + a.L, j0, nreal, psi);
+        load_row<R>(ang + 2 * a.L, j0, nreal, om);
+        const bool chain_end = (s0 + nreal == len);
+        float loc[R][9];
+        Frame<float> agg = walk_regs<R>(a, s_tab, phi, psi, om, j0, nreal, chain_end, loc);
+        if (a.renorm) renormalize(agg);
+        Frame<float> inc = warp_scan_frames(agg, lane);
+        Frame<float> exc = shfl_up_frame(inc, 1);
+        if (lane == 0) frame_identity(exc);
+        Frame<float> tile = shfl_frame(inc, 31);
+        if (a.renorm) renormalize(tile);
+
+        const bool more = s0 + TILE < len;
+        const bool use64 = a.fp64_min_len >= 0 && len >= a.fp64_min_len;
+        fwd_lookback_warp(a, b, t, more, tile, epoch_bits, use64, s_carry[w], s_scratch[w]);
+        Frame<float> c32;
+        frame_load(c32, s_carry[w]);
+        const float o0 = c32.p[0], o1 = c32.p[1], o2 = c32.p[2];
+        c32.p[0] = c32.p[1] = c32.p[2] = 0.f;  // positions relative to the tile origin
+        if (a.renorm) renormalize(c32);
+        Frame<float> P = compose(c32, exc);
+        if (a.renorm) renormalize(P);
+        const float t0 = P.p[0] + o0, t1 = P.p[1] + o1, t2 = P.p[2] + o2;
+        float *dst = out + (size_t)9 * j0;
+        auto world = [&](int e) {
+            const int r = e / 9, q = (e % 9) / 3, c = e % 3;
+            const float x = loc[r][3 * q], y = loc[r][3 * q + 1], z = loc[r][3 * q + 2];
+            const float tc = c == 0 ? t0 : (c == 1 ? t1 : t2);
+            return fmaf(P.r[3 * c], x, fmaf(P.r[3 * c + 1], y, fmaf(P.r[3 * c + 2], z, tc)));
+        };
+        if ((R % 4 == 0) && (j0 + R <= nreal) && ((((uintptr_t)dst) & 15u) == 0)) {
+            float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+            for (int i = 0; i < 9 * R / 4; i++)
+                __stcs(d4 + i, make_float4(world(4 * i), world(4 * i + 1), world(4 * i + 2), world(4 * i + 3)));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 9 * R; e++)
+                if (j0 + e / 9 < nreal) dst[e] = world(e);
+        }
+    }
+    __syncthreads();
+    finish_launch(&a.hdr->fwd_ticket, &a.hdr->fwd_done, &a.hdr->fwd_epoch);
+}
+
+// Backward look-back of one warp tile over its successors' (G, S) sums (about
+// the world origin, FP64).  `own` (lane 0) is this tile's sums; `carry` (6
+// doubles, shared) receives the sums over all later tiles of the chain.
+__device__ __noinline__ void bwd_lookback_warp(const A2bArgs &a, int b, int t, int t_last, const double *own,
+                                               unsigned epoch_bits, double *carry) {
+    const int lane = threadIdx.x & 31;
+    TileRecord *base = a.rec + (size_t)b * a.ntiles;
+    if (lane == 0) {
+        for (int i = 0; i < 6; i++) carry[i] = 0.0;
+        if (t > 0 && t < t_last) {
+            for (int i = 0; i < 6; i++) base[t].bagg[i] = own[i];
+            st_release(&base[t].bflag, epoch_bits | kFlagAgg);
+        }
+    }
+    bool ok = true;
+    for (int tt0 = t + 1; tt0 <= t_last; tt0 += 32) {
+        const int tt = tt0 + lane;
+        bool lane_ok = true;
+        unsigned f = 0;
+        if (tt <= t_last) f = wait_flag(&base[tt].bflag, epoch_bits, a.hdr, lane_ok);
+        if (__ballot_sync(0xffffffffu, !lane_ok)) {
+            ok = false;
+            break;
+        }
+        const unsigned incm = __ballot_sync(0xffffffffu, tt <= t_last && (f & 3u) == kFlagInc);
+        const int stop = incm ? __ffs(incm) - 1 : min(31, t_last - tt0);
+        if (lane == 0) {
+            for (int i = 0; i <= stop; i++) {
+                const TileRecord *q = base + tt0 + i;
+                (void)ld_acquire(&q->bflag);
+                const double *v = (incm && i == stop) ? q->binc : q->bagg;
+                for (int k = 0; k < 6; k++) carry[k] += v[k];
+            }
+        }
+        if (incm) break;
+    }
+    if (lane == 0) {
+        if (!ok)
+            for (int i = 0; i < 6; i++) carry[i] = 0.0;
+        if (t > 0) {
+            for (int i = 0; i < 6; i++) base[t].binc[i] = own[i] + carry[i];
+            st_release(&base[t].bflag, epoch_bits | kFlagInc);
+        }
+    }
+    __syncwarp();
+}
+
+template <int R>
+__global__ void __launch_bounds__(128, warp_tile_min_blocks(R)) a2b_bwd_w_kernel(A2bArgs a) {
+    constexpr int TILE = 32 * R;
+    constexpr int NW = 4;
+    __shared__ float4 s_tab[65];
+    __shared__ float s_g[NW][9 * R][32];  // this lane's upstream gradients, rotated to its local frame
+    __shared__ double s_own[NW][6], s_carry[NW][6];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    load_sincos_table<128>(s_tab);
+    __syncthreads();
+    const unsigned epoch_bits = (*(volatile unsigned *)&a.hdr->bwd_epoch & 0x3fffffffu) << 2;
+    const float inv_d0 = 1.f / a.bc.d[0], inv_d1 = 1.f / a.bc.d[1], inv_d2 = 1.f / a.bc.d[2];
+
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = (int)atomicAdd(&a.hdr->bwd_ticket, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= a.total) break;
+        const int b = item / a.ntiles, t = a.ntiles - 1 - (item - b * a.ntiles);
+        int len = a.lengths[b];
+        if (len < 0 || len > a.L) {
+            if (lane == 0) record_error(a.hdr, TPL_ERR_LENGTH);
+            len = max(0, min(len, a.L));
+        }
+        const int s0 = t * TILE;
+        const int ntile = min(TILE, a.L - s0);
+        const int nreal = max(0, min(ntile, len - s0));
+        float *gout = a.grad_angles + (size_t)b * 3 * a.L + s0;
+        for (int k = 0; k < 3; k++)
+            for (int i = nreal + lane; i < ntile; i += 32) gout[(size_t)k * a.L + i] = 0.f;
+        if (nreal == 0) continue;
+
+        const int j0 = lane * R;
+        const float *ang = a.angles + (size_t)b * 3 * a.L + s0;
+        float phi[R], psi[R], om[R];
+        load_row<R>(ang, j0, nreal, phi);
+        load_row<R>(ang + a.L, j0, nreal, psi);
+        load_row<R>(ang + 2 * a.L, j0, nreal, om);
+        const bool chain_end = (s0 + nreal == len);
+        float loc[R][9];
+        Frame<float> agg = walk_regs<R>(a, s_tab, phi, psi, om, j0, nreal, chain_end, loc);
+        float nxt[3] = {agg.p[0], agg.p[1], agg.p[2]};  // N after this lane's last residue
+        if (a.renorm) renormalize(agg);
+        Frame<float> inc = warp_scan_frames(agg, lane);
+        Frame<float> exc = shfl_up_frame(inc, 1);
+        if (lane == 0) frame_identity(exc);
+
+        Frame<float> c32;
+        if (t == 0) frame_identity(c32);
+        else frame_load(c32, a.rec[(size_t)b * a.ntiles + t].fexc);
+        const float org[3] = {c32.p[0], c32.p[1], c32.p[2]};
+        c32.p[0] = c32.p[1] = c32.p[2] = 0.f;
+        if (a.renorm) renormalize(c32);
+        Frame<float> P = compose(c32, exc);
+        if (a.renorm) renormalize(P);
+
+        // upstream gradients of this lane's atoms, rotated into its local frame
+        const float *gin = a.grad_coords + (size_t)b * 9 * a.L + (size_t)9 * (s0 + j0);
+        float Gl[3] = {0.f, 0.f, 0.f}, Sl[3] = {0.f, 0.f, 0.f};
+        const bool gvec = (R % 4 == 0) && (j0 + R <= nreal) && ((((uintptr_t)gin) & 15u) == 0);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            float gw[9];
+            if (gvec) {
+                // 9 floats per residue; residues r..r+3 span 9 float4
+#pragma unroll
+                for (int c = 0; c < 9; c++) gw[c] = __ldcs(gin + 9 * r + c);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 9; c++) gw[c] = (j0 + r < nreal) ? __ldcs(gin + 9 * r + c) : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                float gl[3], xg[3];
+                rot_t(P, gw + 3 * q, gl);
+#pragma unroll
+                for (int c = 0; c < 3; c++) s_g[w][9 * r + 3 * q + c][lane] = gl[c];
+                cross3(&loc[r][3 * q], gl, xg);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    Gl[c] += gl[c];
+                    Sl[c] += xg[c];
+                }
+            }
+        }
+        // lane totals in the tile frame, exclusive suffix over lanes, tile total
+        float Gt[3], St[3], pxg[3];
+        rot(P, Gl, Gt);
+        rot(P, Sl, St);
+        cross3(P.p, Gt, pxg);
+#pragma unroll
+        for (int c = 0; c < 3; c++) St[c] += pxg[c];
+        float suf[6], tot[6];
+        const float v6[6] = {Gt[0], Gt[1], Gt[2], St[0], St[1], St[2]};
+#pragma unroll
+        for (int i = 0; i < 6; i++) suf[i] = warp_suffix_exclusive(v6[i], lane, tot[i]);
+        if (lane == 0) {
+            // own sums about the world origin: S + o x G
+            const double o[3] = {org[0], org[1], org[2]};
+            double td[6] = {tot[0], tot[1], tot[2], tot[3], tot[4], tot[5]}, ox[3];
+            cross3(o, td, ox);
+            for (int i = 0; i < 3; i++) {
+                s_own[w][i] = td[i];
+                s_own[w][3 + i] = td[3 + i] + ox[i];
+            }
+        }
+        __syncwarp();
+        const int t_last = (len - 1) / TILE;
+        bwd_lookback_warp(a, b, t, t_last, s_own[w], epoch_bits, s_carry[w]);
+        // carry from later tiles, moved to this tile's origin: S_o = S_w - o x G
+        float cg[3], cs[3];
+        {
+            const double o[3] = {org[0], org[1], org[2]};
+            const double *cw = s_carry[w];
+            double ox[3];
+            cross3(o, cw, ox);
+            for (int i = 0; i < 3; i++) {
+                cg[i] = (float)cw[i];
+                cs[i] = (float)(cw[3 + i] - ox[i]);
+            }
+        }
+        // incoming suffix of this lane, in its local frame: G' = R^T G, S' = R^T (S - p x G)
+        float Gw[3], Sw[3], G[3], S[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            Gw[c] = suf[c] + cg[c];
+            Sw[c] = suf[3 + c] + cs[c];
+        }
+        cross3(P.p, Gw, pxg);
+#pragma unroll
+        for (int c = 0; c < 3; c++) Sw[c] -= pxg[c];
+        rot_t(P, Gw, G);
+        rot_t(P, Sw, S);
+
+        float gr[3][R];
+#pragma unroll
+        for (int r = R - 1; r >= 0; r--) {
+            gr[0][r] = gr[1][r] = gr[2][r] = 0.f;
+            const float *xN = &loc[r][0], *xA = &loc[r][3], *xC = &loc[r][6];
+            if (j0 + r < nreal) {
+                float g[9];
+#pragma unroll
+                for (int c = 0; c < 9; c++) g[c] = s_g[w][9 * r + c][lane];
+                float u[3], tmp[3], cr[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (nxt[c] - xC[c]) * inv_d2;
+                cross3(nxt, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                const float gom = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xC[c] - xA[c]) * inv_d1;
+                cross3(xC, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                const float gps = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                cross3(xC, g + 6, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += g[6 + c];
+                    S[c] += cr[c];
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xA[c] - xN[c]) * inv_d0;
+                cross3(xA, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                const float gph = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                cross3(xA, g + 3, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += g[3 + c];
+                    S[c] += cr[c];
+                }
+                cross3(xN, g, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += g[c];
+                    S[c] += cr[c];
+                }
+                const bool last = chain_end && (j0 + r == nreal - 1);
+                gr[0][r] = gph;
+                gr[1][r] = last ? 0.f : gps;
+                gr[2][r] = last ? 0.f : gom;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) nxt[c] = xN[c];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            float *dst = gout + (size_t)k * a.L + j0;
+            if ((R % 4 == 0) && (j0 + R <= nreal) && ((((uintptr_t)dst) & 15u) == 0)) {
+#pragma unroll
+                for (int i = 0; i < R / 4; i++)
+                    __stcs(reinterpret_cast<float4 *>(dst) + i,
+                           make_float4(gr[k][4 * i], gr[k][4 * i + 1], gr[k][4 * i + 2], gr[k][4 * i + 3]));
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; r++)
+                    if (j0 + r < nreal) dst[r] = gr[k][r];
+            }
+        }
+    }
+    __syncthreads();
+    finish_launch(&a.hdr->bwd_ticket, &a.hdr->bwd_done, &a.hdr->bwd_epoch);
+}
+
 // ----------------------------------------------------------- plain FP64 form
 // One chain per CTA, one residue per thread per chunk, Hillis-Steele block scan
 // of residue transforms in shared memory, carry between chunks in registers.
@@ -904,15 +1358,17 @@ static int persistent_grid(K kernel, int threads, int items, int max_ctas, int d
 
 struct A2bShape {
     int R, NT;
+    bool warp;  // warp-granular tiles (default) or CTA tiles of NT threads
 };
 
-// Forward and backward share the tile (the backward re-reads the forward's
-// per-tile carries): NT = 128 threads of R residues.
+// threads_per_cta = 0: warp-granular tiles of 32 R residues (default).
+// threads_per_cta = 128: CTA tiles of 128 R residues with block-wide scans.
 static A2bShape a2b_shape(const tpl_options &opt, bool backward) {
     (void)backward;
     A2bShape s;
     s.R = opt.residues_per_thread > 0 ? opt.residues_per_thread : 4;
-    s.NT = 128;
+    s.warp = opt.threads_per_cta == 0;
+    s.NT = s.warp ? 32 : 128;
     return s;
 }
 
@@ -938,6 +1394,21 @@ static A2bArgs make_args(const float *angles, const int32_t *lengths, void *ws, 
     a.renorm = opt.renormalize >= 0 ? 1 : 0;
     a.bc = bond_constants();
     return a;
+}
+
+template <int R>
+static int launch_fwd_w(A2bArgs &a, int max_ctas, cudaStream_t st) {
+    auto k = a2b_fwd_w_kernel<R>;
+    int grid = persistent_grid(k, 128, (a.total + 3) / 4, max_ctas);
+    k<<<grid, 128, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+template <int R>
+static int launch_bwd_w(A2bArgs &a, int max_ctas, cudaStream_t st) {
+    auto k = a2b_bwd_w_kernel<R>;
+    int grid = persistent_grid(k, 128, (a.total + 3) / 4, max_ctas);
+    k<<<grid, 128, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
 template <int R>
@@ -967,6 +1438,15 @@ int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, 
     A2bShape s = a2b_shape(opt, false);
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.coords = coords;
+    if (s.warp) {
+        switch (s.R) {
+            case 1: return launch_fwd_w<1>(a, opt.max_ctas, st);
+            case 2: return launch_fwd_w<2>(a, opt.max_ctas, st);
+            case 4: return launch_fwd_w<4>(a, opt.max_ctas, st);
+            case 8: return launch_fwd_w<8>(a, opt.max_ctas, st);
+        }
+        return TPL_ERR_UNSUPPORTED;
+    }
     switch (s.R) {
         case 1: return launch_fwd<1>(a, opt.max_ctas, st);
         case 2: return launch_fwd<2>(a, opt.max_ctas, st);
@@ -983,6 +1463,15 @@ int a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.grad_angles = grad_angles;
     a.grad_coords = grad_coords;
+    if (s.warp) {
+        switch (s.R) {
+            case 1: return launch_bwd_w<1>(a, opt.max_ctas, st);
+            case 2: return launch_bwd_w<2>(a, opt.max_ctas, st);
+            case 4: return launch_bwd_w<4>(a, opt.max_ctas, st);
+            case 8: return launch_bwd_w<8>(a, opt.max_ctas, st);
+        }
+        return TPL_ERR_UNSUPPORTED;
+    }
     switch (s.R) {
         case 1: return launch_bwd<1, 128>(a, opt.max_ctas, st);
         case 2: return launch_bwd<2, 128>(a, opt.max_ctas, st);

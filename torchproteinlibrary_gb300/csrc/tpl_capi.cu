@@ -88,14 +88,14 @@ static tpl_options resolve(const tpl_options *opt) {
 static bool options_ok(const tpl_options &o) {
     const int r = o.residues_per_thread;
     if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8)) return false;
-    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128)) return false;
+    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128)) return false;  // 0: warp tiles, 128: CTA tiles
     if (o.max_ctas < 0) return false;
     return true;
 }
 
 static size_t a2b_ws(int B, int L, const tpl_options &o) {
     const int tile = a2b_tile_for(o);
-    const int plain_chunk = 256;
+    const int plain_chunk = 256;  // the plain FP64 backward keeps one record per 256-residue chunk
     const int smallest = tile < plain_chunk ? tile : plain_chunk;
     return ws_bytes_for(B, (L + smallest - 1) / smallest);
 }
