@@ -277,7 +277,7 @@ def run_ours(args):
     value = residues / (ms / 1e3)
 
     if args.no_extras:
-        check = plain = e2e = None
+        check = plain = e2e = a2c = None
     else:
         # correctness of this very run against the FP64 plain form on a slice
         check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
@@ -285,6 +285,7 @@ def run_ours(args):
         plain = time_plain_fp64(rm, ang, lengths, up, dev, steps=max(1, min(3, args.steps)))
         # e2e: public autograd layer, host (pinned) inputs in, results back to the host
         e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(1, min(5, args.steps)))
+        a2c = time_a2c(dev)
 
     peak, peak_kind = peaks()
     fwd_ms, bwd_ms = statistics.mean(t_f), statistics.mean(t_b)
@@ -310,10 +311,13 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": dom_bytes},
         "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
         "tuned": tuned,
+        "tile_sweep": [{k: (round(v, 5) if isinstance(v, float) else v) for k, v in r.items()}
+                       for r in getattr(autotune.tune, "last_sweep", [])],
         "fp64_carry_sweep": sweep_rows,
         "gpu_launches": 2 * args.steps,
         "e2e": e2e,
         "plain_fp64": plain,
+        "angles2coords": a2c,
         "accuracy_vs_fp64": check,
     }
     if rank == 0:
@@ -397,6 +401,62 @@ def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
     return {"value": ang_np.shape[0] * L_RES / (ms / 1e3), "unit": "residues/s", "ms_per_step": ms,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "api": "torchproteinlibrary_gb300.ReducedModel.Angles2Backbone (autograd), pinned host buffers"}
+
+
+def time_a2c(dev, steps=10, seed=1004):
+    """Angles2Coords forward+backward on the training-step shapes: 256 chains of
+    U{50..500} random residues, float32 batched kernels vs float64 kernels, with
+    the FP32 error against FP64 on the same float32 angles."""
+    import torch
+    from torchproteinlibrary_gb300 import load_extension
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+
+    fm = load_extension("_FullAtomModel")
+    g = np.random.default_rng(seed)
+    B = 256
+    lens = g.integers(50, 501, B)
+    aa = np.array(list("ACDEFGHIKLMNPQRSTVWY"))
+    seqs = ["".join(g.choice(aa, n)) for n in lens]
+    L = int(lens.max())
+    ang = torch.from_numpy(g.uniform(-np.pi, np.pi, (B, 8, L)).astype(np.float32)).to(dev)
+    seq = convertStringList(seqs).to(dev)
+    na = [fm.getSeqNumAtoms(x) for x in seqs]
+    maxA = max(na)
+    res = {}
+    outs = {}
+    for name, dt in (("f32", torch.float32), ("f64", torch.float64)):
+        a = ang.to(dt)
+        c = torch.empty(B, 3 * maxA, dtype=dt, device=dev)
+        rn = torch.empty(B, maxA, 4, dtype=torch.uint8, device=dev)
+        an = torch.empty(B, maxA, 4, dtype=torch.uint8, device=dev)
+        gup = torch.from_numpy(g.standard_normal((B, 3 * maxA))).to(dev, dt) if name == "f32" else \
+            outs["f32"][2].to(dt)
+        ga = torch.empty_like(a)
+        for _ in range(2):
+            fm.Angles2Coords_forward(seq, a, c, rn, an)
+            fm.Angles2Coords_backward(gup, ga, seq, a)
+        torch.cuda.synchronize(dev)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        n = steps if name == "f32" else max(1, steps // 4)
+        e[0].record()
+        for _ in range(n):
+            fm.Angles2Coords_forward(seq, a, c, rn, an)
+        e[1].record()
+        for _ in range(n):
+            fm.Angles2Coords_backward(gup, ga, seq, a)
+        e[2].record()
+        torch.cuda.synchronize(dev)
+        fms, bms = e[0].elapsed_time(e[1]) / n, e[1].elapsed_time(e[2]) / n
+        res[name] = {"residues_per_s": float(lens.sum()) / ((fms + bms) / 1e3), "fwd_ms": fms, "bwd_ms": bms}
+        outs[name] = (c.double(), ga.double(), gup)
+    d = (outs["f32"][0] - outs["f64"][0]).view(B, -1, 3).norm(dim=-1)
+    ge = (outs["f32"][1] - outs["f64"][1]).abs().max() / outs["f64"][1].abs().max()
+    res["batched_vs_fp64"] = res["f32"]["residues_per_s"] / res["f64"]["residues_per_s"]
+    res["coord_max_A"] = float(d.max())
+    res["grad_max_rel"] = float(ge)
+    res["workload"] = "Angles2Coords fwd+bwd, 256 chains x U{50..500} random residues"
+    res["bytes_per_residue_f32"] = 298
+    return res
 
 
 def cpu_baseline_entry():

@@ -151,6 +151,31 @@ int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const u
                          const double *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
                          int max_atoms, const tpl_options *opt, void *stream);
 
+/* Coords2RMSD forward: least RMSD between src and dst after optimal superposition
+ * (quaternion method), per chain.  Replaces Coords2RMSDGPU_forward
+ * (Layers/RMSD/Coords2RMSD/coords2rmsd_interface.cpp:52-111); center = 1 also folds
+ * in the centring that Coords2RMSD.forward does with Coords2Center/CoordsTranslate
+ * (TorchProteinLibrary/RMSD/Coords2RMSD/Coords2RMSD.py:71-78).
+ *   src, dst   [batch, 3 * atoms_stride]   num_atoms int32 [batch]
+ *   rmsd [batch], ut [batch, 3, 3] (the transposed rotation, as the reference's UT),
+ *   centroids [batch, 6] doubles (src then dst centroid; may be NULL when center = 0) */
+int tpl_rmsd_forward_f32(const float *src, const float *dst, const int32_t *num_atoms, int batch, int atoms_stride,
+                         int center, float *rmsd, float *ut, double *centroids, void *workspace,
+                         size_t workspace_bytes, void *stream);
+int tpl_rmsd_forward_f64(const double *src, const double *dst, const int32_t *num_atoms, int batch, int atoms_stride,
+                         int center, double *rmsd, double *ut, double *centroids, void *workspace,
+                         size_t workspace_bytes, void *stream);
+
+/* Coords2RMSD backward: dL/dsrc = dL/drmsd (x_i - UT y_i) / (rmsd N) on the centred
+ * coordinates, zero past num_atoms.  Replaces Coords2RMSDFunction.backward
+ * (TorchProteinLibrary/RMSD/Coords2RMSD/Coords2RMSD.py:40-62, a per-chain Python loop). */
+int tpl_rmsd_backward_f32(const float *grad_rmsd, const float *src, const float *dst, const int32_t *num_atoms,
+                          const float *rmsd, const float *ut, const double *centroids, int batch, int atoms_stride,
+                          int center, float *grad_src, void *stream);
+int tpl_rmsd_backward_f64(const double *grad_rmsd, const double *src, const double *dst, const int32_t *num_atoms,
+                          const double *rmsd, const double *ut, const double *centroids, int batch, int atoms_stride,
+                          int center, double *grad_src, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,3 +170,46 @@ def a2c_backward(grad_coords: np.ndarray, angles: np.ndarray, seqs: list[str], i
     if rc != 0:
         raise RuntimeError(f"a2c_backward failed ({rc})")
     return out
+
+
+# ------------------------------------------------------------------ Coords2RMSD
+def rmsd(src: np.ndarray, dst: np.ndarray, num_atoms, center: bool = True):
+    """Least RMSD per chain after optimal superposition, restating the reference's
+    CPU path (Layers/RMSD/Coords2RMSD/coords2rmsd_interface.cpp:113-183: FP64
+    correlation R, 4x4 quaternion matrix, largest eigenpair, rmsd =
+    sqrt((R2 - 2|lambda| + 1e-10)/N), UT = U^T) with the centring of
+    TorchProteinLibrary/RMSD/Coords2RMSD/Coords2RMSD.py:71-78.  The reference solves
+    the eigen problem with torch's eig; this uses numpy.linalg.eigh (symmetric).
+    Returns (rmsd [B], UT [B,3,3], grad_factor) where dL/dsrc = g * grad_factor[b]."""
+    src = np.asarray(src, dtype=np.float64)
+    dst = np.asarray(dst, dtype=np.float64)
+    B = src.shape[0]
+    out = np.zeros(B)
+    UT = np.zeros((B, 3, 3))
+    grads = np.zeros_like(src)
+    for b in range(B):
+        n = int(num_atoms[b])
+        x = src[b, :3 * n].reshape(n, 3)
+        y = dst[b, :3 * n].reshape(n, 3)
+        if center and n:
+            x = x - x.mean(0)
+            y = y - y.mean(0)
+        R = x.T @ y
+        F = np.array([
+            [R[0, 0] + R[1, 1] + R[2, 2], R[1, 2] - R[2, 1], R[2, 0] - R[0, 2], R[0, 1] - R[1, 0]],
+            [R[1, 2] - R[2, 1], R[0, 0] - R[1, 1] - R[2, 2], R[0, 1] + R[1, 0], R[0, 2] + R[2, 0]],
+            [R[2, 0] - R[0, 2], R[0, 1] + R[1, 0], -R[0, 0] + R[1, 1] - R[2, 2], R[1, 2] + R[2, 1]],
+            [R[0, 1] - R[1, 0], R[0, 2] + R[2, 0], R[1, 2] + R[2, 1], -R[0, 0] - R[1, 1] + R[2, 2]]])
+        w, v = np.linalg.eigh(F)
+        lam, q = w[-1], v[:, -1]
+        U = np.array([
+            [q[0] ** 2 + q[1] ** 2 - q[2] ** 2 - q[3] ** 2, 2 * (q[1] * q[2] - q[0] * q[3]), 2 * (q[1] * q[3] + q[0] * q[2])],
+            [2 * (q[1] * q[2] + q[0] * q[3]), q[0] ** 2 - q[1] ** 2 + q[2] ** 2 - q[3] ** 2, 2 * (q[2] * q[3] - q[0] * q[1])],
+            [2 * (q[1] * q[3] - q[0] * q[2]), 2 * (q[2] * q[3] + q[0] * q[1]), q[0] ** 2 - q[1] ** 2 - q[2] ** 2 + q[3] ** 2]])
+        UT[b] = U.T
+        R2 = (x ** 2).sum() + (y ** 2).sum()
+        out[b] = np.sqrt(max((R2 - 2 * abs(lam) + 1e-10) / max(n, 1), 0.0)) if n else 0.0
+        if n and out[b] > 0:
+            # Coords2RMSD.py:48-56: (x - UT y) / (rmsd N), UT applied as out = UT @ y
+            grads[b, :3 * n] = ((x - y @ UT[b].T) / (out[b] * n)).reshape(-1)
+    return out, UT, grads

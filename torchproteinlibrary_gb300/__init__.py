@@ -41,10 +41,10 @@ def load_extension(name: str):
 def install_alias() -> None:
     """Make ``import TorchProteinLibrary`` (and its ReducedModel / FullAtomModel
     sub-packages) resolve to this package."""
-    from . import FullAtomModel, ReducedModel  # noqa: F401
+    from . import RMSD, FullAtomModel, ReducedModel  # noqa: F401
 
     sys.modules.setdefault("TorchProteinLibrary", sys.modules[__name__])
-    sys.modules.setdefault("TorchProteinLibrary.ReducedModel", sys.modules[f"{__name__}.ReducedModel"])
-    sys.modules.setdefault("TorchProteinLibrary.FullAtomModel", sys.modules[f"{__name__}.FullAtomModel"])
-    sys.modules.setdefault("_ReducedModel", load_extension("_ReducedModel"))
-    sys.modules.setdefault("_FullAtomModel", load_extension("_FullAtomModel"))
+    for sub in ("ReducedModel", "FullAtomModel", "RMSD"):
+        sys.modules.setdefault(f"TorchProteinLibrary.{sub}", sys.modules[f"{__name__}.{sub}"])
+    for ext in ("_ReducedModel", "_FullAtomModel", "_RMSD"):
+        sys.modules.setdefault(ext, load_extension(ext))

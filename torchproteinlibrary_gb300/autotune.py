@@ -115,6 +115,7 @@ def tune(ang, lengths, up, use_cache=True, steps=5):
     rm = load_extension("_ReducedModel")
     key = f"{torch.cuda.get_device_name(ang.device)}|{_bucket(ang.shape[0], ang.shape[2])}"
     cache = _load_cache() if use_cache else {}
+    rows = []
     if key in cache:
         best = cache[key]
     else:
@@ -125,4 +126,5 @@ def tune(ang, lengths, up, use_cache=True, steps=5):
         if use_cache:
             _save_cache(cache)
     rm.set_options(best["residues_per_thread"], best["fp64_carry_min_len"], 0, 0, best["threads_per_cta"])
+    tune.last_sweep = rows
     return best

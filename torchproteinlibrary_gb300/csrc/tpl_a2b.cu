@@ -223,56 +223,160 @@ __device__ __forceinline__ void copy_d(double *d, const double *s) {
     for (int i = 0; i < 12; i++) d[i] = s[i];
 }
 
-// Forward inter-tile carry by decoupled look-back (thread 0 only).  Publishes this
-// tile's aggregate (and inclusive prefix when a later tile exists), waits on the
-// predecessors, and returns in `carry` the chain frame at the start of tile t.
-// `scratch` holds 3 x 12 doubles of shared memory.
-__device__ __noinline__ void forward_carry(const A2bArgs &a, int b, int t, bool more, const Frame<float> &tile_agg,
-                                           unsigned epoch_bits, bool use64, double *carry, double *scratch) {
-    TileRecord *rc = a.rec + (size_t)b * a.ntiles + t;
-    double *acc = scratch, *agg = scratch + 12, *tmp = scratch + 24;
-#pragma unroll 1
-    for (int i = 0; i < 9; i++) agg[i] = (double)tile_agg.r[i];
-#pragma unroll 1
-    for (int i = 0; i < 3; i++) agg[9 + i] = (double)tile_agg.p[i];
-    identity_d(carry);
-    if (t == 0) {
-        // test hook: leave the first tile of chain 0 unpublished so that its
-        // successor's bounded wait runs out (tpl_workspace_status reports it)
-        if (more && !(b == 0 && a.hdr->test_skip_publish)) {
-            copy_d(rc->finc, agg);
-            st_release(&rc->fflag, epoch_bits | kFlagInc);
-        }
-        return;
+// Element e of the composition A o B of two 12-double frames (e < 9: rotation
+// entry (e / 3, e % 3); e >= 9: translation entry e - 9).
+__device__ __forceinline__ double compose_elem(const double *A, const double *B, int e) {
+    if (e < 9) {
+        const int i = e / 3, j = e % 3;
+        return fma(A[3 * i], B[j], fma(A[3 * i + 1], B[3 + j], A[3 * i + 2] * B[6 + j]));
     }
-    if (more) {
-        copy_d(rc->fagg, agg);
-        st_release(&rc->fflag, epoch_bits | kFlagAgg);
+    const int i = e - 9;
+    return fma(A[3 * i], B[9], fma(A[3 * i + 1], B[10], fma(A[3 * i + 2], B[11], A[9 + i])));
+}
+
+__device__ __forceinline__ float frame_elem(const Frame<float> &f, int e) {
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < 12; k++) v = (e == k) ? (k < 9 ? f.r[k] : f.p[k - 9]) : v;
+    return v;
+}
+
+// Forward inter-tile carry by decoupled look-back, executed by one full warp.
+// FP64 is slow on GB300 and a one-lane FP64 instruction costs a full pipe slot,
+// so every FP64 frame product is spread over 12 lanes (one entry each, 3 FMA).
+// Lane i polls the flag of predecessor tile t-1-i; the published frames are then
+// folded from the nearest inclusive prefix.  `carry` (12 doubles, shared) receives
+// the chain frame at the start of tile t; `scr` holds 36 doubles of shared memory.
+__device__ __noinline__ void fwd_carry_warp(const A2bArgs &a, int b, int t, bool more, const Frame<float> &tile_agg,
+                                            unsigned epoch_bits, bool use64, double *carry, double *scr) {
+    const int lane = threadIdx.x & 31;
+    const bool el = lane < 12;
+    TileRecord *base = a.rec + (size_t)b * a.ntiles;
+    double *acc = scr, *agg = scr + 24;
+    if (el) {
+        agg[lane] = (double)frame_elem(tile_agg, lane);
+        acc[lane] = (lane < 9 && lane % 4 == 0) ? 1.0 : 0.0;
     }
-    identity_d(acc);
+    __syncwarp();
+    if (t > 0 && more) {
+        if (el) base[t].fagg[lane] = agg[lane];
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(&base[t].fflag, epoch_bits | kFlagAgg);
+    }
     bool ok = true;
-    for (int tt = t - 1; tt >= 0; tt--) {
-        const TileRecord *q = a.rec + (size_t)b * a.ntiles + tt;
-        unsigned f = wait_flag(&q->fflag, epoch_bits, a.hdr, ok);
-        if (!ok) break;
-        if ((f & 3u) == kFlagInc) {
-            compose_d(carry, q->finc, acc);
-            if (!use64) round_to_float_d(carry);
+    for (int tt0 = t - 1; tt0 >= 0; tt0 -= 32) {
+        const int tt = tt0 - lane;
+        bool lane_ok = true;
+        unsigned f = 0;
+        if (tt >= 0) f = wait_flag(&base[tt].fflag, epoch_bits, a.hdr, lane_ok);
+        if (__ballot_sync(0xffffffffu, !lane_ok)) {
+            ok = false;
             break;
         }
-        compose_d(tmp, q->fagg, acc);
-        copy_d(acc, tmp);
-        if (!use64) round_to_float_d(acc);
+        const unsigned incm = __ballot_sync(0xffffffffu, tt >= 0 && (f & 3u) == kFlagInc);
+        const int stop = incm ? __ffs(incm) - 1 : min(31, tt0);
+        for (int i = 0; i <= stop; i++) {
+            const TileRecord *q = base + (tt0 - i);
+            double v = 0.0;
+            if (el) {
+                (void)ld_acquire(&q->fflag);
+                v = compose_elem((incm && i == stop) ? q->finc : q->fagg, acc, lane);
+            }
+            __syncwarp();
+            if (el) acc[lane] = use64 ? v : (double)(float)v;
+            __syncwarp();
+        }
+        if (incm) break;
     }
-    if (!ok) identity_d(carry);
-    if (a.renorm) renormalize_d(carry);
-    copy_d(rc->fexc, carry);
-    if (more) {
-        compose_d(tmp, carry, agg);
-        if (!use64) round_to_float_d(tmp);
-        if (a.renorm) renormalize_d(tmp);
-        copy_d(rc->finc, tmp);
-        st_release(&rc->fflag, epoch_bits | kFlagInc);
+    if (!ok && el) acc[lane] = (lane < 9 && lane % 4 == 0) ? 1.0 : 0.0;
+    __syncwarp();
+    if (el) {
+        carry[lane] = acc[lane];
+        if (t > 0) base[t].fexc[lane] = acc[lane];
+    }
+    // test hook: the first tile of chain 0 stays unpublished when the workspace asks
+    // for it, so that its successor's bounded wait runs out
+    const bool skip = (t == 0 && b == 0 && a.hdr->test_skip_publish);
+    if (more && !skip) {
+        if (el) {
+            const double v = compose_elem(acc, agg, lane);
+            base[t].finc[lane] = use64 ? v : (double)(float)v;
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(&base[t].fflag, epoch_bits | kFlagInc);
+    }
+    __syncwarp();
+}
+
+// Backward suffix look-back over the later tiles of a chain, executed by one full
+// warp; lanes 0..5 own one component of (G, S) each (S about the world origin,
+// FP64).  own: this tile's sums (shared); carry: the sums over all later tiles.
+__device__ __noinline__ void bwd_carry_warp(const A2bArgs &a, int b, int t, int t_last, const double *own,
+                                            unsigned epoch_bits, double *carry) {
+    const int lane = threadIdx.x & 31;
+    const bool el = lane < 6;
+    TileRecord *base = a.rec + (size_t)b * a.ntiles;
+    double c = 0.0;
+    if (t > 0 && t < t_last) {
+        if (el) base[t].bagg[lane] = own[lane];
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(&base[t].bflag, epoch_bits | kFlagAgg);
+    }
+    bool ok = true;
+    for (int tt0 = t + 1; tt0 <= t_last; tt0 += 32) {
+        const int tt = tt0 + lane;
+        bool lane_ok = true;
+        unsigned f = 0;
+        if (tt <= t_last) f = wait_flag(&base[tt].bflag, epoch_bits, a.hdr, lane_ok);
+        if (__ballot_sync(0xffffffffu, !lane_ok)) {
+            ok = false;
+            break;
+        }
+        const unsigned incm = __ballot_sync(0xffffffffu, tt <= t_last && (f & 3u) == kFlagInc);
+        const int stop = incm ? __ffs(incm) - 1 : min(31, t_last - tt0);
+        if (el)
+            for (int i = 0; i <= stop; i++) {
+                const TileRecord *q = base + tt0 + i;
+                (void)ld_acquire(&q->bflag);
+                c += (incm && i == stop) ? q->binc[lane] : q->bagg[lane];
+            }
+        if (incm) break;
+    }
+    if (!ok) c = 0.0;
+    if (el) carry[lane] = c;
+    if (t > 0) {
+        if (el) base[t].binc[lane] = own[lane] + c;
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(&base[t].bflag, epoch_bits | kFlagInc);
+    }
+    __syncwarp();
+}
+
+// Lanes 0..5 of a warp: own[k] = tile sums (G, S) moved from the tile origin o to
+// the world origin (S + o x G), from the FP32 totals present in every lane.
+__device__ __forceinline__ void own_sums_world(const float *tot, const float *o, double *own) {
+    const int k = threadIdx.x & 31;
+    if (k < 3) {
+        own[k] = (double)tot[k];
+    } else if (k < 6) {
+        const int i = k - 3, i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+        own[k] = (double)tot[3 + i] + fma((double)o[i1], (double)tot[i2], -(double)o[i2] * (double)tot[i1]);
+    }
+    __syncwarp();
+}
+
+// Every lane: the carry from later tiles moved to the tile origin o,
+// S_o = S_world - o x G, in FP32.
+__device__ __forceinline__ void carry_to_origin(const double *cw, const float *o, float *g, float *sv) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+        g[i] = (float)cw[i];
+        sv[i] = (float)(cw[3 + i] - ((double)o[i1] * cw[i2] - (double)o[i2] * cw[i1]));
     }
 }
 
@@ -344,18 +448,17 @@ __global__ void __launch_bounds__(NT, 5) a2b_fwd_f32_kernel(A2bArgs a) {
         if (w == 0) {
             Frame<float> tile;
             Frame<float> wexc = warp_totals_scan<NW>(s_wtot, a.renorm, tile);
+            const bool more = s0 + TILE < len;
+            const bool use64 = a.fp64_min_len >= 0 && len >= a.fp64_min_len;
+            fwd_carry_warp(a, b, t, more, tile, s_epoch, use64, s_fcarry, s_fscratch);
+            Frame<float> c32;
+            frame_load(c32, s_fcarry);
             if (tid == 0) {
-                const bool more = s0 + TILE < len;
-                const bool use64 = a.fp64_min_len >= 0 && len >= a.fp64_min_len;
-                forward_carry(a, b, t, more, tile, s_epoch, use64, s_fcarry, s_fscratch);
-                Frame<float> c32;
-                frame_load(c32, s_fcarry);
                 s_org[0] = c32.p[0]; s_org[1] = c32.p[1]; s_org[2] = c32.p[2];
-                c32.p[0] = c32.p[1] = c32.p[2] = 0.f;  // positions relative to the tile origin
-                s_carry = c32;
             }
-            __syncwarp();
-            if (tid < NW) s_wpre[tid] = compose(s_carry, wexc);
+            c32.p[0] = c32.p[1] = c32.p[2] = 0.f;  // positions relative to the tile origin
+            if (a.renorm) renormalize(c32);
+            if (tid < NW) s_wpre[tid] = compose(c32, wexc);
         }
         __syncthreads();
 
@@ -388,43 +491,6 @@ __global__ void __launch_bounds__(NT, 5) a2b_fwd_f32_kernel(A2bArgs a) {
 }
 
 // ------------------------------------------------------------------ backward
-// Suffix look-back over later tiles of the chain (thread 0 only).  own = this
-// tile's (G, S) with S about the world origin.  Returns the sums over all later
-// tiles.
-__device__ __noinline__ void backward_suffix(const A2bArgs &a, int b, int t, int t_last, const double own[6],
-                                unsigned epoch_bits, double carry[6]) {
-    TileRecord *rc = a.rec + (size_t)b * a.ntiles + t;
-    for (int i = 0; i < 6; i++) carry[i] = 0.0;
-    if (t == t_last) {
-        if (t > 0) {
-            for (int i = 0; i < 6; i++) rc->binc[i] = own[i];
-            st_release(&rc->bflag, epoch_bits | kFlagInc);
-        }
-        return;
-    }
-    if (t > 0) {
-        for (int i = 0; i < 6; i++) rc->bagg[i] = own[i];
-        st_release(&rc->bflag, epoch_bits | kFlagAgg);
-    }
-    bool ok = true;
-    for (int tt = t + 1; tt <= t_last; tt++) {
-        const TileRecord *q = a.rec + (size_t)b * a.ntiles + tt;
-        unsigned f = wait_flag(&q->bflag, epoch_bits, a.hdr, ok);
-        if (!ok) break;
-        if ((f & 3u) == kFlagInc) {
-            for (int i = 0; i < 6; i++) carry[i] += q->binc[i];
-            break;
-        }
-        for (int i = 0; i < 6; i++) carry[i] += q->bagg[i];
-    }
-    if (!ok)
-        for (int i = 0; i < 6; i++) carry[i] = 0.0;
-    if (t > 0) {
-        for (int i = 0; i < 6; i++) rc->binc[i] = own[i] + carry[i];
-        st_release(&rc->bflag, epoch_bits | kFlagInc);
-    }
-}
-
 __device__ __forceinline__ float warp_suffix_exclusive(float v, int lane, float &total) {
     // inclusive suffix sum: sum over lanes >= lane
     float inc = v;
@@ -467,6 +533,7 @@ __global__ void __launch_bounds__(NT, 5) a2b_bwd_f32_kernel(A2bArgs a) {
     __shared__ Frame<float> s_wpre[NW];
     __shared__ float s_wsum[NW][6];
     __shared__ float s_wsuf[NW][6];
+    __shared__ double s_bown[6], s_bcarry[6];
     __shared__ float s_org[3];
     __shared__ int s_item;
     __shared__ unsigned s_epoch;
@@ -566,32 +633,28 @@ __global__ void __launch_bounds__(NT, 5) a2b_bwd_f32_kernel(A2bArgs a) {
 #pragma unroll
             for (int i = 0; i < 6; i++) s_wsum[w][i] = wt[i];
         __syncthreads();
-        if (tid == 0) {
-            const double org64[3] = {(double)s_org[0], (double)s_org[1], (double)s_org[2]};
-            double tot[6] = {0, 0, 0, 0, 0, 0};
-            for (int ww = 0; ww < NW; ww++)
-                for (int i = 0; i < 6; i++) tot[i] += (double)s_wsum[ww][i];
-            double own[6], oxg[3];
-            cross3(org64, tot, oxg);
-            for (int i = 0; i < 3; i++) {
-                own[i] = tot[i];
-                own[3 + i] = tot[3 + i] + oxg[i];
+        if (w == 0) {
+            float tot6[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) {
+                float v = 0.f;
+                for (int ww = 0; ww < NW; ww++) v += s_wsum[ww][i];
+                tot6[i] = v;
             }
+            const float o3[3] = {s_org[0], s_org[1], s_org[2]};
+            own_sums_world(tot6, o3, s_bown);
             const int t_last = (len - 1) / TILE;
-            double cw[6];
-            backward_suffix(a, b, t, t_last, own, s_epoch, cw);
-            double oxc[3];
-            cross3(org64, cw, oxc);
-            float run[6];
-            for (int i = 0; i < 3; i++) {
-                run[i] = (float)cw[i];
-                run[3 + i] = (float)(cw[3 + i] - oxc[i]);
+            bwd_carry_warp(a, b, t, t_last, s_bown, s_epoch, s_bcarry);
+            float cg[3], cs[3];
+            carry_to_origin(s_bcarry, o3, cg, cs);
+            if (tid == 0) {
+                float run[6] = {cg[0], cg[1], cg[2], cs[0], cs[1], cs[2]};
+                for (int ww = NW - 1; ww >= 0; ww--)
+                    for (int i = 0; i < 6; i++) {
+                        s_wsuf[ww][i] = run[i];
+                        run[i] += s_wsum[ww][i];
+                    }
             }
-            for (int ww = NW - 1; ww >= 0; ww--)
-                for (int i = 0; i < 6; i++) {
-                    s_wsuf[ww][i] = run[i];
-                    run[i] += s_wsum[ww][i];
-                }
         }
         __syncthreads();
         // incoming suffix (atoms after this thread) in the thread's local frame:
@@ -739,65 +802,6 @@ __device__ __forceinline__ Frame<float> shfl_frame(const Frame<float> &f, int sr
     return o;
 }
 
-// Forward look-back of one warp tile.  All lanes poll predecessor flags (lane i
-// the tile t-1-i); lane 0 folds the published frames (FP64, or rounded to FP32
-// per compose when !use64) and publishes this tile.  `carry` (12 doubles, shared)
-// receives the chain frame at the start of tile t; `scratch` holds 36 doubles.
-__device__ __noinline__ void fwd_lookback_warp(const A2bArgs &a, int b, int t, bool more,
-                                               const Frame<float> &tile_agg, unsigned epoch_bits, bool use64,
-                                               double *carry, double *scratch) {
-    const int lane = threadIdx.x & 31;
-    TileRecord *base = a.rec + (size_t)b * a.ntiles;
-    double *acc = scratch, *agg = scratch + 12, *tmp = scratch + 24;
-    if (lane == 0) {
-        for (int i = 0; i < 9; i++) agg[i] = (double)tile_agg.r[i];
-        for (int i = 0; i < 3; i++) agg[9 + i] = (double)tile_agg.p[i];
-        identity_d(acc);
-        if (t > 0 && more) {
-            copy_d(base[t].fagg, agg);
-            st_release(&base[t].fflag, epoch_bits | kFlagAgg);
-        }
-    }
-    bool ok = true;
-    for (int tt0 = t - 1; tt0 >= 0; tt0 -= 32) {
-        const int tt = tt0 - lane;
-        bool lane_ok = true;
-        unsigned f = 0;
-        if (tt >= 0) f = wait_flag(&base[tt].fflag, epoch_bits, a.hdr, lane_ok);
-        if (__ballot_sync(0xffffffffu, !lane_ok)) {
-            ok = false;
-            break;
-        }
-        const unsigned incm = __ballot_sync(0xffffffffu, tt >= 0 && (f & 3u) == kFlagInc);
-        const int stop = incm ? __ffs(incm) - 1 : min(31, tt0);
-        if (lane == 0) {
-            for (int i = 0; i <= stop; i++) {
-                const TileRecord *q = base + (tt0 - i);
-                (void)ld_acquire(&q->fflag);
-                compose_d(tmp, (incm && i == stop) ? q->finc : q->fagg, acc);
-                copy_d(acc, tmp);
-                if (!use64) round_to_float_d(acc);
-            }
-        }
-        if (incm) break;
-    }
-    if (lane == 0) {
-        if (!ok) identity_d(acc);
-        copy_d(carry, acc);
-        if (t > 0) copy_d(base[t].fexc, acc);
-        // test hook: the first tile of chain 0 stays unpublished when the workspace
-        // asks for it, so that its successor's bounded wait runs out
-        const bool skip = (t == 0 && b == 0 && a.hdr->test_skip_publish);
-        if (more && !skip) {
-            compose_d(tmp, acc, agg);
-            if (!use64) round_to_float_d(tmp);
-            copy_d(base[t].finc, tmp);
-            st_release(&base[t].fflag, epoch_bits | kFlagInc);
-        }
-    }
-    __syncwarp();
-}
-
 // Resident CTAs of 128 threads per SM the register budget is sized for.
 constexpr int warp_tile_min_blocks(int R) { return R <= 2 ? 5 : (R == 4 ? 4 : 3); }
 
@@ -848,7 +852,7 @@ __global__ void __launch_bounds__(128, warp_tile_min_blocks(R)) a2b_fwd_w_kernel
 
         const bool more = s0 + TILE < len;
         const bool use64 = a.fp64_min_len >= 0 && len >= a.fp64_min_len;
-        fwd_lookback_warp(a, b, t, more, tile, epoch_bits, use64, s_carry[w], s_scratch[w]);
+        fwd_carry_warp(a, b, t, more, tile, epoch_bits, use64, s_carry[w], s_scratch[w]);
         Frame<float> c32;
         frame_load(c32, s_carry[w]);
         const float o0 = c32.p[0], o1 = c32.p[1], o2 = c32.p[2];
@@ -877,53 +881,6 @@ __global__ void __launch_bounds__(128, warp_tile_min_blocks(R)) a2b_fwd_w_kernel
     }
     __syncthreads();
     finish_launch(&a.hdr->fwd_ticket, &a.hdr->fwd_done, &a.hdr->fwd_epoch);
-}
-
-// Backward look-back of one warp tile over its successors' (G, S) sums (about
-// the world origin, FP64).  `own` (lane 0) is this tile's sums; `carry` (6
-// doubles, shared) receives the sums over all later tiles of the chain.
-__device__ __noinline__ void bwd_lookback_warp(const A2bArgs &a, int b, int t, int t_last, const double *own,
-                                               unsigned epoch_bits, double *carry) {
-    const int lane = threadIdx.x & 31;
-    TileRecord *base = a.rec + (size_t)b * a.ntiles;
-    if (lane == 0) {
-        for (int i = 0; i < 6; i++) carry[i] = 0.0;
-        if (t > 0 && t < t_last) {
-            for (int i = 0; i < 6; i++) base[t].bagg[i] = own[i];
-            st_release(&base[t].bflag, epoch_bits | kFlagAgg);
-        }
-    }
-    bool ok = true;
-    for (int tt0 = t + 1; tt0 <= t_last; tt0 += 32) {
-        const int tt = tt0 + lane;
-        bool lane_ok = true;
-        unsigned f = 0;
-        if (tt <= t_last) f = wait_flag(&base[tt].bflag, epoch_bits, a.hdr, lane_ok);
-        if (__ballot_sync(0xffffffffu, !lane_ok)) {
-            ok = false;
-            break;
-        }
-        const unsigned incm = __ballot_sync(0xffffffffu, tt <= t_last && (f & 3u) == kFlagInc);
-        const int stop = incm ? __ffs(incm) - 1 : min(31, t_last - tt0);
-        if (lane == 0) {
-            for (int i = 0; i <= stop; i++) {
-                const TileRecord *q = base + tt0 + i;
-                (void)ld_acquire(&q->bflag);
-                const double *v = (incm && i == stop) ? q->binc : q->bagg;
-                for (int k = 0; k < 6; k++) carry[k] += v[k];
-            }
-        }
-        if (incm) break;
-    }
-    if (lane == 0) {
-        if (!ok)
-            for (int i = 0; i < 6; i++) carry[i] = 0.0;
-        if (t > 0) {
-            for (int i = 0; i < 6; i++) base[t].binc[i] = own[i] + carry[i];
-            st_release(&base[t].bflag, epoch_bits | kFlagInc);
-        }
-    }
-    __syncwarp();
 }
 
 template <int R>
@@ -1022,31 +979,12 @@ __global__ void __launch_bounds__(128, warp_tile_min_blocks(R)) a2b_bwd_w_kernel
         const float v6[6] = {Gt[0], Gt[1], Gt[2], St[0], St[1], St[2]};
 #pragma unroll
         for (int i = 0; i < 6; i++) suf[i] = warp_suffix_exclusive(v6[i], lane, tot[i]);
-        if (lane == 0) {
-            // own sums about the world origin: S + o x G
-            const double o[3] = {org[0], org[1], org[2]};
-            double td[6] = {tot[0], tot[1], tot[2], tot[3], tot[4], tot[5]}, ox[3];
-            cross3(o, td, ox);
-            for (int i = 0; i < 3; i++) {
-                s_own[w][i] = td[i];
-                s_own[w][3 + i] = td[3 + i] + ox[i];
-            }
-        }
-        __syncwarp();
+        own_sums_world(tot, org, s_own[w]);
         const int t_last = (len - 1) / TILE;
-        bwd_lookback_warp(a, b, t, t_last, s_own[w], epoch_bits, s_carry[w]);
+        bwd_carry_warp(a, b, t, t_last, s_own[w], epoch_bits, s_carry[w]);
         // carry from later tiles, moved to this tile's origin: S_o = S_w - o x G
         float cg[3], cs[3];
-        {
-            const double o[3] = {org[0], org[1], org[2]};
-            const double *cw = s_carry[w];
-            double ox[3];
-            cross3(o, cw, ox);
-            for (int i = 0; i < 3; i++) {
-                cg[i] = (float)cw[i];
-                cs[i] = (float)(cw[3 + i] - ox[i]);
-            }
-        }
+        carry_to_origin(s_carry[w], org, cg, cs);
         // incoming suffix of this lane, in its local frame: G' = R^T G, S' = R^T (S - p x G)
         float Gw[3], Sw[3], G[3], S[3];
 #pragma unroll

@@ -265,4 +265,57 @@ int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const u
                           workspace_bytes, batch, max_len, max_atoms, opt, stream);
 }
 
+static int rmsd_fwd_common(bool f64, const void *src, const void *dst, const int32_t *num_atoms, int batch,
+                           int stride, int center, void *rmsd, void *ut, double *centroids, void *ws, size_t ws_bytes,
+                           void *stream) {
+    if (batch < 0 || stride < 0) return TPL_ERR_ARGUMENT;
+    if (batch == 0) return TPL_OK;
+    if (!src || !dst || !num_atoms || !rmsd || !ut || (center && !centroids)) return TPL_ERR_ARGUMENT;
+    if (ws) {
+        int s = check_ws(ws, ws_bytes, sizeof(WsHeader));
+        if (s) return s;
+    }
+    return rmsd_forward(f64, src, dst, num_atoms, batch, stride, center, rmsd, ut, centroids, ws,
+                        (cudaStream_t)stream);
+}
+
+int tpl_rmsd_forward_f32(const float *src, const float *dst, const int32_t *num_atoms, int batch, int atoms_stride,
+                         int center, float *rmsd, float *ut, double *centroids, void *workspace,
+                         size_t workspace_bytes, void *stream) {
+    return rmsd_fwd_common(false, src, dst, num_atoms, batch, atoms_stride, center, rmsd, ut, centroids, workspace,
+                           workspace_bytes, stream);
+}
+
+int tpl_rmsd_forward_f64(const double *src, const double *dst, const int32_t *num_atoms, int batch, int atoms_stride,
+                         int center, double *rmsd, double *ut, double *centroids, void *workspace,
+                         size_t workspace_bytes, void *stream) {
+    return rmsd_fwd_common(true, src, dst, num_atoms, batch, atoms_stride, center, rmsd, ut, centroids, workspace,
+                           workspace_bytes, stream);
+}
+
+static int rmsd_bwd_common(bool f64, const void *grad_rmsd, const void *src, const void *dst, const int32_t *num_atoms,
+                           const void *rmsd, const void *ut, const double *centroids, int batch, int stride,
+                           int center, void *grad_src, void *stream) {
+    if (batch < 0 || stride < 0) return TPL_ERR_ARGUMENT;
+    if (batch == 0) return TPL_OK;
+    if (!grad_rmsd || !src || !dst || !num_atoms || !rmsd || !ut || !grad_src || (center && !centroids))
+        return TPL_ERR_ARGUMENT;
+    return rmsd_backward(f64, grad_rmsd, src, dst, num_atoms, rmsd, ut, centroids, batch, stride, center, grad_src,
+                         (cudaStream_t)stream);
+}
+
+int tpl_rmsd_backward_f32(const float *grad_rmsd, const float *src, const float *dst, const int32_t *num_atoms,
+                          const float *rmsd, const float *ut, const double *centroids, int batch, int atoms_stride,
+                          int center, float *grad_src, void *stream) {
+    return rmsd_bwd_common(false, grad_rmsd, src, dst, num_atoms, rmsd, ut, centroids, batch, atoms_stride, center,
+                           grad_src, stream);
+}
+
+int tpl_rmsd_backward_f64(const double *grad_rmsd, const double *src, const double *dst, const int32_t *num_atoms,
+                          const double *rmsd, const double *ut, const double *centroids, int batch, int atoms_stride,
+                          int center, double *grad_src, void *stream) {
+    return rmsd_bwd_common(true, grad_rmsd, src, dst, num_atoms, rmsd, ut, centroids, batch, atoms_stride, center,
+                           grad_src, stream);
+}
+
 }  // extern "C"

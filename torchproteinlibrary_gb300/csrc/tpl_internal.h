@@ -70,4 +70,11 @@ int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const uns
                  const void *angles, void *ws, int B, int L, int maxA, const tpl_options &opt, cudaStream_t st);
 int num_atoms_host(const char *seq);
 
+// Coords2RMSD launchers (tpl_rmsd.cu).
+int rmsd_forward(bool f64, const void *src, const void *dst, const int *num_atoms, int B, int stride, int center,
+                 void *rmsd, void *ut, double *centroids, void *ws, cudaStream_t st);
+int rmsd_backward(bool f64, const void *grad_rmsd, const void *src, const void *dst, const int *num_atoms,
+                  const void *rmsd, const void *ut, const double *centroids, int B, int stride, int center,
+                  void *grad_src, cudaStream_t st);
+
 }  // namespace tpl
