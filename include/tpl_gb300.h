@@ -42,7 +42,8 @@ typedef enum tpl_status {
     TPL_ERR_SEQUENCE = -5,          /* a residue letter outside the 20 standard ones */
     TPL_ERR_LOOKBACK_TIMEOUT = -6,  /* a bounded inter-tile wait gave up (device-detected) */
     TPL_ERR_ATOMS = -7,             /* a chain needs more atom slots than max_atoms */
-    TPL_ERR_UNSUPPORTED = -8        /* option combination without a compiled kernel */
+    TPL_ERR_UNSUPPORTED = -8,       /* option combination without a compiled kernel */
+    TPL_ERR_TOO_LARGE = -9          /* problem exceeds the fixed scratch of tpl_a2b_forward_f32_noalloc */
 } tpl_status;
 
 /* Tuning knobs.  A NULL options pointer, or a zero field, selects the tuned default. */
@@ -150,6 +151,31 @@ int tpl_a2c_backward_f32(float *grad_angles, const float *grad_coords, const uin
 int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const uint8_t *sequences, int seq_stride,
                          const double *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
                          int max_atoms, const tpl_options *opt, void *stream);
+
+/* Angles2Backbone forward, batched FP32, for callers that cannot allocate device
+ * memory.  This entry point has no counterpart in the reference.
+ *
+ * Some hosts cannot hand this library a workspace: a plugin or FFI caller that
+ * only owns the input and output buffers it passes in, or a process whose
+ * framework has already reserved the device memory, so that cudaMalloc fails.
+ * This variant of tpl_a2b_forward_f32 takes the same inputs and outputs but keeps
+ * its scratch (the look-back records of the tile scan) in a fixed 4 MiB array
+ * that the library declares in device memory; every GPU that loads the library
+ * holds that array until the process exits.  It calls no cudaMalloc or cudaFree.
+ *
+ *   - Size limit: 64 + 400 * batch * ceil(max_len / tile) bytes must fit in 4 MiB
+ *     (tile = 32 * residues_per_thread for warp tiles, 128 * residues_per_thread for
+ *     CTA tiles; 128 by default), e.g. 2048 chains of up to 640 residues.  Larger
+ *     problems return TPL_ERR_TOO_LARGE before anything is enqueued.
+ *   - The first call on a device looks up the array's device address on that
+ *     device; make that first call before any CUDA stream capture.
+ *   - All calls share the one array: it is cleared on `stream` at the start of every
+ *     call, keeps the last call's contents afterwards, and calls that overlap on
+ *     the GPU (two streams, or two host threads) race on it.
+ *   - Its records are not kept for a backward pass: run tpl_a2b_forward_f32 with a
+ *     workspace when the backward is needed. */
+int tpl_a2b_forward_f32_noalloc(const float *angles, const int32_t *lengths, float *coords, int batch, int max_len,
+                                const tpl_options *opt, void *stream);
 
 /* Coords2RMSD forward: least RMSD between src and dst after optimal superposition
  * (quaternion method), per chain.  Replaces Coords2RMSDGPU_forward

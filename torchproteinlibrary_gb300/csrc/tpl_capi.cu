@@ -79,13 +79,13 @@ const BondConsts &bond_constants() {
     return bc;
 }
 
-static tpl_options resolve(const tpl_options *opt) {
+tpl_options resolve(const tpl_options *opt) {
     tpl_options o{};
     if (opt) o = *opt;
     return o;
 }
 
-static bool options_ok(const tpl_options &o) {
+bool options_ok(const tpl_options &o) {
     const int r = o.residues_per_thread;
     if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8)) return false;
     if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128)) return false;  // 0: warp tiles, 128: CTA tiles
@@ -93,7 +93,7 @@ static bool options_ok(const tpl_options &o) {
     return true;
 }
 
-static size_t a2b_ws(int B, int L, const tpl_options &o) {
+size_t a2b_ws(int B, int L, const tpl_options &o) {
     const int tile = a2b_tile_for(o);
     const int plain_chunk = 256;  // the plain FP64 backward keeps one record per 256-residue chunk
     const int smallest = tile < plain_chunk ? tile : plain_chunk;
@@ -117,6 +117,7 @@ const char *tpl_status_string(int status) {
         case TPL_ERR_LOOKBACK_TIMEOUT: return "inter-tile look-back wait timed out";
         case TPL_ERR_ATOMS: return "chain has more atoms than max_atoms";
         case TPL_ERR_UNSUPPORTED: return "unsupported option combination";
+        case TPL_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
     }
     return "unknown status";
 }

@@ -61,6 +61,9 @@ int a2b_forward_f64_plain(const double *angles, const int32_t *lengths, double *
 int a2b_backward_f64_plain(double *grad_angles, const double *grad_coords, const double *angles,
                            const int32_t *lengths, void *ws, int B, int L, cudaStream_t st);
 int a2b_tile_for(const tpl_options &opt);
+size_t a2b_ws(int B, int L, const tpl_options &o);  // workspace bytes of the FP32 Angles2Backbone entries
+tpl_options resolve(const tpl_options *opt);
+bool options_ok(const tpl_options &o);
 
 // Angles2Coords launchers (tpl_a2c.cu).  ws holds at least a WsHeader (status word).
 int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *angles, void *coords,
