@@ -497,7 +497,7 @@ def main():
                     help="chains per GPU (smaller batches are for profiling; the metric uses 4096)")
     ap.add_argument("--rpt", type=int, default=0,
                     help="residues per thread; 0 = autotune (the default)")
-    ap.add_argument("--cta", type=int, default=0, help="0 = warp tiles, 128 = CTA tiles (with --rpt)")
+    ap.add_argument("--cta", type=int, default=0, help="0 = warp tiles, 128 = CTA tiles, 32 = one warp per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
     args = ap.parse_args()

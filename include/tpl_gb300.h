@@ -48,8 +48,13 @@ typedef enum tpl_status {
 
 /* Tuning knobs.  A NULL options pointer, or a zero field, selects the tuned default. */
 typedef struct tpl_options {
-    int residues_per_thread;   /* residues each thread scans serially: 1, 2, 4 or 8 */
-    int threads_per_cta;       /* 64, 128 or 256 */
+    int residues_per_thread;   /* residues each thread scans serially: 1, 2, 4 or 8 (4 or 8 when
+                                  threads_per_cta = 32) */
+    int threads_per_cta;       /* scan scheme: 0 = warp-granular tiles of 32 R residues joined by
+                                  look-back; 128 = CTA tiles of 128 R residues; 32 = one warp walks
+                                  a whole chain in chunks of 32 R residues (no look-back; the
+                                  forward records the chain frame every 128 residues in the
+                                  workspace and the backward starts from those records) */
     int fp64_carry_min_len;    /* chains at least this long compose inter-tile carries in FP64;
                                   0 = default (always), -1 = never */
     int renormalize;           /* 0 = default (on), 1 = on, -1 = off: Newton-Schulz renormalisation
@@ -176,6 +181,11 @@ int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const u
  *     workspace when the backward is needed. */
 int tpl_a2b_forward_f32_noalloc(const float *angles, const int32_t *lengths, float *coords, int batch, int max_len,
                                 const tpl_options *opt, void *stream);
+
+/* Diagnostics (no counterpart in the reference): s[i], c[i] = sin, cos of a[i] as
+ * the FP32 Angles2Backbone kernels evaluate them (Cody-Waite reduction by pi/2 and
+ * Taylor series), for n device floats on `stream`. */
+int tpl_sincos_f32(const float *a, float *s, float *c, int n, void *stream);
 
 /* Coords2RMSD forward: least RMSD between src and dst after optimal superposition
  * (quaternion method), per chain.  Replaces Coords2RMSDGPU_forward

@@ -99,10 +99,12 @@ def test_fp64_plain_matches_oracle(rm, B, L, seed):
     check(c, gi, rc, rg, lengths, L, COORD_TOL_F64, GRAD_TOL_F64)
 
 
-@pytest.mark.parametrize("rpt,cta", [(1, 0), (2, 0), (4, 0), (8, 0), (1, 128), (4, 128), (8, 128)])
+@pytest.mark.parametrize("rpt,cta", [(1, 0), (2, 0), (4, 0), (8, 0), (1, 128), (4, 128), (8, 128), (4, 32),
+                                      (8, 32)])
 def test_tile_shapes_and_lookback(rm, rpt, cta):
     """Chains of 1000 residues split into up to 32 warp tiles (R=1: 32-residue tiles)
-    or CTA tiles (128 R residues, one tile at R=8); all within tolerance of the oracle."""
+    or CTA tiles (128 R residues, one tile at R=8), or walked by one warp per chain
+    in chunks of 32 R residues (cta=32); all within tolerance of the oracle."""
     B, L = 6, 1000
     ang, lengths, g = make_case(B, L, 40 + rpt, lengths=[1000, 999, 129, 128, 127, 1])
     rm.set_options(rpt, 0, 0, 0, cta)
@@ -130,14 +132,19 @@ def test_fp64_carry_threshold_and_renorm_off(rm):
         check(c, gi, rc, rg, lengths, L, ctol, GRAD_TOL_F32)
 
 
-def test_padding_nan_does_not_leak(rm):
+@pytest.mark.parametrize("rpt,cta", [(0, 0), (8, 32), (4, 32)])
+def test_padding_nan_does_not_leak(rm, rpt, cta):
     B, L = 4, 64
     ang, lengths, g = make_case(B, L, 9, lengths=[64, 30, 1, 0])
     for b, n in enumerate(lengths):
         ang[b, :, n:] = np.nan
         g[b, 9 * n:] = np.nan
     ang[1, 2, 29] = np.nan  # omega of the last residue is never used
-    c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+    rm.set_options(rpt, 0, 0, 0, cta)
+    try:
+        c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+    finally:
+        rm.set_options(0, 0, 0, 0)
     a2 = np.nan_to_num(ang, nan=0.0)
     g2 = np.nan_to_num(g, nan=0.0)
     rc, rg = oracle_ref(a2, lengths, g2, True)
@@ -296,3 +303,108 @@ def test_config3_full_size_against_fp64_form(rm):
     idx = np.argsort(lengths)[-2:]
     rc, rg = oracle_ref(ang[idx], lengths[idx], g[idx], True)
     check(c64[idx], g64[idx], rc, rg, lengths[idx], 700, COORD_TOL_F64, GRAD_TOL_F64)
+
+
+@pytest.mark.parametrize("rpt", [4, 8])
+@pytest.mark.parametrize("L", [1001, 258, 1000])
+def test_one_warp_per_chain_ragged_and_unaligned(rm, rpt, L):
+    """One warp per chain over ragged lengths at chunk edges, with rows that are not
+    16-byte aligned (L % 4 != 0: scalar loads and stores) and aligned (float4)."""
+    lens = [L, L - 1, 257, 256, 255, 129, 128, 127, 1, 0]
+    ang, lengths, g = make_case(len(lens), L, 300 + L + rpt, lengths=lens)
+    rm.set_options(rpt, 0, 0, 0, 32)
+    try:
+        c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+    finally:
+        rm.set_options(0, 0, 0, 0)
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def test_one_warp_per_chain_mixed_chunk_sizes_through_c_abi(built):
+    """The backward starts its chunks from frames the forward recorded every 128
+    residues, so a forward with 256-residue chunks and a backward with 128-residue
+    chunks (and the reverse) agree with the oracle."""
+    from torchproteinlibrary_gb300 import capi
+    lib = capi.lib()
+    dev = torch.device("cuda")
+    B, L = 8, 640
+    ang, lengths, g = make_case(B, L, 91, lengths=[640, 639, 600, 384, 257, 128, 3, 0])
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    a = torch.tensor(ang, dtype=torch.float32, device=dev)
+    ln = torch.tensor(lengths, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    for cf, cb in [(8, 4), (4, 8)]:
+        of, ob = capi.options(residues_per_thread=cf, threads_per_cta=32), \
+            capi.options(residues_per_thread=cb, threads_per_cta=32)
+        n = max(lib.tpl_a2b_workspace_bytes(B, L, ctypes.byref(of)), lib.tpl_a2b_workspace_bytes(B, L, ctypes.byref(ob)))
+        ws = torch.zeros(n, dtype=torch.uint8, device=dev)
+        coords = torch.full((B, 9 * L), float("nan"), device=dev)
+        gi = torch.full((B, 3, L), float("nan"), device=dev)
+        st = capi.stream_ptr()
+        capi.check(lib.tpl_a2b_forward_f32(a.data_ptr(), ln.data_ptr(), coords.data_ptr(), ws.data_ptr(), n, B, L,
+                                           ctypes.byref(of), st), "forward")
+        capi.check(lib.tpl_a2b_backward_f32(gi.data_ptr(), gt.data_ptr(), a.data_ptr(), ln.data_ptr(), ws.data_ptr(),
+                                            n, B, L, ctypes.byref(ob), st), "backward")
+        torch.cuda.synchronize()
+        check(coords.double().cpu().numpy(), gi.double().cpu().numpy(), rc, rg, lengths, L, COORD_TOL_F32,
+              GRAD_TOL_F32)
+
+
+def test_one_warp_per_chain_graph_replay(rm):
+    dev = torch.device("cuda")
+    B, L = 96, 500
+    ang, lengths, g = make_case(B, L, 17)
+    a = torch.tensor(ang, dtype=torch.float32, device=dev)
+    ln = torch.tensor(lengths, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    rm.set_options(8, 0, 0, 0, 32)
+    try:
+        ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+        coords = torch.empty(B, 9 * L, device=dev)
+        gi = torch.empty(B, 3, L, device=dev)
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
+            rm.Angles2BackboneGPU_backward(gi, gt, a, ln, ws, torch.empty(0, device=dev))
+        torch.cuda.current_stream().wait_stream(s)
+        ref_c, ref_g = coords.clone(), gi.clone()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
+            rm.Angles2BackboneGPU_backward(gi, gt, a, ln, ws, torch.empty(0, device=dev))
+        for _ in range(2):
+            coords.zero_(); gi.zero_()
+            graph.replay()
+            torch.cuda.synchronize()
+            assert torch.equal(coords, ref_c) and torch.equal(gi, ref_g)
+        assert rm.workspace_status(ws) == 0
+    finally:
+        rm.set_options(0, 0, 0, 0)
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    check(ref_c.double().cpu().numpy(), ref_g.double().cpu().numpy(), rc, rg, lengths, L, COORD_TOL_F32,
+          GRAD_TOL_F32)
+
+
+def test_sincos_error_bound(built):
+    """The kernels' own sin/cos (Cody-Waite reduction by pi/2, Taylor series)
+    against FP64: within 2.5e-7 absolute on [-pi, pi] and up to |a| = 1e4, and
+    within 3e-7 of unit norm."""
+    from torchproteinlibrary_gb300 import capi
+    lib = capi.lib()
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(12)
+    x = np.concatenate([rng.uniform(-np.pi, np.pi, 200000), rng.uniform(-1e4, 1e4, 50000),
+                        np.linspace(-np.pi, np.pi, 4097), np.array([0.0, -0.0, np.pi / 4, -np.pi / 4, np.pi / 2])])
+    x = x.astype(np.float32)
+    a = torch.tensor(x, device=dev)
+    s = torch.empty_like(a)
+    c = torch.empty_like(a)
+    capi.check(lib.tpl_sincos_f32(a.data_ptr(), s.data_ptr(), c.data_ptr(), a.numel(), capi.stream_ptr()), "sincos")
+    torch.cuda.synchronize()
+    xs = x.astype(np.float64)
+    sv, cv = s.double().cpu().numpy(), c.double().cpu().numpy()
+    assert np.abs(sv - np.sin(xs)).max() <= 2.5e-7
+    assert np.abs(cv - np.cos(xs)).max() <= 2.5e-7
+    assert np.abs(sv * sv + cv * cv - 1.0).max() <= 3e-7

@@ -1311,6 +1311,7 @@ static A2bShape a2b_shape(const tpl_options &opt, bool backward) {
 }
 
 int a2b_tile_for(const tpl_options &opt) {
+    if (opt.threads_per_cta == 32) return a2b_chain_record_stride();  // one warp per chain: frame records
     A2bShape f = a2b_shape(opt, false);
     return f.R * f.NT;
 }
@@ -1373,6 +1374,7 @@ static int launch_bwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
 int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, void *ws, int B, int L,
                     const tpl_options &opt, cudaStream_t st) {
     if (B == 0 || L == 0) return TPL_OK;
+    if (opt.threads_per_cta == 32) return a2b_forward_chain(angles, lengths, coords, ws, B, L, opt, st);
     A2bShape s = a2b_shape(opt, false);
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.coords = coords;
@@ -1397,6 +1399,8 @@ int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, 
 int a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
                      void *ws, int B, int L, const tpl_options &opt, cudaStream_t st) {
     if (B == 0 || L == 0) return TPL_OK;
+    if (opt.threads_per_cta == 32)
+        return a2b_backward_chain(grad_angles, grad_coords, angles, lengths, ws, B, L, opt, st);
     A2bShape s = a2b_shape(opt, true);
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.grad_angles = grad_angles;

@@ -1,0 +1,612 @@
+// Angles2Backbone FP32, one warp per chain (threads_per_cta = 32), sm_103a.
+//
+// The tile kernels of tpl_a2b.cu split long chains over CTAs and join the pieces
+// by decoupled look-back.  When the batch alone fills the GPU (a few hundred
+// chains or more) that machinery is pure overhead, so here one warp owns one
+// chain and walks it chunk after chunk, holding the chain frame at the chunk start
+// in registers.  A chunk is 32 C residues, C = 4 or 8 contiguous residues per
+// lane, so every global access is a coalesced row piece of the chunk.
+//
+// Forward, per chunk k with chain frame F_k at its start:
+//   1. each lane composes the 3C joints of its residues from identity (the joint
+//      algebra of Layers/ReducedModel/cBackboneProteinCPUKernels.cpp:42-58, in the
+//      factored form of tpl_common.cuh) and stages the lane-local N, CA, C
+//      positions in a per-warp shared buffer;
+//   2. a Kogge-Stone warp scan of the lane transforms gives each lane's exclusive
+//      prefix E_l, and its world frame is P_l = F_k o E_l;
+//   3. lanes map their staged positions through P_l in place and the warp stores
+//      the chunk's 9 * 32C coordinates as coalesced float4 rows (zeros past the
+//      chain length);
+//   4. F_{k+1} = F_k o (chunk total).  The world frame at every 128-residue
+//      boundary is recorded in the workspace for the backward.
+// Backward (reference: cBackboneProteinCUDAKernels.cu:84-163), chunks last to
+// first, starting each chunk from the frame the forward recorded:
+//   1. the same walk and scan; the chunk's dL/dx is staged by a coalesced load and
+//      rotated into each lane's local frame;
+//   2. lane sums G = sum g, S = sum x x g are moved to the chunk frame, suffix-
+//      scanned over the warp and completed by the running sums of later chunks;
+//   3. each lane walks its residues backwards, accumulating (G, S), and evaluates
+//      dL/dtheta_m = u_m . (S_m - x_m x G_m) for its 3C joints.
+// No CTA-wide barrier, no atomics and no FP64 on this path.
+#include "tpl_common.cuh"
+#include "tpl_internal.h"
+
+namespace tpl {
+namespace {
+
+constexpr int kWarpsPerCta = 4;
+constexpr int kRecordStride = 128;  // residues between recorded chain frames
+
+// One recorded chain frame (rotation row-major, translation), laid over the
+// workspace's record array.
+struct ChainRecord {
+    float f[12];
+};
+
+struct ChainArgs {
+    const float *angles;
+    const int *lengths;
+    float *coords;
+    float *grad_angles;
+    const float *grad_coords;
+    WsHeader *hdr;
+    ChainRecord *rec;
+    int B, L, nrec;
+    int renorm;
+    int vec;  // rows are 16-byte aligned (L % 4 == 0, aligned bases): float4 accesses
+    BondConsts bc;
+};
+
+__device__ __forceinline__ void record_error(WsHeader *h, int code) { atomicCAS(&h->status, 0u, (unsigned)code); }
+
+// sin and cos without tables or special-function units: Cody-Waite reduction by
+// pi/2 (two-term split of pi/2, exact products in the FMA) to |r| <= pi/4, then the
+// Taylor series of sin to r^9 and of cos to r^10 (truncation below 2e-9 on that
+// range), and the quadrant's swap and signs.  |a| > 1e4 and NaN take sincosf.
+__device__ __forceinline__ void sincos_poly(float a, float *s, float *c) {
+    if (!(fabsf(a) <= 1.0e4f)) {
+        sincosf(a, s, c);
+        return;
+    }
+    constexpr float kTwoOverPi = 0.636619772367581343f;
+    constexpr float kPio2Hi = 1.57079637050628662f;      // float(pi / 2)
+    constexpr float kPio2Lo = -4.37113900018624283e-8f;  // pi / 2 - kPio2Hi
+    const float k = rintf(a * kTwoOverPi);
+    float r = fmaf(-k, kPio2Hi, a);
+    r = fmaf(-k, kPio2Lo, r);
+    const float r2 = r * r;
+    // 1/n! coefficients
+    float ps = fmaf(r2, 2.7557319223985891e-6f, -1.9841269841269841e-4f);
+    ps = fmaf(ps, r2, 8.3333333333333333e-3f);
+    ps = fmaf(ps, r2, -1.6666666666666667e-1f);
+    const float sr = fmaf(ps * r2, r, r);
+    float pc = fmaf(r2, -2.7557319223985891e-7f, 2.4801587301587302e-5f);
+    pc = fmaf(pc, r2, -1.3888888888888889e-3f);
+    pc = fmaf(pc, r2, 4.1666666666666667e-2f);
+    pc = fmaf(pc, r2, -0.5f);
+    const float cr = fmaf(pc, r2, 1.0f);
+    const int q = ((int)k) & 3;  // a = r + q pi/2 (mod 2 pi)
+    float ss = (q & 1) ? cr : sr;
+    float cc = (q & 1) ? sr : cr;
+    if (q & 2) ss = -ss;
+    if ((q + 1) & 2) cc = -cc;
+    *s = ss;
+    *c = cc;
+}
+
+__device__ __forceinline__ Frame<float> shfl_idx_frame(const Frame<float> &f, int src) {
+    Frame<float> o;
+#pragma unroll
+    for (int i = 0; i < 9; i++) o.r[i] = __shfl_sync(0xffffffffu, f.r[i], src);
+#pragma unroll
+    for (int i = 0; i < 3; i++) o.p[i] = __shfl_sync(0xffffffffu, f.p[i], src);
+    return o;
+}
+
+// Exclusive prefix of the lane transforms in lane order, and the warp total.
+__device__ __forceinline__ Frame<float> warp_exclusive_total(Frame<float> t, int lane, bool renorm,
+                                                             Frame<float> &total) {
+    if (renorm) renormalize(t);
+    const Frame<float> inc = warp_scan_frames(t, lane);
+    total = shfl_idx_frame(inc, 31);
+    Frame<float> exc = shfl_up_frame(inc, 1);
+    if (lane == 0) frame_identity(exc);
+    return exc;
+}
+
+// Sum over lanes > lane (exclusive suffix) of v, and the warp total.
+__device__ __forceinline__ float warp_suffix_excl(float v, int lane, float &total) {
+    float inc = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, inc, off);
+        if (lane + off < 32) inc += o;
+    }
+    total = __shfl_sync(0xffffffffu, inc, 0);
+    return inc - v;
+}
+
+// Angles of one row for residues j..j+3, zero from len on.
+__device__ __forceinline__ void load4(const float *row, int j, int len, bool vec, float (&v)[4]) {
+    if (vec) {
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (j < len) x = __ldg(reinterpret_cast<const float4 *>(row + j));
+        v[0] = x.x;
+        v[1] = j + 1 < len ? x.y : 0.f;
+        v[2] = j + 2 < len ? x.z : 0.f;
+        v[3] = j + 3 < len ? x.w : 0.f;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; i++) v[i] = j + i < len ? __ldg(row + j + i) : 0.f;
+    }
+}
+
+// Four residues of a lane's walk: composes their 12 joints onto f and writes the
+// lane-local N, CA, C positions (36 floats, 9 float4s) to seg.
+__device__ __forceinline__ void walk4(const BondConsts &bc, Frame<float> &f, const float (&a0)[4],
+                                      const float (&a1)[4], const float (&a2)[4], float *seg) {
+    float buf[36];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        float s0, c0, s1, c1, s2, c2;
+        sincos_poly(a0[r], &s0, &c0);
+        sincos_poly(a1[r], &s1, &c1);
+        sincos_poly(a2[r], &s2, &c2);
+        buf[9 * r] = f.p[0]; buf[9 * r + 1] = f.p[1]; buf[9 * r + 2] = f.p[2];
+        apply_joint(f, bc.cb[0], bc.sb[0], bc.d[0], c0, s0);
+        buf[9 * r + 3] = f.p[0]; buf[9 * r + 4] = f.p[1]; buf[9 * r + 5] = f.p[2];
+        apply_joint(f, bc.cb[1], bc.sb[1], bc.d[1], c1, s1);
+        buf[9 * r + 6] = f.p[0]; buf[9 * r + 7] = f.p[1]; buf[9 * r + 8] = f.p[2];
+        apply_joint(f, bc.cb[2], bc.sb[2], bc.d[2], c2, s2);
+#pragma unroll
+        for (int q = 0; q < 9; q++)  // flush the float4s this residue completed
+            if (4 * q + 3 <= 9 * r + 8 && 4 * q + 3 > 9 * r - 1)
+                *reinterpret_cast<float4 *>(seg + 4 * q) =
+                    make_float4(buf[4 * q], buf[4 * q + 1], buf[4 * q + 2], buf[4 * q + 3]);
+    }
+}
+
+// Walk of one lane's C residues (j0..j0+C-1) from identity, in groups of four;
+// positions (9C floats) go to seg.  Returns the lane transform.  Angles at and
+// past the chain end (and omega of its last residue) are taken as 0, so padding
+// values, NaN included, never enter a transform.
+template <int C>
+__device__ __forceinline__ Frame<float> walk_chunk(const BondConsts &bc, const float *ang, int L, int j0, int len,
+                                                   bool vec, float *seg) {
+    Frame<float> f;
+    frame_identity(f);
+#pragma unroll 1
+    for (int g = 0; g < C / 4; g++) {
+        const int j = j0 + 4 * g;
+        float v0[4], v1[4], v2[4];
+        load4(ang, j, len, vec, v0);
+        load4(ang + L, j, len, vec, v1);
+        load4(ang + 2 * L, j, len - 1, vec, v2);  // omega of the last residue moves nothing: 0
+        walk4(bc, f, v0, v1, v2, seg + 36 * g);
+    }
+    return f;
+}
+
+// Map the 3C staged points of a lane through P in place; zeros for residues at or
+// past len.
+template <int C>
+__device__ __forceinline__ void map_positions(float *seg, const Frame<float> &P, int j0, int len) {
+#pragma unroll 1
+    for (int g = 0; g < 3 * C / 4; g++) {
+        float4 *q = reinterpret_cast<float4 *>(seg + 12 * g);
+        const float4 v0 = q[0], v1 = q[1], v2 = q[2];
+        const float x[12] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w, v2.x, v2.y, v2.z, v2.w};
+        float y[12];
+#pragma unroll
+        for (int pt = 0; pt < 4; pt++) {
+            frame_point(P, x[3 * pt], x[3 * pt + 1], x[3 * pt + 2], &y[3 * pt]);
+            if (j0 + (4 * g + pt) / 3 >= len) y[3 * pt] = y[3 * pt + 1] = y[3 * pt + 2] = 0.f;
+        }
+        q[0] = make_float4(y[0], y[1], y[2], y[3]);
+        q[1] = make_float4(y[4], y[5], y[6], y[7]);
+        q[2] = make_float4(y[8], y[9], y[10], y[11]);
+    }
+}
+
+// Stage floats [0, 32 SEG) of a chunk: src[f] for f < nvalid, 0 after.  Lane l's
+// segment (floats l SEG .. l SEG + SEG - 1) lands at stage + l SP.
+template <int SEG, int SP>
+__device__ __forceinline__ void stage_chunk(float *stage, const float *src, int nvalid, int lane, bool vec) {
+    if (vec) {
+#pragma unroll 2
+        for (int q = lane; q < 8 * SEG; q += 32) {
+            const int f = 4 * q, sl = f / SEG;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (f < nvalid) {
+                v = __ldcs(reinterpret_cast<const float4 *>(src) + q);
+                if (f + 1 >= nvalid) v.y = 0.f;
+                if (f + 2 >= nvalid) v.z = 0.f;
+                if (f + 3 >= nvalid) v.w = 0.f;
+            }
+            *reinterpret_cast<float4 *>(stage + sl * SP + f - sl * SEG) = v;
+        }
+    } else {
+        for (int f = lane; f < 32 * SEG; f += 32) {
+            const int sl = f / SEG;
+            stage[sl * SP + f - sl * SEG] = f < nvalid ? src[f] : 0.f;
+        }
+    }
+}
+
+// Store staged floats [0, n) of a chunk to dst (coalesced).
+template <int SEG, int SP>
+__device__ __forceinline__ void store_chunk(float *dst, const float *stage, int n, int lane, bool vec) {
+    if (vec) {
+#pragma unroll 2
+        for (int q = lane; 4 * q < n; q += 32) {
+            const int f = 4 * q, sl = f / SEG;
+            __stcs(reinterpret_cast<float4 *>(dst) + q, *reinterpret_cast<const float4 *>(stage + sl * SP + f - sl * SEG));
+        }
+    } else {
+        for (int f = lane; f < n; f += 32) {
+            const int sl = f / SEG;
+            dst[f] = stage[sl * SP + f - sl * SEG];
+        }
+    }
+}
+
+__device__ __forceinline__ void zero_floats(float *dst, int n, int lane, bool vec) {
+    if (vec) {
+        for (int q = lane; 4 * q < n; q += 32) __stcs(reinterpret_cast<float4 *>(dst) + q, make_float4(0.f, 0.f, 0.f, 0.f));
+    } else {
+        for (int f = lane; f < n; f += 32) dst[f] = 0.f;
+    }
+}
+
+__device__ __forceinline__ int checked_length(const ChainArgs &a, int b, int lane) {
+    int len = a.lengths[b];
+    if (len < 0 || len > a.L) {
+        if (lane == 0) record_error(a.hdr, TPL_ERR_LENGTH);
+        len = max(0, min(len, a.L));
+    }
+    return len;
+}
+
+constexpr int fwd_min_blocks(int C) { return C >= 8 ? 5 : 6; }
+constexpr int bwd_min_blocks(int C) { return C >= 8 ? 2 : 4; }
+
+template <int C>
+__global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_chain_kernel(ChainArgs a) {
+    constexpr int CH = 32 * C, SEG = 9 * C, SP = SEG + 4;
+    extern __shared__ __align__(16) float s_dyn[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarpsPerCta + w;
+    if (b >= a.B) return;  // warps are independent: no CTA-wide barrier follows
+    float *stage = s_dyn + w * 32 * SP;
+    float *seg = stage + lane * SP;
+    const int len = checked_length(a, b, lane);
+    const float *ang = a.angles + (size_t)b * 3 * a.L;
+    float *out = a.coords + (size_t)b * 9 * a.L;
+    ChainRecord *rec = a.rec + (size_t)b * a.nrec;
+    const bool vec = a.vec != 0;
+
+    Frame<float> F;  // chain frame at the chunk start (world)
+    frame_identity(F);
+    for (int s0 = 0; s0 < a.L; s0 += CH) {
+        const int nout = min(CH, a.L - s0);
+        float *dst = out + (size_t)9 * s0;
+        if (s0 >= len) {
+            zero_floats(dst, 9 * nout, lane, vec);
+            continue;
+        }
+        const int j0 = s0 + C * lane;
+        const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg);
+        Frame<float> tot;
+        const Frame<float> E = warp_exclusive_total(t, lane, a.renorm, tot);
+        Frame<float> P = compose(F, E);
+        if (a.renorm) renormalize(P);
+        if ((C * lane) % kRecordStride == 0 && j0 < len) {
+            float *r = rec[j0 / kRecordStride].f;
+#pragma unroll
+            for (int i = 0; i < 9; i++) r[i] = P.r[i];
+#pragma unroll
+            for (int i = 0; i < 3; i++) r[9 + i] = P.p[i];
+        }
+        F = compose(F, tot);
+        if (a.renorm) renormalize(F);
+        map_positions<C>(seg, P, j0, len);
+        __syncwarp();
+        store_chunk<SEG, SP>(dst, stage, 9 * nout, lane, vec);
+        __syncwarp();  // the next chunk's walk rewrites the staging buffer
+    }
+}
+
+template <int C>
+__global__ void __launch_bounds__(32 * kWarpsPerCta, bwd_min_blocks(C)) a2b_bwd_chain_kernel(ChainArgs a) {
+    constexpr int CH = 32 * C, SEG = 9 * C, SP = SEG + 4;
+    extern __shared__ __align__(16) float s_dyn[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarpsPerCta + w;
+    if (b >= a.B) return;
+    float *sx = s_dyn + w * 64 * SP;  // lane-local positions
+    float *sg = sx + 32 * SP;         // dL/dx, rotated in place into lane-local frames
+    float *xs = sx + lane * SP, *gs = sg + lane * SP;
+    const int len = checked_length(a, b, lane);
+    const float *ang = a.angles + (size_t)b * 3 * a.L;
+    const float *gin = a.grad_coords + (size_t)b * 9 * a.L;
+    float *gout = a.grad_angles + (size_t)b * 3 * a.L;
+    const ChainRecord *rec = a.rec + (size_t)b * a.nrec;
+    const bool vec = a.vec != 0;
+    const float inv_d0 = 1.f / a.bc.d[0], inv_d1 = 1.f / a.bc.d[1], inv_d2 = 1.f / a.bc.d[2];
+
+    // gradient rows past the last chunk that holds residues are zero
+    const int nchunk = (len + CH - 1) / CH;
+    const int s_end = min(a.L, nchunk * CH);
+    for (int k = 0; k < 3; k++) zero_floats(gout + (size_t)k * a.L + s_end, a.L - s_end, lane, vec && (s_end % 4 == 0));
+
+    // sums over all atoms after the current chunk: G, and S about origin oc
+    float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, oc[3] = {0.f, 0.f, 0.f};
+    for (int k = nchunk - 1; k >= 0; k--) {
+        const int s0 = k * CH;
+        const int nreal = min(CH, len - s0);
+        const int j0 = s0 + C * lane;
+        Frame<float> F;
+        frame_load(F, rec[s0 / kRecordStride].f);
+        {  // move the carried sums to this chunk's origin: S_o = S_oc + (oc - o) x G
+            const float d[3] = {oc[0] - F.p[0], oc[1] - F.p[1], oc[2] - F.p[2]};
+            float dx[3];
+            cross3(d, Gc, dx);
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                Sc[i] += dx[i];
+                oc[i] = F.p[i];
+            }
+        }
+        stage_chunk<SEG, SP>(sg, gin + (size_t)9 * s0, 9 * nreal, lane, vec);
+        const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, xs);
+        Frame<float> tot;
+        const Frame<float> E = warp_exclusive_total(t, lane, a.renorm, tot);
+        F.p[0] = F.p[1] = F.p[2] = 0.f;  // lane frames relative to the chunk origin
+        Frame<float> P = compose(F, E);
+        if (a.renorm) renormalize(P);
+        __syncwarp();  // staged dL/dx complete
+
+        // rotate the lane's dL/dx into its frame; lane sums about the lane origin
+        float Gl[3] = {0.f, 0.f, 0.f}, Sl[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int g = 0; g < 3 * C / 4; g++) {
+            float4 *gq = reinterpret_cast<float4 *>(gs + 12 * g);
+            const float4 *xq = reinterpret_cast<const float4 *>(xs + 12 * g);
+            const float4 g0 = gq[0], g1 = gq[1], g2 = gq[2];
+            const float4 x0 = xq[0], x1 = xq[1], x2 = xq[2];
+            const float gw[12] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x, g2.y, g2.z, g2.w};
+            const float xv[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x, x2.y, x2.z, x2.w};
+            float gl[12];
+#pragma unroll
+            for (int pt = 0; pt < 4; pt++) {
+                const float *v = gw + 3 * pt;
+                float *o = gl + 3 * pt;
+                o[0] = fmaf(P.r[0], v[0], fmaf(P.r[3], v[1], P.r[6] * v[2]));
+                o[1] = fmaf(P.r[1], v[0], fmaf(P.r[4], v[1], P.r[7] * v[2]));
+                o[2] = fmaf(P.r[2], v[0], fmaf(P.r[5], v[1], P.r[8] * v[2]));
+                float xg[3];
+                cross3(xv + 3 * pt, o, xg);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    Gl[c] += o[c];
+                    Sl[c] += xg[c];
+                }
+            }
+            gq[0] = make_float4(gl[0], gl[1], gl[2], gl[3]);
+            gq[1] = make_float4(gl[4], gl[5], gl[6], gl[7]);
+            gq[2] = make_float4(gl[8], gl[9], gl[10], gl[11]);
+        }
+        // lane sums in the chunk frame: G = R Gl, S = R Sl + p x G
+        float v6[6];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            v6[i] = fmaf(P.r[3 * i], Gl[0], fmaf(P.r[3 * i + 1], Gl[1], P.r[3 * i + 2] * Gl[2]));
+            v6[3 + i] = fmaf(P.r[3 * i], Sl[0], fmaf(P.r[3 * i + 1], Sl[1], P.r[3 * i + 2] * Sl[2]));
+        }
+        {
+            float pg[3];
+            cross3(P.p, v6, pg);
+#pragma unroll
+            for (int i = 0; i < 3; i++) v6[3 + i] += pg[i];
+        }
+        float Gin[3], Sin[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            float tg, ts;
+            Gin[i] = warp_suffix_excl(v6[i], lane, tg) + Gc[i];
+            Sin[i] = warp_suffix_excl(v6[3 + i], lane, ts) + Sc[i];
+            Gc[i] += tg;
+            Sc[i] += ts;
+        }
+        // incoming sums in the lane frame: G' = R^T G, S' = R^T (S - p x G)
+        float G[3], S[3];
+        {
+            float pg[3], Sm[3];
+            cross3(P.p, Gin, pg);
+#pragma unroll
+            for (int i = 0; i < 3; i++) Sm[i] = Sin[i] - pg[i];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                G[i] = fmaf(P.r[i], Gin[0], fmaf(P.r[3 + i], Gin[1], P.r[6 + i] * Gin[2]));
+                S[i] = fmaf(P.r[i], Sm[0], fmaf(P.r[3 + i], Sm[1], P.r[6 + i] * Sm[2]));
+            }
+        }
+        // backwards over the lane's residues, four at a time (9 float4s of positions
+        // and of gradients per group)
+        float nxt[3] = {t.p[0], t.p[1], t.p[2]};  // N of the residue after the lane's last
+#pragma unroll 1
+        for (int gi = C / 4 - 1; gi >= 0; gi--) {
+            const float4 *xq = reinterpret_cast<const float4 *>(xs + 36 * gi);
+            const float4 *gq = reinterpret_cast<const float4 *>(gs + 36 * gi);
+            float xb[36], gb[36];  // read as float4s when first needed
+            float gph[4], gps[4], gom[4];
+#pragma unroll
+            for (int r = 3; r >= 0; r--) {
+#pragma unroll
+                for (int q = (9 * r) / 4; q <= (9 * r + 8) / 4; q++)
+                    if (r == 3 || q < (9 * (r + 1)) / 4) {  // not read for residue r + 1
+                        const float4 xv = xq[q], gv = gq[q];
+                        xb[4 * q] = xv.x; xb[4 * q + 1] = xv.y; xb[4 * q + 2] = xv.z; xb[4 * q + 3] = xv.w;
+                        gb[4 * q] = gv.x; gb[4 * q + 1] = gv.y; gb[4 * q + 2] = gv.z; gb[4 * q + 3] = gv.w;
+                    }
+                float xN[3], xA[3], xC[3], gN[3], gA[3], gC[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    xN[c] = xb[9 * r + c]; xA[c] = xb[9 * r + 3 + c]; xC[c] = xb[9 * r + 6 + c];
+                    gN[c] = gb[9 * r + c]; gA[c] = gb[9 * r + 3 + c]; gC[c] = gb[9 * r + 6 + c];
+                }
+                float u[3], tmp[3], cr[3];
+                // omega_j: axis C -> N_{j+1}, through N_{j+1}; moves the atoms after C_j
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (nxt[c] - xC[c]) * inv_d2;
+                cross3(nxt, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gom[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                // psi_j: axis CA -> C, through C; same atoms
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xC[c] - xA[c]) * inv_d1;
+                cross3(xC, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gps[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                cross3(xC, gC, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += gC[c];
+                    S[c] += cr[c];
+                }
+                // phi_j: axis N -> CA, through CA; moves C_j and everything after
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xA[c] - xN[c]) * inv_d0;
+                cross3(xA, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gph[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                cross3(xA, gA, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += gA[c];
+                    S[c] += cr[c];
+                }
+                cross3(xN, gN, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    G[c] += gN[c];
+                    S[c] += cr[c];
+                    nxt[c] = xN[c];
+                }
+            }
+            // zeros at and past len; psi and omega of the last residue move nothing
+            const int jg = j0 + 4 * gi;
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int j = jg + r;
+                const bool ok = j < len, last = j == len - 1;
+                gph[r] = ok ? gph[r] : 0.f;
+                gps[r] = ok && !last ? gps[r] : 0.f;
+                gom[r] = ok && !last ? gom[r] : 0.f;
+            }
+            if (vec) {
+                if (jg < a.L) {
+                    __stcs(reinterpret_cast<float4 *>(gout + jg), make_float4(gph[0], gph[1], gph[2], gph[3]));
+                    __stcs(reinterpret_cast<float4 *>(gout + a.L + jg), make_float4(gps[0], gps[1], gps[2], gps[3]));
+                    __stcs(reinterpret_cast<float4 *>(gout + 2 * a.L + jg),
+                           make_float4(gom[0], gom[1], gom[2], gom[3]));
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const int j = jg + r;
+                    if (j < a.L) {
+                        gout[j] = gph[r];
+                        gout[a.L + j] = gps[r];
+                        gout[2 * a.L + j] = gom[r];
+                    }
+                }
+            }
+        }
+        __syncwarp();  // the next chunk rewrites both staging buffers
+    }
+}
+
+// Sincos check kernel for the tests: s[i], c[i] = sincos_poly(a[i]).
+__global__ void sincos_poly_kernel(const float *a, float *s, float *c, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) sincos_poly(a[i], s + i, c + i);
+}
+
+template <int C>
+constexpr int fwd_smem() {
+    return kWarpsPerCta * 32 * (9 * C + 4) * (int)sizeof(float);
+}
+template <int C>
+constexpr int bwd_smem() {
+    return 2 * fwd_smem<C>();
+}
+
+ChainArgs chain_args(const float *angles, const int32_t *lengths, void *ws, int B, int L, const tpl_options &opt) {
+    ChainArgs a{};
+    a.angles = angles;
+    a.lengths = lengths;
+    a.hdr = reinterpret_cast<WsHeader *>(ws);
+    a.rec = reinterpret_cast<ChainRecord *>(reinterpret_cast<char *>(ws) + sizeof(WsHeader));
+    a.B = B;
+    a.L = L;
+    a.nrec = (L + kRecordStride - 1) / kRecordStride;
+    a.renorm = opt.renormalize >= 0 ? 1 : 0;
+    a.bc = bond_constants();
+    return a;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <typename K>
+int launch_chain(K kernel, int smem, int B, const ChainArgs &a, cudaStream_t st) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return TPL_ERR_LAUNCH;
+    const int grid = (B + kWarpsPerCta - 1) / kWarpsPerCta;
+    kernel<<<grid, 32 * kWarpsPerCta, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+}  // namespace
+
+int a2b_chain_record_stride() { return kRecordStride; }
+
+int a2b_forward_chain(const float *angles, const int32_t *lengths, float *coords, void *ws, int B, int L,
+                      const tpl_options &opt, cudaStream_t st) {
+    if (B == 0 || L == 0) return TPL_OK;
+    ChainArgs a = chain_args(angles, lengths, ws, B, L, opt);
+    a.coords = coords;
+    a.vec = (L % 4 == 0) && aligned16(angles) && aligned16(coords);
+    const int C = opt.residues_per_thread > 0 ? opt.residues_per_thread : 8;
+    switch (C) {
+        case 4: return launch_chain(a2b_fwd_chain_kernel<4>, fwd_smem<4>(), B, a, st);
+        case 8: return launch_chain(a2b_fwd_chain_kernel<8>, fwd_smem<8>(), B, a, st);
+    }
+    return TPL_ERR_UNSUPPORTED;
+}
+
+int a2b_backward_chain(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
+                       void *ws, int B, int L, const tpl_options &opt, cudaStream_t st) {
+    if (B == 0 || L == 0) return TPL_OK;
+    ChainArgs a = chain_args(angles, lengths, ws, B, L, opt);
+    a.grad_angles = grad_angles;
+    a.grad_coords = grad_coords;
+    a.vec = (L % 4 == 0) && aligned16(angles) && aligned16(grad_angles) && aligned16(grad_coords);
+    const int C = opt.residues_per_thread > 0 ? opt.residues_per_thread : 8;
+    switch (C) {
+        case 4: return launch_chain(a2b_bwd_chain_kernel<4>, bwd_smem<4>(), B, a, st);
+        case 8: return launch_chain(a2b_bwd_chain_kernel<8>, bwd_smem<8>(), B, a, st);
+    }
+    return TPL_ERR_UNSUPPORTED;
+}
+
+int sincos_poly_f32(const float *a, float *s, float *c, int n, cudaStream_t st) {
+    if (n <= 0) return TPL_OK;
+    sincos_poly_kernel<<<(n + 255) / 256, 256, 0, st>>>(a, s, c, n);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+}  // namespace tpl

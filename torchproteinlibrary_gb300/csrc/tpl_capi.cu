@@ -88,7 +88,9 @@ tpl_options resolve(const tpl_options *opt) {
 bool options_ok(const tpl_options &o) {
     const int r = o.residues_per_thread;
     if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8)) return false;
-    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128)) return false;  // 0: warp tiles, 128: CTA tiles
+    // 0: warp tiles, 128: CTA tiles, 32: one warp per chain (4 or 8 residues per lane)
+    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128 || o.threads_per_cta == 32)) return false;
+    if (o.threads_per_cta == 32 && !(r == 0 || r == 4 || r == 8)) return false;
     if (o.max_ctas < 0) return false;
     return true;
 }
@@ -123,6 +125,11 @@ const char *tpl_status_string(int status) {
 }
 
 int tpl_version(void) { return 100; }
+
+int tpl_sincos_f32(const float *a, float *s, float *c, int n, void *stream) {
+    if (n < 0 || (n > 0 && (!a || !s || !c))) return TPL_ERR_ARGUMENT;
+    return sincos_poly_f32(a, s, c, n, (cudaStream_t)stream);
+}
 
 size_t tpl_a2b_workspace_bytes(int batch, int max_len, const tpl_options *opt) {
     if (batch < 0 || max_len < 0) return 0;

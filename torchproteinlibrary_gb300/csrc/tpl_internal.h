@@ -61,6 +61,15 @@ int a2b_forward_f64_plain(const double *angles, const int32_t *lengths, double *
 int a2b_backward_f64_plain(double *grad_angles, const double *grad_coords, const double *angles,
                            const int32_t *lengths, void *ws, int B, int L, cudaStream_t st);
 int a2b_tile_for(const tpl_options &opt);
+// One warp per chain (tpl_a2b_chain.cu; threads_per_cta = 32, residues_per_thread 4 or 8).
+// The forward records the chain frame every a2b_chain_record_stride() residues in
+// the workspace; the backward starts its chunks from those records.
+int a2b_forward_chain(const float *angles, const int32_t *lengths, float *coords, void *ws, int B, int L,
+                      const tpl_options &opt, cudaStream_t st);
+int a2b_backward_chain(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
+                       void *ws, int B, int L, const tpl_options &opt, cudaStream_t st);
+int a2b_chain_record_stride();
+int sincos_poly_f32(const float *a, float *s, float *c, int n, cudaStream_t st);
 size_t a2b_ws(int B, int L, const tpl_options &o);  // workspace bytes of the FP32 Angles2Backbone entries
 tpl_options resolve(const tpl_options *opt);
 bool options_ok(const tpl_options &o);
