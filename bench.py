@@ -33,7 +33,8 @@ sys.path.insert(0, ROOT)
 
 B_CHAINS, L_RES = 4096, 1000
 FWD_BYTES_PER_RES = 12 + 36          # angles in, N/CA/C coordinates out (FP32)
-BWD_BYTES_PER_RES = 12 + 36 + 12     # angles + dL/dcoords in, dL/dangles out
+BWD_BYTES_PER_RES = 12 + 36 + 12     # angles + dL/dcoords in, dL/dangles out (layer contract)
+BWD_COORDS_MOVED_PER_RES = 36 + 36 + 12  # the backward from coordinates reads coordinates, not angles
 WORKLOAD = "Angles2Backbone fwd+bwd, 4096 chains x 1000 residues, FP32"
 
 
@@ -211,7 +212,9 @@ def run_ours(args):
     sweep_rows = None
     if args.rpt:
         rm.set_options(args.rpt, 0, 0, 0, args.cta)
-        tuned = {"residues_per_thread": args.rpt, "threads_per_cta": args.cta, "fp64_carry_min_len": 0}
+        rm.set_backward_options(args.bwd_rpt)
+        tuned = {"residues_per_thread": args.rpt, "threads_per_cta": args.cta, "fp64_carry_min_len": 0,
+                 "backward_coords": {"residues_per_thread": args.bwd_rpt}}
     else:
         tuned = autotune.tune(ang, lengths, up, use_cache=False)
         if not args.no_extras:
@@ -226,8 +229,8 @@ def run_ours(args):
     def fwd():
         rm.Angles2BackboneGPU_forward(ang, coords, lengths, ws)
 
-    def bwd():
-        rm.Angles2BackboneGPU_backward(gang, up, ang, lengths, ws, none)
+    def bwd():  # what the float32 layer runs: the backward from the forward's coordinates
+        rm.Angles2BackboneGPU_backward_coords(gang, up, coords, lengths, ws)
 
     # warm-up (eager), then capture one step per graph for per-kernel events
     s = torch.cuda.Stream(device=dev)
@@ -305,14 +308,20 @@ def run_ours(args):
                    "l2": "inputs and outputs larger than L2; no flush", "launch": "CUDA graph per pass",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm",
-                     "kernel": f"a2b_{'bwd' if dom == 'backward' else 'fwd'}_{'w' if tuned['threads_per_cta'] == 0 else 'f32'}",
+                     "kernel": "a2b_bwd_coords_kernel" if dom == "backward" else
+                               {0: "a2b_fwd_w_kernel", 128: "a2b_fwd_f32_kernel", 32: "a2b_fwd_chain_kernel"}[
+                                   tuned["threads_per_cta"]],
                      "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": dom_bytes},
+                     "algorithmic_bytes_per_launch": dom_bytes,
+                     "bytes_moved_per_launch": B * L * (BWD_COORDS_MOVED_PER_RES if dom == "backward"
+                                                        else FWD_BYTES_PER_RES)},
         "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
         "tuned": tuned,
         "tile_sweep": [{k: (round(v, 5) if isinstance(v, float) else v) for k, v in r.items()}
                        for r in getattr(autotune.tune, "last_sweep", [])],
+        "backward_coords_sweep": [{k: (round(v, 7) if isinstance(v, float) else v) for k, v in r.items()}
+                                  for r in getattr(autotune.tune, "last_backward_sweep", [])],
         "fp64_carry_sweep": sweep_rows,
         "gpu_launches": 2 * args.steps,
         "e2e": e2e,
@@ -497,6 +506,7 @@ def main():
                     help="chains per GPU (smaller batches are for profiling; the metric uses 4096)")
     ap.add_argument("--rpt", type=int, default=0,
                     help="residues per thread; 0 = autotune (the default)")
+    ap.add_argument("--bwd-rpt", type=int, default=4, help="residues per lane of the coordinate backward (with --rpt)")
     ap.add_argument("--cta", type=int, default=0, help="0 = warp tiles, 128 = CTA tiles, 32 = one warp per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")

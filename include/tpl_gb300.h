@@ -40,7 +40,7 @@ typedef enum tpl_status {
     TPL_ERR_LAUNCH = -3,            /* CUDA reported an error at launch */
     TPL_ERR_LENGTH = -4,            /* a chain length outside [0, max_len] (device-detected) */
     TPL_ERR_SEQUENCE = -5,          /* a residue letter outside the 20 standard ones */
-    TPL_ERR_LOOKBACK_TIMEOUT = -6,  /* a bounded inter-tile wait gave up (device-detected) */
+    TPL_ERR_LOOKBACK_TIMEOUT = -6,  /* a bounded device wait gave up: inter-tile look-back or bulk copy */
     TPL_ERR_ATOMS = -7,             /* a chain needs more atom slots than max_atoms */
     TPL_ERR_UNSUPPORTED = -8,       /* option combination without a compiled kernel */
     TPL_ERR_TOO_LARGE = -9          /* problem exceeds the fixed scratch of tpl_a2b_forward_f32_noalloc */
@@ -100,6 +100,19 @@ int tpl_a2b_forward_f32(const float *angles, const int32_t *lengths, float *coor
 int tpl_a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles,
                          const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch, int max_len,
                          const tpl_options *opt, void *stream);
+
+/* Angles2Backbone backward, batched FP32, from the forward's output coordinates.
+ * Also replaces Angles2BackboneGPU_backward (angles2backbone_interface.cpp:27-56); the
+ * reference's backward reads the forward's saved transforms `A`, whose translations
+ * are these coordinates.  Same result as tpl_a2b_backward_f32 without recomputing
+ * the chain: coords must be the unmodified output of tpl_a2b_forward_f32 for the
+ * same angles and lengths.  It reads 36 B of coordinates per residue instead of
+ * 12 B of angles and does a fraction of the arithmetic.  The workspace only needs
+ * its status word (>= 64 bytes, zeroed once).  opt->residues_per_thread: 4 (default)
+ * or 8 residues per lane. */
+int tpl_a2b_backward_coords_f32(float *grad_angles, const float *grad_coords, const float *coords,
+                                const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch,
+                                int max_len, const tpl_options *opt, void *stream);
 
 /* Angles2Backbone forward, plain FP64 form: one chain per CTA, one launch.
  * Same contract as tpl_a2b_forward_f32 in double precision; replaces

@@ -408,3 +408,85 @@ def test_sincos_error_bound(built):
     assert np.abs(sv - np.sin(xs)).max() <= 2.5e-7
     assert np.abs(cv - np.cos(xs)).max() <= 2.5e-7
     assert np.abs(sv * sv + cv * cv - 1.0).max() <= 3e-7
+
+
+def run_gpu_coords_backward(rm, ang, lengths, g, rpt):
+    """Forward with the current options, then the backward from its coordinates."""
+    dev = torch.device("cuda")
+    a = torch.tensor(ang, dtype=torch.float32, device=dev)
+    ln = torch.tensor(lengths, dtype=torch.int32, device=dev)
+    B, _, L = a.shape
+    ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+    coords = torch.full((B, 9 * L), float("nan"), device=dev)
+    rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
+    gi = torch.full((B, 3, L), float("nan"), device=dev)
+    rm.set_backward_options(rpt)
+    try:
+        rm.Angles2BackboneGPU_backward_coords(gi, torch.tensor(g, dtype=torch.float32, device=dev), coords, ln, ws)
+    finally:
+        rm.set_backward_options(0)
+    assert rm.workspace_status(ws) == 0
+    return coords.double().cpu().numpy(), gi.double().cpu().numpy()
+
+
+@pytest.mark.parametrize("rpt", [4, 8])
+@pytest.mark.parametrize("L", [1000, 1001, 258])
+def test_backward_from_coordinates_matches_oracle(rm, rpt, L):
+    """The float32 backward from the forward's output coordinates (bulk-copied chunk
+    rows when L % 4 == 0, plain loads otherwise) against the oracle."""
+    lens = [L, L - 1, 257, 256, 255, 129, 128, 127, 2, 1, 0]
+    ang, lengths, g = make_case(len(lens), L, 500 + L + rpt, lengths=lens)
+    c, gi = run_gpu_coords_backward(rm, ang, lengths, g, rpt)
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def test_backward_from_coordinates_ignores_padding(rm):
+    B, L = 4, 64
+    ang, lengths, g = make_case(B, L, 19, lengths=[64, 30, 1, 0])
+    for b, n in enumerate(lengths):
+        g[b, 9 * n:] = np.nan
+    c, gi = run_gpu_coords_backward(rm, ang, lengths, g, 4)
+    rc, rg = oracle_ref(ang, lengths, np.nan_to_num(g, nan=0.0), True)
+    assert np.isfinite(gi).all()
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def test_backward_from_coordinates_c_abi_and_layer(built):
+    """Through the C ABI (status-word workspace only) and through the autograd
+    layer, which saves its output coordinates for the backward; both agree with the
+    backward that recomputes the chain from the angles."""
+    from torchproteinlibrary_gb300 import capi
+    from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+    from torchproteinlibrary_gb300.ReducedModel.Angles2Backbone.Angles2Backbone import Angles2BackboneGPUFunction
+    lib = capi.lib()
+    dev = torch.device("cuda")
+    B, L = 12, 300
+    ang, lengths, g = make_case(B, L, 23)
+    lengths[0] = L
+    a = torch.tensor(ang, dtype=torch.float32, device=dev)
+    ln = torch.tensor(lengths, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    layer = Angles2Backbone()
+    grads = []
+    for from_coords in (True, False):
+        Angles2BackboneGPUFunction.backward_from_coords = from_coords
+        try:
+            x = a.clone().requires_grad_()
+            out = layer(x, ln)
+            out.backward(gt)
+            grads.append(x.grad.clone())
+        finally:
+            Angles2BackboneGPUFunction.backward_from_coords = True
+    scale = grads[1].abs().max().item()
+    assert (grads[0] - grads[1]).abs().max().item() <= GRAD_TOL_F32 * scale
+    # C ABI: 64-byte status workspace
+    ws = torch.zeros(64, dtype=torch.uint8, device=dev)
+    coords = layer(a, ln).detach().contiguous()
+    gi = torch.full((B, 3, L), float("nan"), device=dev)
+    capi.check(lib.tpl_a2b_backward_coords_f32(gi.data_ptr(), gt.data_ptr(), coords.data_ptr(), ln.data_ptr(),
+                                               ws.data_ptr(), 64, B, L, None, capi.stream_ptr()), "backward_coords")
+    torch.cuda.synchronize()
+    assert (gi - grads[1]).abs().max().item() <= GRAD_TOL_F32 * scale
+    assert lib.tpl_a2b_backward_coords_f32(gi.data_ptr(), gt.data_ptr(), coords.data_ptr(), ln.data_ptr(),
+                                           ws.data_ptr(), 16, B, L, None, capi.stream_ptr()) == -2

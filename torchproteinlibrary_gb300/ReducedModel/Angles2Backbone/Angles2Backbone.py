@@ -16,6 +16,10 @@ Differences from the reference:
     variable TPL_CHECK_NAN=1; it also reads back device-detected errors.
   * dL/domega of each chain's last residue is 0 (the reference reads one matrix
     past the chain there).
+  * The float32 backward works from the coordinates the forward returned (saved
+    for backward, as the reference saves its frame buffer ``A``), so it does not
+    walk the chain again.  Set ``Angles2BackboneGPUFunction.backward_from_coords``
+    to False to recompute from the angles instead.
 """
 import math
 import os
@@ -45,6 +49,8 @@ def new_workspace(batch, max_len, device):
 class Angles2BackboneGPUFunction(Function):
     """Backbone angles -> backbone coordinates (CUDA, float32 or float64)."""
 
+    backward_from_coords = True
+
     @staticmethod
     def forward(ctx, input_angles, angles_length):
         if input_angles.dim() != 3:
@@ -55,16 +61,21 @@ class Angles2BackboneGPUFunction(Function):
         ctx.A = new_workspace(batch_size, max_len, input_angles.device)
         _ReducedModel.Angles2BackboneGPU_forward(input_angles, coords, angles_length, ctx.A)
         _check_nan(coords, ctx.A, "forward")
-        ctx.save_for_backward(input_angles, angles_length)
+        ctx.from_coords = (Angles2BackboneGPUFunction.backward_from_coords and
+                           input_angles.dtype == torch.float32)
+        ctx.save_for_backward(input_angles, angles_length, coords if ctx.from_coords else None)
         return coords
 
     @staticmethod
     def backward(ctx, gradOutput):
-        input_angles, angles_length = ctx.saved_tensors
+        input_angles, angles_length, coords = ctx.saved_tensors
         gradOutput = gradOutput.contiguous()
         gradInput = torch.empty_like(input_angles)
-        _ReducedModel.Angles2BackboneGPU_backward(gradInput, gradOutput, input_angles, angles_length, ctx.A,
-                                                  gradInput.new_empty(0))
+        if ctx.from_coords:
+            _ReducedModel.Angles2BackboneGPU_backward_coords(gradInput, gradOutput, coords, angles_length, ctx.A)
+        else:
+            _ReducedModel.Angles2BackboneGPU_backward(gradInput, gradOutput, input_angles, angles_length, ctx.A,
+                                                      gradInput.new_empty(0))
         _check_nan(gradInput, ctx.A, "backward")
         return gradInput, None
 

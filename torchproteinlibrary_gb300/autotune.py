@@ -1,8 +1,10 @@
 """Autotuner for the Angles2Backbone FP32 kernels.
 
 Knobs (tpl_options): residues per thread R (the scan tile is 32 R residues for
-warp tiles, 128 R for CTA tiles), the tile scheme (warp-granular or CTA), and
-the length from which inter-tile carries are composed in FP64.  For a shape
+warp tiles, 128 R for CTA tiles, a 32 R-residue chunk for one warp per chain),
+the scan scheme (warp tiles, CTA tiles, one warp per chain), the length from
+which inter-tile carries are composed in FP64, and the residues per lane of the
+backward from coordinates.  For a shape
 (batch, max_len) the tuner times forward+backward of every candidate on
 synthetic chains of that shape with CUDA events and keeps the fastest whose
 coordinates stay within the accuracy bound of the FP64 form.  Results are
@@ -112,21 +114,62 @@ def sweep(ang, lengths, up, candidates=CANDIDATES, carry_thresholds=(0,), steps=
     return out
 
 
+COORDS_BWD_CANDIDATES = (4, 8)  # residues per lane of the backward from coordinates
+
+
+def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, steps=5):
+    """Time the float32 backward from the forward's coordinates for each residues-per-lane
+    value (the forward runs once with the current options); returns a list of dicts
+    with the gradient error against the FP64 form."""
+    rm = load_extension("_ReducedModel")
+    saved = rm.get_backward_options()
+    B, _, L = ang.shape
+    ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=ang.device)
+    coords = torch.empty(B, 9 * L, device=ang.device)
+    rm.Angles2BackboneGPU_forward(ang, coords, lengths, ws)
+    gang = torch.empty(B, 3, L, device=ang.device)
+    out = []
+    try:
+        for c in candidates:
+            rm.set_backward_options(c)
+            for _ in range(2):
+                rm.Angles2BackboneGPU_backward_coords(gang, up, coords, lengths, ws)
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record()
+            for _ in range(steps):
+                rm.Angles2BackboneGPU_backward_coords(gang, up, coords, lengths, ws)
+            e[1].record()
+            torch.cuda.synchronize(ang.device)
+            _, _, grel = _errors(rm, ang, lengths, up, coords, gang)
+            out.append({"residues_per_thread": c, "bwd_ms": e[0].elapsed_time(e[1]) / steps, "grad_max_rel": grel})
+    finally:
+        rm.set_backward_options(saved)
+    return out
+
+
 def tune(ang, lengths, up, use_cache=True, steps=5):
-    """Pick and install the fastest candidate within COORD_BOUND for this shape."""
+    """Pick and install, for this shape, the fastest forward candidate whose
+    coordinates stay within COORD_BOUND, and the fastest backward from coordinates
+    (what the float32 layer runs).  The returned dict describes the forward choice
+    and carries the backward's under "backward_coords"."""
     rm = load_extension("_ReducedModel")
     key = f"{torch.cuda.get_device_name(ang.device)}|{_bucket(ang.shape[0], ang.shape[2])}"
     cache = _load_cache() if use_cache else {}
-    rows = []
-    if key in cache:
+    rows, brows = [], []
+    if key in cache and "backward_coords" in cache[key]:
         best = cache[key]
     else:
         rows = sweep(ang, lengths, up, steps=steps)
         ok = [r for r in rows if r["coord_max_A"] <= COORD_BOUND] or rows
-        best = min(ok, key=lambda r: r["fwd_ms"] + r["bwd_ms"])
+        best = dict(min(ok, key=lambda r: r["fwd_ms"]))
+        rm.set_options(best["residues_per_thread"], best["fp64_carry_min_len"], 0, 0, best["threads_per_cta"])
+        brows = sweep_backward_coords(ang, lengths, up, steps=steps)
+        best["backward_coords"] = min(brows, key=lambda r: r["bwd_ms"])
         cache[key] = best
         if use_cache:
             _save_cache(cache)
     rm.set_options(best["residues_per_thread"], best["fp64_carry_min_len"], 0, 0, best["threads_per_cta"])
+    rm.set_backward_options(best["backward_coords"]["residues_per_thread"])
     tune.last_sweep = rows
+    tune.last_backward_sweep = brows
     return best

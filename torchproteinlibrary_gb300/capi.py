@@ -31,6 +31,7 @@ _SIGNATURES = {
     "tpl_workspace_status": (_i, [_vp, _vp, ctypes.POINTER(_i)]),
     "tpl_a2b_forward_f32": (_i, [_vp, _vp, _vp, _vp, _sz, _i, _i, _vp, _vp]),
     "tpl_a2b_backward_f32": (_i, [_vp, _vp, _vp, _vp, _vp, _sz, _i, _i, _vp, _vp]),
+    "tpl_a2b_backward_coords_f32": (_i, [_vp, _vp, _vp, _vp, _vp, _sz, _i, _i, _vp, _vp]),
     "tpl_a2b_forward_f64": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
     "tpl_a2b_backward_f64": (_i, [_vp, _vp, _vp, _vp, _vp, _sz, _i, _i, _vp]),
     "tpl_num_atoms": (_i, [ctypes.c_char_p]),

@@ -97,6 +97,41 @@ void Angles2BackboneGPU_backward(torch::Tensor gradInput, torch::Tensor gradOutp
     check_status(s, "Angles2BackboneGPU_backward");
 }
 
+// Backward of the FP32 path from the forward's output coordinates (no re-walk).
+// Not a reference entry point: the Python layer calls it with the coordinates it
+// saved; Angles2BackboneGPU_backward above keeps the reference's signature.
+int g_bwd_rpt = 0;  // residues per lane of the coordinate backward: 0 (= 4), 4 or 8
+
+void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor gradOutput, torch::Tensor output_coords,
+                                        torch::Tensor angles_length, torch::Tensor A) {
+    check_cuda(gradInput, "gradInput");
+    check_cuda(gradOutput, "gradOutput");
+    check_cuda(output_coords, "output_coords");
+    check_cuda(angles_length, "angles_length");
+    check_cuda(A, "A");
+    TORCH_CHECK(gradInput.dim() == 3 && gradInput.size(1) == 3, "gradInput must be [batch, 3, max_len]");
+    TORCH_CHECK(angles_length.scalar_type() == torch::kInt, "angles_length must be int32");
+    TORCH_CHECK(gradInput.scalar_type() == torch::kFloat && gradOutput.scalar_type() == torch::kFloat &&
+                    output_coords.scalar_type() == torch::kFloat,
+                "the coordinate backward is float32");
+    const int64_t B = gradInput.size(0), L = gradInput.size(2);
+    TORCH_CHECK(gradOutput.numel() == B * 9 * L && output_coords.numel() == B * 9 * L,
+                "gradOutput and output_coords must hold batch * 9 * max_len values");
+    const at::cuda::CUDAGuard guard(gradInput.device());
+    tpl_options o = g_opt;
+    o.residues_per_thread = g_bwd_rpt;
+    const int s = tpl_a2b_backward_coords_f32(gradInput.data_ptr<float>(), gradOutput.data_ptr<float>(),
+                                              output_coords.data_ptr<float>(), angles_length.data_ptr<int32_t>(),
+                                              A.data_ptr(), A.nbytes(), (int)B, (int)L, &o, stream_of(gradInput));
+    check_status(s, "Angles2BackboneGPU_backward_coords");
+}
+
+void set_backward_options(int64_t residues_per_thread) {
+    TORCH_CHECK(residues_per_thread == 0 || residues_per_thread == 4 || residues_per_thread == 8,
+                "residues_per_thread of the coordinate backward must be 0, 4 or 8");
+    g_bwd_rpt = (int)residues_per_thread;
+}
+
 void no_cpu_path(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
     TORCH_CHECK(false, "Angles2Backbone: this build has no CPU path; move the tensors to a CUDA device");
 }
@@ -147,4 +182,9 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
           py::arg("fp64_carry_min_len") = 0, py::arg("renormalize") = 0, py::arg("max_ctas") = 0,
           py::arg("threads_per_cta") = 0);
     m.def("get_options", &get_options, "current tuning knobs");
+    m.def("Angles2BackboneGPU_backward_coords", &Angles2BackboneGPU_backward_coords,
+          "float32 backward from the forward's output coordinates");
+    m.def("set_backward_options", &set_backward_options, "residues per lane of the coordinate backward",
+          py::arg("residues_per_thread") = 0);
+    m.def("get_backward_options", []() { return (int64_t)g_bwd_rpt; }, "residues per lane of the coordinate backward");
 }

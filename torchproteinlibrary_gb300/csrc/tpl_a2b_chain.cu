@@ -530,6 +530,285 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, bwd_min_blocks(C)) a2b_bwd_
     }
 }
 
+// ------------------------------------------------- backward from the coordinates
+// The forward's output already holds every atom position, so this backward reads
+// them instead of re-walking the chain: per chunk (last to first) a warp stages
+// the chunk's coordinates and dL/dx (two bulk copies into shared memory when the
+// rows are 16-byte aligned), and evaluates
+//     dL/dtheta_m = u_m . (S_m - x_m x G_m),  G_m = sum_{i>m} g_i,  S_m = sum_{i>m} x_i x g_i,
+// with u_m the unit bond vector into the rotated joint, as a lane pass (lane
+// sums), a warp suffix scan and a reverse pass over each lane's residues.
+// Positions are taken relative to the chunk's first N atom to keep the sums small.
+
+constexpr unsigned kWaitPolls = 1u << 22;  // bounded mbarrier wait (~0.5 s with back-off)
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_load_pair(float *dx, const float *sx, float *dg, const float *sg, unsigned bytes,
+                                               uint64_t *bar) {
+    // the buffers were last read through the generic proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(2 * bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dx)),
+                 "l"(sx), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dg)),
+                 "l"(sg), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+// Wait for the phase with the given parity to complete; false after kWaitPolls polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    for (unsigned i = 0; i < kWaitPolls; i++) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (i >= 8) __nanosleep(100);
+    }
+    return false;
+}
+
+// Floats 4q..4q+3 of a lane's staged segment, fetched the first time residue r
+// (descending or ascending order alike) needs them.
+template <int C>
+__device__ __forceinline__ void fetch_residue(const float *seg, float *buf, int r, bool first) {
+#pragma unroll
+    for (int q = (9 * r) / 4; q <= (9 * r + 8) / 4; q++)
+        if (first || q < (9 * (r + 1)) / 4) {
+            const float4 v = reinterpret_cast<const float4 *>(seg)[q];
+            buf[4 * q] = v.x; buf[4 * q + 1] = v.y; buf[4 * q + 2] = v.z; buf[4 * q + 3] = v.w;
+        }
+}
+
+template <int C>
+__global__ void __launch_bounds__(32 * kWarpsPerCta, C >= 8 ? 3 : 5) a2b_bwd_coords_kernel(ChainArgs a) {
+    constexpr int CH = 32 * C, SEG = 9 * C;
+    extern __shared__ __align__(16) float s_dyn[];
+    __shared__ __align__(8) uint64_t s_bar[kWarpsPerCta];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarpsPerCta + w;
+    if (b >= a.B) return;  // warps are independent
+    float *sx = s_dyn + w * 64 * SEG;  // coordinates of the chunk, contiguous as in the row
+    float *sg = sx + 32 * SEG;         // dL/dx of the chunk
+    const float *xs = sx + lane * SEG, *gs = sg + lane * SEG;
+    uint64_t *bar = &s_bar[w];
+    const bool vec = a.vec != 0;
+    if (vec && lane == 0) mbar_init(bar);
+    __syncwarp();
+    const int len = checked_length(a, b, lane);
+    const float *xin = a.coords + (size_t)b * 9 * a.L;
+    const float *gin = a.grad_coords + (size_t)b * 9 * a.L;
+    float *gout = a.grad_angles + (size_t)b * 3 * a.L;
+    const float inv_d0 = 1.f / a.bc.d[0], inv_d1 = 1.f / a.bc.d[1], inv_d2 = 1.f / a.bc.d[2];
+
+    const int nchunk = (len + CH - 1) / CH;
+    const int s_end = min(a.L, nchunk * CH);
+    for (int k = 0; k < 3; k++) zero_floats(gout + (size_t)k * a.L + s_end, a.L - s_end, lane, vec && (s_end % 4 == 0));
+
+    float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, oc[3] = {0.f, 0.f, 0.f};  // sums after the chunk
+    float nN[3] = {0.f, 0.f, 0.f};  // N of the first residue after the chunk (world)
+    unsigned phase = 0;
+    for (int k = nchunk - 1; k >= 0; k--) {
+        const int s0 = k * CH;
+        const int nreal = min(CH, len - s0);
+        __syncwarp();  // the previous chunk's reads of both buffers are done
+        if (vec) {
+            // whole residues up to a multiple of 4 (inside the row since L % 4 == 0)
+            const unsigned bytes = 36u * (unsigned)((nreal + 3) & ~3);
+            if (lane == 0) bulk_load_pair(sx, xin + (size_t)9 * s0, sg, gin + (size_t)9 * s0, bytes, bar);
+            const bool ok = mbar_wait(bar, phase);
+            phase ^= 1u;
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) record_error(a.hdr, TPL_ERR_LOOKBACK_TIMEOUT);
+                (void)mbar_wait(bar, phase ^ 1u);  // bounded: let the copies in flight land before exiting
+                return;
+            }
+        } else {
+            stage_chunk<SEG, SEG>(sx, xin + (size_t)9 * s0, 9 * nreal, lane, false);
+            stage_chunk<SEG, SEG>(sg, gin + (size_t)9 * s0, 9 * nreal, lane, false);
+            __syncwarp();
+        }
+        const int j0 = s0 + C * lane;
+        const float o[3] = {sx[0], sx[1], sx[2]};  // chunk origin: its first N atom
+        {
+            const float d[3] = {oc[0] - o[0], oc[1] - o[1], oc[2] - o[2]};
+            float dx[3];
+            cross3(d, Gc, dx);
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                Sc[i] += dx[i];
+                oc[i] = o[i];
+            }
+        }
+        // lane sums about o over the lane's residues below len
+        float Gl[3] = {0.f, 0.f, 0.f}, Sl[3] = {0.f, 0.f, 0.f};
+        {
+            float xb[9 * C], gb[9 * C];
+#pragma unroll
+            for (int r = 0; r < C; r++) {
+#pragma unroll
+                for (int q = (9 * r) / 4; q <= (9 * r + 8) / 4; q++)
+                    if (r == 0 || q > (9 * r - 1) / 4) {  // not fetched for residue r - 1
+                        const float4 xv = reinterpret_cast<const float4 *>(xs)[q];
+                        const float4 gv = reinterpret_cast<const float4 *>(gs)[q];
+                        xb[4 * q] = xv.x; xb[4 * q + 1] = xv.y; xb[4 * q + 2] = xv.z; xb[4 * q + 3] = xv.w;
+                        gb[4 * q] = gv.x; gb[4 * q + 1] = gv.y; gb[4 * q + 2] = gv.z; gb[4 * q + 3] = gv.w;
+                    }
+                if (j0 + r < len) {
+#pragma unroll
+                    for (int at = 0; at < 3; at++) {
+                        const float *x = xb + 9 * r + 3 * at, *g = gb + 9 * r + 3 * at;
+                        const float xr[3] = {x[0] - o[0], x[1] - o[1], x[2] - o[2]};
+                        float xg[3];
+                        cross3(xr, g, xg);
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            Gl[c] += g[c];
+                            Sl[c] += xg[c];
+                        }
+                    }
+                }
+            }
+        }
+        float G[3], S[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            float tg, ts;
+            G[i] = warp_suffix_excl(Gl[i], lane, tg) + Gc[i];
+            S[i] = warp_suffix_excl(Sl[i], lane, ts) + Sc[i];
+            Gc[i] += tg;
+            Sc[i] += ts;
+        }
+        // N after the lane's last residue: the next lane's first N, or the next chunk's
+        float nxt[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float mine = xs[c];
+            const float nb = __shfl_down_sync(0xffffffffu, mine, 1);
+            const float first = __shfl_sync(0xffffffffu, mine, 0);
+            nxt[c] = (lane == 31 ? nN[c] : nb) - o[c];
+            nN[c] = first;
+        }
+        // backwards over the lane's residues, positions relative to o
+        float gph[C], gps[C], gom[C];
+        {
+            float xb[9 * C], gb[9 * C];
+#pragma unroll
+            for (int r = C - 1; r >= 0; r--) {
+#pragma unroll
+                for (int q = (9 * r) / 4; q <= (9 * r + 8) / 4; q++)
+                    if (r == C - 1 || q < (9 * (r + 1)) / 4) {  // not fetched for residue r + 1
+                        const float4 xv = reinterpret_cast<const float4 *>(xs)[q];
+                        const float4 gv = reinterpret_cast<const float4 *>(gs)[q];
+                        xb[4 * q] = xv.x; xb[4 * q + 1] = xv.y; xb[4 * q + 2] = xv.z; xb[4 * q + 3] = xv.w;
+                        gb[4 * q] = gv.x; gb[4 * q + 1] = gv.y; gb[4 * q + 2] = gv.z; gb[4 * q + 3] = gv.w;
+                    }
+                const int j = j0 + r;
+                float xN[3], xA[3], xC[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    xN[c] = xb[9 * r + c] - o[c];
+                    xA[c] = xb[9 * r + 3 + c] - o[c];
+                    xC[c] = xb[9 * r + 6 + c] - o[c];
+                }
+                const float *gN = gb + 9 * r, *gA = gb + 9 * r + 3, *gC = gb + 9 * r + 6;
+                float u[3], tmp[3], cr[3];
+                // omega_j: axis C -> N_{j+1}, through N_{j+1}; moves the atoms after C_j
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (nxt[c] - xC[c]) * inv_d2;
+                cross3(nxt, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gom[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                // psi_j: axis CA -> C, through C; same atoms
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xC[c] - xA[c]) * inv_d1;
+                cross3(xC, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gps[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                const bool in = j < len;
+                if (in) {
+                    cross3(xC, gC, cr);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += gC[c];
+                        S[c] += cr[c];
+                    }
+                }
+                // phi_j: axis N -> CA, through CA; moves C_j and everything after
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xA[c] - xN[c]) * inv_d0;
+                cross3(xA, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gph[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                if (in) {
+                    cross3(xA, gA, cr);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += gA[c];
+                        S[c] += cr[c];
+                    }
+                    cross3(xN, gN, cr);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += gN[c];
+                        S[c] += cr[c];
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++) nxt[c] = xN[c];
+            }
+        }
+        // zeros at and past len (stale or padding positions are never stored);
+        // psi and omega of the last residue move nothing
+#pragma unroll
+        for (int r = 0; r < C; r++) {
+            const int j = j0 + r;
+            const bool ok = j < len, last = j == len - 1;
+            gph[r] = ok ? gph[r] : 0.f;
+            gps[r] = ok && !last ? gps[r] : 0.f;
+            gom[r] = ok && !last ? gom[r] : 0.f;
+        }
+        if (vec) {
+#pragma unroll
+            for (int i = 0; i < C / 4; i++) {
+                const int j = j0 + 4 * i;
+                if (j < a.L) {
+                    __stcs(reinterpret_cast<float4 *>(gout + j),
+                           make_float4(gph[4 * i], gph[4 * i + 1], gph[4 * i + 2], gph[4 * i + 3]));
+                    __stcs(reinterpret_cast<float4 *>(gout + a.L + j),
+                           make_float4(gps[4 * i], gps[4 * i + 1], gps[4 * i + 2], gps[4 * i + 3]));
+                    __stcs(reinterpret_cast<float4 *>(gout + 2 * a.L + j),
+                           make_float4(gom[4 * i], gom[4 * i + 1], gom[4 * i + 2], gom[4 * i + 3]));
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < C; r++) {
+                const int j = j0 + r;
+                if (j < a.L) {
+                    gout[j] = gph[r];
+                    gout[a.L + j] = gps[r];
+                    gout[2 * a.L + j] = gom[r];
+                }
+            }
+        }
+    }
+}
+
 // Sincos check kernel for the tests: s[i], c[i] = sincos_poly(a[i]).
 __global__ void sincos_poly_kernel(const float *a, float *s, float *c, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -599,6 +878,24 @@ int a2b_backward_chain(float *grad_angles, const float *grad_coords, const float
     switch (C) {
         case 4: return launch_chain(a2b_bwd_chain_kernel<4>, bwd_smem<4>(), B, a, st);
         case 8: return launch_chain(a2b_bwd_chain_kernel<8>, bwd_smem<8>(), B, a, st);
+    }
+    return TPL_ERR_UNSUPPORTED;
+}
+
+int a2b_backward_coords(float *grad_angles, const float *grad_coords, const float *coords, const int32_t *lengths,
+                        void *ws, int B, int L, const tpl_options &opt, cudaStream_t st) {
+    if (B == 0 || L == 0) return TPL_OK;
+    ChainArgs a = chain_args(nullptr, lengths, ws, B, L, opt);
+    a.coords = const_cast<float *>(coords);  // read only
+    a.grad_angles = grad_angles;
+    a.grad_coords = grad_coords;
+    a.vec = (L % 4 == 0) && aligned16(coords) && aligned16(grad_angles) && aligned16(grad_coords);
+    const int C = opt.residues_per_thread > 0 ? opt.residues_per_thread : 4;
+    constexpr int smem4 = kWarpsPerCta * 64 * 36 * (int)sizeof(float);
+    constexpr int smem8 = kWarpsPerCta * 64 * 72 * (int)sizeof(float);
+    switch (C) {
+        case 4: return launch_chain(a2b_bwd_coords_kernel<4>, smem4, B, a, st);
+        case 8: return launch_chain(a2b_bwd_coords_kernel<8>, smem8, B, a, st);
     }
     return TPL_ERR_UNSUPPORTED;
 }

@@ -116,7 +116,7 @@ const char *tpl_status_string(int status) {
         case TPL_ERR_LAUNCH: return "CUDA kernel launch failed";
         case TPL_ERR_LENGTH: return "chain length outside [0, max_len]";
         case TPL_ERR_SEQUENCE: return "unknown residue letter";
-        case TPL_ERR_LOOKBACK_TIMEOUT: return "inter-tile look-back wait timed out";
+        case TPL_ERR_LOOKBACK_TIMEOUT: return "a bounded device wait timed out (inter-tile look-back or bulk copy)";
         case TPL_ERR_ATOMS: return "chain has more atoms than max_atoms";
         case TPL_ERR_UNSUPPORTED: return "unsupported option combination";
         case TPL_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
@@ -181,6 +181,21 @@ int tpl_a2b_backward_f32(float *grad_angles, const float *grad_coords, const flo
     if (s) return s;
     return a2b_backward_f32(grad_angles, grad_coords, angles, lengths, workspace, batch, max_len, o,
                             (cudaStream_t)stream);
+}
+
+int tpl_a2b_backward_coords_f32(float *grad_angles, const float *grad_coords, const float *coords,
+                                const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch,
+                                int max_len, const tpl_options *opt, void *stream) {
+    if (batch < 0 || max_len < 0) return TPL_ERR_ARGUMENT;
+    const tpl_options o = resolve(opt);
+    if (!(o.residues_per_thread == 0 || o.residues_per_thread == 4 || o.residues_per_thread == 8))
+        return TPL_ERR_ARGUMENT;
+    if (batch == 0 || max_len == 0) return TPL_OK;
+    if (!grad_angles || !grad_coords || !coords || !lengths) return TPL_ERR_ARGUMENT;
+    int s = check_ws(workspace, workspace_bytes, sizeof(WsHeader));
+    if (s) return s;
+    return a2b_backward_coords(grad_angles, grad_coords, coords, lengths, workspace, batch, max_len, o,
+                               (cudaStream_t)stream);
 }
 
 int tpl_a2b_forward_f64(const double *angles, const int32_t *lengths, double *coords, int batch, int max_len,

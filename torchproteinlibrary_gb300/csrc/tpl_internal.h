@@ -69,6 +69,9 @@ int a2b_forward_chain(const float *angles, const int32_t *lengths, float *coords
 int a2b_backward_chain(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
                        void *ws, int B, int L, const tpl_options &opt, cudaStream_t st);
 int a2b_chain_record_stride();
+// Backward from the forward's output coordinates (no re-walk; tpl_a2b_chain.cu).
+int a2b_backward_coords(float *grad_angles, const float *grad_coords, const float *coords, const int32_t *lengths,
+                        void *ws, int B, int L, const tpl_options &opt, cudaStream_t st);
 int sincos_poly_f32(const float *a, float *s, float *c, int n, cudaStream_t st);
 size_t a2b_ws(int B, int L, const tpl_options &o);  // workspace bytes of the FP32 Angles2Backbone entries
 tpl_options resolve(const tpl_options *opt);
