@@ -62,12 +62,9 @@ __device__ __forceinline__ void record_error(WsHeader *h, int code) { atomicCAS(
 // sin and cos without tables or special-function units: Cody-Waite reduction by
 // pi/2 (two-term split of pi/2, exact products in the FMA) to |r| <= pi/4, then the
 // Taylor series of sin to r^9 and of cos to r^10 (truncation below 2e-9 on that
-// range), and the quadrant's swap and signs.  |a| > 1e4 and NaN take sincosf.
-__device__ __forceinline__ void sincos_poly(float a, float *s, float *c) {
-    if (!(fabsf(a) <= 1.0e4f)) {
-        sincosf(a, s, c);
-        return;
-    }
+// range), and the quadrant's swap and signs.  Valid for |a| <= 1e4; NaN and
+// infinities give NaN.  Callers send larger arguments to sincosf.
+__device__ __forceinline__ void sincos_fast(float a, float *s, float *c) {
     constexpr float kTwoOverPi = 0.636619772367581343f;
     constexpr float kPio2Hi = 1.57079637050628662f;      // float(pi / 2)
     constexpr float kPio2Lo = -4.37113900018624283e-8f;  // pi / 2 - kPio2Hi
@@ -92,6 +89,14 @@ __device__ __forceinline__ void sincos_poly(float a, float *s, float *c) {
     if ((q + 1) & 2) cc = -cc;
     *s = ss;
     *c = cc;
+}
+
+__device__ __forceinline__ void sincos_poly(float a, float *s, float *c) {
+    if (fabsf(a) > 1.0e4f) {
+        sincosf(a, s, c);
+        return;
+    }
+    sincos_fast(a, s, c);
 }
 
 __device__ __forceinline__ Frame<float> shfl_idx_frame(const Frame<float> &f, int src) {
@@ -142,16 +147,24 @@ __device__ __forceinline__ void load4(const float *row, int j, int len, bool vec
 }
 
 // Four residues of a lane's walk: composes their 12 joints onto f and writes the
-// lane-local N, CA, C positions (36 floats, 9 float4s) to seg.
+// lane-local N, CA, C positions (36 floats, 9 float4s) to seg.  FAST: every angle
+// is known to be within the range of sincos_fast.
+template <bool FAST>
 __device__ __forceinline__ void walk4(const BondConsts &bc, Frame<float> &f, const float (&a0)[4],
                                       const float (&a1)[4], const float (&a2)[4], float *seg) {
     float buf[36];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         float s0, c0, s1, c1, s2, c2;
-        sincos_poly(a0[r], &s0, &c0);
-        sincos_poly(a1[r], &s1, &c1);
-        sincos_poly(a2[r], &s2, &c2);
+        if (FAST) {
+            sincos_fast(a0[r], &s0, &c0);
+            sincos_fast(a1[r], &s1, &c1);
+            sincos_fast(a2[r], &s2, &c2);
+        } else {
+            sincos_poly(a0[r], &s0, &c0);
+            sincos_poly(a1[r], &s1, &c1);
+            sincos_poly(a2[r], &s2, &c2);
+        }
         buf[9 * r] = f.p[0]; buf[9 * r + 1] = f.p[1]; buf[9 * r + 2] = f.p[2];
         apply_joint(f, bc.cb[0], bc.sb[0], bc.d[0], c0, s0);
         buf[9 * r + 3] = f.p[0]; buf[9 * r + 4] = f.p[1]; buf[9 * r + 5] = f.p[2];
@@ -170,6 +183,12 @@ __device__ __forceinline__ void walk4(const BondConsts &bc, Frame<float> &f, con
 // positions (9C floats) go to seg.  Returns the lane transform.  Angles at and
 // past the chain end (and omega of its last residue) are taken as 0, so padding
 // values, NaN included, never enter a transform.
+// Rare path of walk_chunk: a group with an angle beyond the range of sincos_fast.
+__device__ __noinline__ void walk4_any(const BondConsts &bc, Frame<float> &f, const float (&a0)[4],
+                                       const float (&a1)[4], const float (&a2)[4], float *seg) {
+    walk4<false>(bc, f, a0, a1, a2, seg);
+}
+
 template <int C>
 __device__ __forceinline__ Frame<float> walk_chunk(const BondConsts &bc, const float *ang, int L, int j0, int len,
                                                    bool vec, float *seg) {
@@ -179,19 +198,33 @@ __device__ __forceinline__ Frame<float> walk_chunk(const BondConsts &bc, const f
     for (int g = 0; g < C / 4; g++) {
         const int j = j0 + 4 * g;
         float v0[4], v1[4], v2[4];
-        load4(ang, j, len, vec, v0);
-        load4(ang + L, j, len, vec, v1);
-        load4(ang + 2 * L, j, len - 1, vec, v2);  // omega of the last residue moves nothing: 0
-        walk4(bc, f, v0, v1, v2, seg + 36 * g);
+        if (vec && j + 4 < len) {  // whole group inside the chain, omega included
+            const float4 x0 = __ldg(reinterpret_cast<const float4 *>(ang + j));
+            const float4 x1 = __ldg(reinterpret_cast<const float4 *>(ang + L + j));
+            const float4 x2 = __ldg(reinterpret_cast<const float4 *>(ang + 2 * L + j));
+            v0[0] = x0.x; v0[1] = x0.y; v0[2] = x0.z; v0[3] = x0.w;
+            v1[0] = x1.x; v1[1] = x1.y; v1[2] = x1.z; v1[3] = x1.w;
+            v2[0] = x2.x; v2[1] = x2.y; v2[2] = x2.z; v2[3] = x2.w;
+        } else {
+            load4(ang, j, len, vec, v0);
+            load4(ang + L, j, len, vec, v1);
+            load4(ang + 2 * L, j, len - 1, vec, v2);  // omega of the last residue moves nothing: 0
+        }
+        // one range check per group (NaN passes: sincos_fast returns NaN for it)
+        float m = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; i++) m = fmaxf(m, fmaxf(fabsf(v0[i]), fmaxf(fabsf(v1[i]), fabsf(v2[i]))));
+        if (m <= 1.0e4f) walk4<true>(bc, f, v0, v1, v2, seg + 36 * g);
+        else walk4_any(bc, f, v0, v1, v2, seg + 36 * g);
     }
     return f;
 }
 
 // Map the 3C staged points of a lane through P in place; zeros for residues at or
 // past len.
-template <int C>
-__device__ __forceinline__ void map_positions(float *seg, const Frame<float> &P, int j0, int len) {
-#pragma unroll 1
+template <int C, bool MASK>
+__device__ __forceinline__ void map_points(float *seg, const Frame<float> &P, int nvalid) {
+#pragma unroll
     for (int g = 0; g < 3 * C / 4; g++) {
         float4 *q = reinterpret_cast<float4 *>(seg + 12 * g);
         const float4 v0 = q[0], v1 = q[1], v2 = q[2];
@@ -200,12 +233,18 @@ __device__ __forceinline__ void map_positions(float *seg, const Frame<float> &P,
 #pragma unroll
         for (int pt = 0; pt < 4; pt++) {
             frame_point(P, x[3 * pt], x[3 * pt + 1], x[3 * pt + 2], &y[3 * pt]);
-            if (j0 + (4 * g + pt) / 3 >= len) y[3 * pt] = y[3 * pt + 1] = y[3 * pt + 2] = 0.f;
+            if (MASK && (4 * g + pt) / 3 >= nvalid) y[3 * pt] = y[3 * pt + 1] = y[3 * pt + 2] = 0.f;
         }
         q[0] = make_float4(y[0], y[1], y[2], y[3]);
         q[1] = make_float4(y[4], y[5], y[6], y[7]);
         q[2] = make_float4(y[8], y[9], y[10], y[11]);
     }
+}
+
+template <int C>
+__device__ __forceinline__ void map_positions(float *seg, const Frame<float> &P, int j0, int len) {
+    if (j0 + C <= len) map_points<C, false>(seg, P, C);
+    else map_points<C, true>(seg, P, len - j0);
 }
 
 // Stage floats [0, 32 SEG) of a chunk: src[f] for f < nvalid, 0 after.  Lane l's
@@ -237,10 +276,19 @@ __device__ __forceinline__ void stage_chunk(float *stage, const float *src, int 
 template <int SEG, int SP>
 __device__ __forceinline__ void store_chunk(float *dst, const float *stage, int n, int lane, bool vec) {
     if (vec) {
+        // float4 q = lane + 32 i lives in lane segment sl at offset off: both are
+        // advanced by the constant step of 128 floats instead of divided out
+        constexpr int kStepSeg = 128 / SEG, kStepOff = 128 - kStepSeg * SEG;
+        int sl = (4 * lane) / SEG, off = 4 * lane - sl * SEG;
 #pragma unroll 2
         for (int q = lane; 4 * q < n; q += 32) {
-            const int f = 4 * q, sl = f / SEG;
-            __stcs(reinterpret_cast<float4 *>(dst) + q, *reinterpret_cast<const float4 *>(stage + sl * SP + f - sl * SEG));
+            __stcs(reinterpret_cast<float4 *>(dst) + q, *reinterpret_cast<const float4 *>(stage + sl * SP + off));
+            sl += kStepSeg;
+            off += kStepOff;
+            if (off >= SEG) {
+                off -= SEG;
+                sl += 1;
+            }
         }
     } else {
         for (int f = lane; f < n; f += 32) {
@@ -298,8 +346,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_
         const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg);
         Frame<float> tot;
         const Frame<float> E = warp_exclusive_total(t, lane, a.renorm, tot);
-        Frame<float> P = compose(F, E);
-        if (a.renorm) renormalize(P);
+        // E composes at most 31 renormalised lane transforms: P needs no renormalisation
+        const Frame<float> P = compose(F, E);
         if ((C * lane) % kRecordStride == 0 && j0 < len) {
             float *r = rec[j0 / kRecordStride].f;
 #pragma unroll
