@@ -218,9 +218,9 @@ def run_ours(args):
     else:
         tuned = autotune.tune(ang, lengths, up, use_cache=False)
         if not args.no_extras:
-            # FP64 inter-tile carry threshold sweep at the tuned tile shape (-1 = never FP64)
-            sweep_rows = autotune.sweep(ang, lengths, up,
-                                        candidates=[(tuned["residues_per_thread"], tuned["threads_per_cta"])],
+            # FP64 inter-tile carry threshold sweep (-1 = never FP64)
+            # (on warp tiles of 256 residues: the one-warp-per-chain scheme has no inter-tile carry)
+            sweep_rows = autotune.sweep(ang, lengths, up, candidates=[(8, 0)],
                                         carry_thresholds=(128, 256, 512, -1), steps=5)
             rm.set_options(tuned["residues_per_thread"], tuned["fp64_carry_min_len"], 0, 0,
                            tuned["threads_per_cta"])
