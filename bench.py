@@ -280,7 +280,7 @@ def run_ours(args):
     value = residues / (ms / 1e3)
 
     if args.no_extras:
-        check = plain = e2e = a2c = None
+        check = plain = e2e = a2c = train = None
     else:
         # correctness of this very run against the FP64 plain form on a slice
         check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
@@ -289,6 +289,7 @@ def run_ours(args):
         # e2e: public autograd layer, host (pinned) inputs in, results back to the host
         e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
         a2c = time_a2c(dev)
+        train = time_training_step(dev)
 
     peak, peak_kind = peaks()
     fwd_ms, bwd_ms = statistics.mean(t_f), statistics.mean(t_b)
@@ -327,6 +328,7 @@ def run_ours(args):
         "e2e": e2e,
         "plain_fp64": plain,
         "angles2coords": a2c,
+        "training_step": train,
         "accuracy_vs_fp64": check,
     }
     if rank == 0:
@@ -481,6 +483,60 @@ def time_a2c(dev, steps=10, seed=1004):
     res["grad_max_rel"] = float(ge)
     res["workload"] = "Angles2Coords fwd+bwd, 256 chains x U{50..500} random residues"
     res["bytes_per_residue_f32"] = 298
+    return res
+
+
+def time_training_step(dev, steps=10, seed=1004):
+    """The training step on its own workload: 256 chains of U{50..500} random
+    residues, angles ~ U[-pi, pi) with omega = pi, target = Angles2Coords(angles +
+    N(0, 0.3)); one step = Angles2Coords forward, Coords2RMSD (centred) forward, mean,
+    backward through both, all through the public autograd layers, inputs resident.
+    FP32 batched kernels vs FP64 kernels, with the FP32 gradient's error against FP64."""
+    import torch
+    from torchproteinlibrary_gb300.FullAtomModel import Angles2Coords
+    from torchproteinlibrary_gb300.RMSD import Coords2RMSD
+
+    g = np.random.default_rng(seed)
+    B = 256
+    lens = g.integers(50, 501, B)
+    aa = np.array(list("ACDEFGHIKLMNPQRSTVWY"))
+    seqs = ["".join(g.choice(aa, n)) for n in lens]
+    L = int(lens.max())
+    ang = g.uniform(-np.pi, np.pi, (B, 8, L))
+    ang[:, 2] = np.pi
+    noisy = ang + g.normal(0.0, 0.3, ang.shape)
+    res, grads = {}, {}
+    for name, dt in (("f32", torch.float32), ("f64", torch.float64)):
+        a2c, rmsd = Angles2Coords(), Coords2RMSD()
+        with torch.no_grad():
+            target, _, _, na = a2c(torch.tensor(noisy, dtype=dt, device=dev), seqs)
+        na = na.to(dev)
+        x = torch.tensor(ang, dtype=dt, device=dev, requires_grad=True)
+
+        def step():
+            x.grad = None
+            c, _, _, _ = a2c(x, seqs)
+            loss = rmsd(c, target, na).mean()
+            loss.backward()
+            return loss
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize(dev)
+        n = steps if name == "f32" else max(1, steps // 4)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            loss = step()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / n
+        res[name] = {"residues_per_s": float(lens.sum()) / (ms / 1e3), "ms_per_step": ms, "loss": float(loss)}
+        grads[name] = x.grad.double()
+    res["batched_vs_fp64"] = res["f32"]["residues_per_s"] / res["f64"]["residues_per_s"]
+    res["grad_max_rel_f32_vs_f64"] = float((grads["f32"] - grads["f64"]).abs().max() / grads["f64"].abs().max())
+    res["workload"] = ("training step: Angles2Coords + Coords2RMSD loss (mean) fwd+bwd, 256 chains x U{50..500} "
+                       "random residues, autograd layers, inputs resident")
     return res
 
 
