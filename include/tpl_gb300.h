@@ -195,6 +195,48 @@ int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const u
 int tpl_a2b_forward_f32_noalloc(const float *angles, const int32_t *lengths, float *coords, int batch, int max_len,
                                 const tpl_options *opt, void *stream);
 
+/* ---------------------------------------------------------------- CoordsTransform
+ * Batched coordinate rows [batch, 3 * atoms_stride] (xyz per atom); the first
+ * num_atoms[b] atoms of row b are transformed and the rest of the row is written
+ * as zeros (the reference fills zero-initialised outputs).  Counts past
+ * atoms_stride are clamped to it.  All entries launch on `stream` and return a
+ * tpl_status.  _f64 variants take double.
+ *
+ * Translate: out = in + translation[b] (translation [batch, 3]); with
+ * translation == NULL it is the masked copy that is the backward of
+ * CoordsTranslateGPU_forward/_backward (Layers/FullAtomModel/CoordsTransform/
+ * coordsTransformGPU_interface.cpp:8-56, kernels TransformCUDAKernels.cu:4-37). */
+int tpl_coords_translate_f32(const float *in, float *out, const float *translation, const int32_t *num_atoms,
+                             int batch, int atoms_stride, void *stream);
+int tpl_coords_translate_f64(const double *in, double *out, const double *translation, const int32_t *num_atoms,
+                             int batch, int atoms_stride, void *stream);
+/* Rotate: out = R[b] in (transpose = 0, CoordsRotateGPU_forward) or R[b]^T in
+ * (transpose = 1, CoordsRotateGPU_backward); rotation [batch, 3, 3] row-major.
+ * Replaces coordsTransformGPU_interface.cpp:58-110, TransformCUDAKernels.cu:40-75. */
+int tpl_coords_rotate_f32(const float *in, float *out, const float *rotation, int transpose,
+                          const int32_t *num_atoms, int batch, int atoms_stride, void *stream);
+int tpl_coords_rotate_f64(const double *in, double *out, const double *rotation, int transpose,
+                          const int32_t *num_atoms, int batch, int atoms_stride, void *stream);
+/* Centre: center[b] = mean of the first num_atoms[b] atoms (FP64 accumulation; 0 for
+ * an empty chain, where the reference divides by zero), and its backward
+ * grad_in[b, atom] = grad_center[b] / num_atoms[b].  Replaces Coords2CenterGPU_forward/
+ * _backward (coordsTransformGPU_interface.cpp:112-160, TransformCUDAKernels.cu:77-107). */
+int tpl_coords_center_f32(const float *in, float *center, const int32_t *num_atoms, int batch, int atoms_stride,
+                          void *stream);
+int tpl_coords_center_f64(const double *in, double *center, const int32_t *num_atoms, int batch, int atoms_stride,
+                          void *stream);
+int tpl_coords_center_backward_f32(const float *grad_center, float *grad_in, const int32_t *num_atoms, int batch,
+                                   int atoms_stride, void *stream);
+int tpl_coords_center_backward_f64(const double *grad_center, double *grad_in, const int32_t *num_atoms, int batch,
+                                   int atoms_stride, void *stream);
+/* Bounding box: lo[b] / hi[b] = per-coordinate min / max over the first
+ * num_atoms[b] atoms (+inf / -inf for an empty chain).  Replaces getBBox
+ * (coordsTransform_interface.cpp:175-200, Math/nUtil.cpp:27-57), which runs on the CPU. */
+int tpl_coords_bbox_f32(const float *in, float *lo, float *hi, const int32_t *num_atoms, int batch,
+                        int atoms_stride, void *stream);
+int tpl_coords_bbox_f64(const double *in, double *lo, double *hi, const int32_t *num_atoms, int batch,
+                        int atoms_stride, void *stream);
+
 /* Diagnostics (no counterpart in the reference): s[i], c[i] = sin, cos of a[i] as
  * the FP32 Angles2Backbone kernels evaluate them (Cody-Waite reduction by pi/2 and
  * Taylor series), for n device floats on `stream`. */

@@ -213,3 +213,78 @@ def rmsd(src: np.ndarray, dst: np.ndarray, num_atoms, center: bool = True):
             # Coords2RMSD.py:48-56: (x - UT y) / (rmsd N), UT applied as out = UT @ y
             grads[b, :3 * n] = ((x - y @ UT[b].T) / (out[b] * n)).reshape(-1)
     return out, UT, grads
+
+
+# -------------------------------------------------------------- CoordsTransform
+# Restatements of Layers/FullAtomModel/TransformCUDAKernels.cu:4-107 and
+# Math/nUtil.cpp:27-79 on [B, 3 * atoms_stride] rows; atoms past num_atoms[b] are 0.
+def coords_translate(x: np.ndarray, T, num_atoms) -> np.ndarray:
+    """out = x + T[b] for the first num_atoms[b] atoms (T None: the masked copy, the backward)."""
+    x = np.asarray(x)
+    out = np.zeros_like(x)
+    for b, n in enumerate(num_atoms):
+        n = int(min(max(n, 0), x.shape[1] // 3))
+        v = x[b, :3 * n].reshape(n, 3)
+        out[b, :3 * n] = (v + (0 if T is None else np.asarray(T)[b])).reshape(-1)
+    return out
+
+
+def coords_rotate(x: np.ndarray, R, num_atoms, transpose: bool = False) -> np.ndarray:
+    """out = R[b] x (transpose: R[b]^T x) per atom, mat33Vec3Mul of the reference."""
+    x = np.asarray(x)
+    out = np.zeros_like(x)
+    for b, n in enumerate(num_atoms):
+        n = int(min(max(n, 0), x.shape[1] // 3))
+        M = np.asarray(R)[b].T if transpose else np.asarray(R)[b]
+        out[b, :3 * n] = (x[b, :3 * n].reshape(n, 3) @ M.T).reshape(-1)
+    return out
+
+
+def coords_center(x: np.ndarray, num_atoms) -> np.ndarray:
+    """Mean of the first num_atoms[b] atoms (0 for an empty chain)."""
+    x = np.asarray(x)
+    out = np.zeros((x.shape[0], 3), dtype=x.dtype)
+    for b, n in enumerate(num_atoms):
+        n = int(min(max(n, 0), x.shape[1] // 3))
+        if n:
+            out[b] = x[b, :3 * n].reshape(n, 3).astype(np.float64).mean(0)
+    return out
+
+
+def coords_center_backward(grad_center, num_atoms, atoms_stride: int) -> np.ndarray:
+    g = np.asarray(grad_center)
+    out = np.zeros((g.shape[0], 3 * atoms_stride), dtype=g.dtype)
+    for b, n in enumerate(num_atoms):
+        n = int(min(max(n, 0), atoms_stride))
+        if n:
+            out[b, :3 * n] = np.tile(g[b] / n, n)
+    return out
+
+
+def coords_bbox(x: np.ndarray, num_atoms):
+    """Per-coordinate min / max of the first num_atoms[b] atoms (+inf / -inf when empty)."""
+    x = np.asarray(x)
+    lo = np.full((x.shape[0], 3), np.inf, dtype=x.dtype)
+    hi = np.full((x.shape[0], 3), -np.inf, dtype=x.dtype)
+    for b, n in enumerate(num_atoms):
+        n = int(min(max(n, 0), x.shape[1] // 3))
+        if n:
+            v = x[b, :3 * n].reshape(n, 3)
+            lo[b], hi[b] = v.min(0), v.max(0)
+    return lo, hi
+
+
+def rotation_from_u(u: np.ndarray) -> np.ndarray:
+    """Math/nUtil.cpp:60-79: rotation matrix of the quaternion built from u in [0,1)^3."""
+    u = np.asarray(u, dtype=np.float64)
+    out = np.zeros((u.shape[0], 3, 3))
+    for b, (u1, u2, u3) in enumerate(u):
+        q = [np.sqrt(1 - u1) * np.sin(2 * np.pi * u2), np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
+             np.sqrt(u1) * np.sin(2 * np.pi * u3), np.sqrt(u1) * np.cos(2 * np.pi * u3)]
+        out[b] = [[q[0] ** 2 + q[1] ** 2 - q[2] ** 2 - q[3] ** 2, 2 * (q[1] * q[2] - q[0] * q[3]),
+                   2 * (q[1] * q[3] + q[0] * q[2])],
+                  [2 * (q[1] * q[2] + q[0] * q[3]), q[0] ** 2 - q[1] ** 2 + q[2] ** 2 - q[3] ** 2,
+                   2 * (q[2] * q[3] - q[0] * q[1])],
+                  [2 * (q[1] * q[3] - q[0] * q[2]), 2 * (q[2] * q[3] + q[0] * q[1]),
+                   q[0] ** 2 - q[1] ** 2 - q[2] ** 2 + q[3] ** 2]]
+    return out

@@ -1,1 +1,2 @@
 from .Angles2Coords import Angles2Coords
+from .CoordsTransform import *

@@ -186,9 +186,167 @@ int64_t workspace_status(int64_t device) {
     return st;
 }
 
+// ------------------------------------------------------------- CoordsTransform
+// The reference's entry points (Layers/FullAtomModel/CoordsTransform/
+// coordsTransformGPU_interface.cpp, coordsTransform_interface.cpp), CUDA tensors
+// only; the CPU variants raise.  Coordinates [batch, 3 * atoms_stride], num_atoms
+// int32 [batch] on the same device.
+void check_coords(const torch::Tensor &x, const char *name) {
+    TORCH_CHECK(x.is_cuda(), name, " must be a CUDA tensor (this build has no CPU path)");
+    TORCH_CHECK(x.is_contiguous(), name, " must be contiguous");
+    TORCH_CHECK(x.scalar_type() == torch::kFloat || x.scalar_type() == torch::kDouble, name,
+                " must be float32 or float64");
+}
+void check_num_atoms(const torch::Tensor &na, const torch::Tensor &x) {
+    TORCH_CHECK(na.is_cuda() && na.device() == x.device(), "num_atoms must be on the coordinates' device");
+    TORCH_CHECK(na.scalar_type() == torch::kInt && na.is_contiguous() && na.numel() == x.size(0),
+                "num_atoms must be contiguous int32 [batch]");
+}
+void check_same(const torch::Tensor &a, const torch::Tensor &b, const char *name) {
+    TORCH_CHECK(a.is_cuda() && a.device() == b.device() && a.scalar_type() == b.scalar_type() && a.is_contiguous(),
+                name, " must be a contiguous CUDA tensor of the coordinates' dtype and device");
+}
+
+void coords_translate(torch::Tensor in, torch::Tensor out, torch::Tensor T, torch::Tensor num_atoms, bool with_T,
+                      const char *what) {
+    check_coords(in, "input");
+    TORCH_CHECK(in.dim() == 2 && in.size(1) % 3 == 0, what, ": coordinates must be [batch, 3 * atoms]");
+    check_same(out, in, "output");
+    TORCH_CHECK(out.sizes() == in.sizes(), what, ": output shape must match the input");
+    check_num_atoms(num_atoms, in);
+    if (with_T) {
+        check_same(T, in, "T");
+        TORCH_CHECK(T.numel() == in.size(0) * 3, what, ": T must be [batch, 3]");
+    }
+    const at::cuda::CUDAGuard guard(in.device());
+    const int B = (int)in.size(0), S = (int)(in.size(1) / 3);
+    int s;
+    if (in.scalar_type() == torch::kFloat)
+        s = tpl_coords_translate_f32(in.data_ptr<float>(), out.data_ptr<float>(), with_T ? T.data_ptr<float>() : nullptr,
+                                     num_atoms.data_ptr<int32_t>(), B, S, stream_of(in));
+    else
+        s = tpl_coords_translate_f64(in.data_ptr<double>(), out.data_ptr<double>(),
+                                     with_T ? T.data_ptr<double>() : nullptr, num_atoms.data_ptr<int32_t>(), B, S,
+                                     stream_of(in));
+    check_status(s, what);
+}
+void CoordsTranslateGPU_forward(torch::Tensor input_coords, torch::Tensor output_coords, torch::Tensor T,
+                                torch::Tensor num_atoms) {
+    coords_translate(input_coords, output_coords, T, num_atoms, true, "CoordsTranslateGPU_forward");
+}
+void CoordsTranslateGPU_backward(torch::Tensor grad_output_coords, torch::Tensor grad_input_coords, torch::Tensor T,
+                                 torch::Tensor num_atoms) {
+    coords_translate(grad_output_coords, grad_input_coords, T, num_atoms, false, "CoordsTranslateGPU_backward");
+}
+
+void coords_rotate(torch::Tensor in, torch::Tensor out, torch::Tensor R, torch::Tensor num_atoms, int transpose,
+                   const char *what) {
+    check_coords(in, "input");
+    TORCH_CHECK(in.dim() == 2 && in.size(1) % 3 == 0, what, ": coordinates must be [batch, 3 * atoms]");
+    check_same(out, in, "output");
+    TORCH_CHECK(out.sizes() == in.sizes(), what, ": output shape must match the input");
+    check_same(R, in, "R");
+    TORCH_CHECK(R.numel() == in.size(0) * 9, what, ": R must be [batch, 3, 3]");
+    check_num_atoms(num_atoms, in);
+    const at::cuda::CUDAGuard guard(in.device());
+    const int B = (int)in.size(0), S = (int)(in.size(1) / 3);
+    int s;
+    if (in.scalar_type() == torch::kFloat)
+        s = tpl_coords_rotate_f32(in.data_ptr<float>(), out.data_ptr<float>(), R.data_ptr<float>(), transpose,
+                                  num_atoms.data_ptr<int32_t>(), B, S, stream_of(in));
+    else
+        s = tpl_coords_rotate_f64(in.data_ptr<double>(), out.data_ptr<double>(), R.data_ptr<double>(), transpose,
+                                  num_atoms.data_ptr<int32_t>(), B, S, stream_of(in));
+    check_status(s, what);
+}
+void CoordsRotateGPU_forward(torch::Tensor input_coords, torch::Tensor output_coords, torch::Tensor R,
+                             torch::Tensor num_atoms) {
+    coords_rotate(input_coords, output_coords, R, num_atoms, 0, "CoordsRotateGPU_forward");
+}
+void CoordsRotateGPU_backward(torch::Tensor grad_output_coords, torch::Tensor grad_input_coords, torch::Tensor R,
+                              torch::Tensor num_atoms) {
+    coords_rotate(grad_output_coords, grad_input_coords, R, num_atoms, 1, "CoordsRotateGPU_backward");
+}
+
+void Coords2CenterGPU_forward(torch::Tensor input_coords, torch::Tensor output_T, torch::Tensor num_atoms) {
+    check_coords(input_coords, "input_coords");
+    TORCH_CHECK(input_coords.dim() == 2 && input_coords.size(1) % 3 == 0, "coordinates must be [batch, 3 * atoms]");
+    check_same(output_T, input_coords, "output_T");
+    TORCH_CHECK(output_T.numel() == input_coords.size(0) * 3, "output_T must be [batch, 3]");
+    check_num_atoms(num_atoms, input_coords);
+    const at::cuda::CUDAGuard guard(input_coords.device());
+    const int B = (int)input_coords.size(0), S = (int)(input_coords.size(1) / 3);
+    int s;
+    if (input_coords.scalar_type() == torch::kFloat)
+        s = tpl_coords_center_f32(input_coords.data_ptr<float>(), output_T.data_ptr<float>(),
+                                  num_atoms.data_ptr<int32_t>(), B, S, stream_of(input_coords));
+    else
+        s = tpl_coords_center_f64(input_coords.data_ptr<double>(), output_T.data_ptr<double>(),
+                                  num_atoms.data_ptr<int32_t>(), B, S, stream_of(input_coords));
+    check_status(s, "Coords2CenterGPU_forward");
+}
+void Coords2CenterGPU_backward(torch::Tensor grad_output_T, torch::Tensor grad_input_coords,
+                               torch::Tensor num_atoms) {
+    check_coords(grad_input_coords, "grad_input_coords");
+    TORCH_CHECK(grad_input_coords.dim() == 2 && grad_input_coords.size(1) % 3 == 0,
+                "gradients must be [batch, 3 * atoms]");
+    check_same(grad_output_T, grad_input_coords, "grad_output_T");
+    TORCH_CHECK(grad_output_T.numel() == grad_input_coords.size(0) * 3, "grad_output_T must be [batch, 3]");
+    check_num_atoms(num_atoms, grad_input_coords);
+    const at::cuda::CUDAGuard guard(grad_input_coords.device());
+    const int B = (int)grad_input_coords.size(0), S = (int)(grad_input_coords.size(1) / 3);
+    int s;
+    if (grad_input_coords.scalar_type() == torch::kFloat)
+        s = tpl_coords_center_backward_f32(grad_output_T.data_ptr<float>(), grad_input_coords.data_ptr<float>(),
+                                           num_atoms.data_ptr<int32_t>(), B, S, stream_of(grad_input_coords));
+    else
+        s = tpl_coords_center_backward_f64(grad_output_T.data_ptr<double>(), grad_input_coords.data_ptr<double>(),
+                                           num_atoms.data_ptr<int32_t>(), B, S, stream_of(grad_input_coords));
+    check_status(s, "Coords2CenterGPU_backward");
+}
+
+void getBBox(torch::Tensor input_coords, torch::Tensor a, torch::Tensor b, torch::Tensor num_atoms) {
+    check_coords(input_coords, "input_coords");
+    TORCH_CHECK(input_coords.dim() == 2 && input_coords.size(1) % 3 == 0, "coordinates must be [batch, 3 * atoms]");
+    check_same(a, input_coords, "a");
+    check_same(b, input_coords, "b");
+    TORCH_CHECK(a.numel() == input_coords.size(0) * 3 && b.numel() == a.numel(), "a and b must be [batch, 3]");
+    check_num_atoms(num_atoms, input_coords);
+    const at::cuda::CUDAGuard guard(input_coords.device());
+    const int B = (int)input_coords.size(0), S = (int)(input_coords.size(1) / 3);
+    int s;
+    if (input_coords.scalar_type() == torch::kFloat)
+        s = tpl_coords_bbox_f32(input_coords.data_ptr<float>(), a.data_ptr<float>(), b.data_ptr<float>(),
+                                num_atoms.data_ptr<int32_t>(), B, S, stream_of(input_coords));
+    else
+        s = tpl_coords_bbox_f64(input_coords.data_ptr<double>(), a.data_ptr<double>(), b.data_ptr<double>(),
+                                num_atoms.data_ptr<int32_t>(), B, S, stream_of(input_coords));
+    check_status(s, "getBBox");
+}
+
+void no_cpu_transform(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
+    TORCH_CHECK(false, "CoordsTransform: this build has no CPU path; move the tensors to a CUDA device");
+}
+void no_cpu_center(torch::Tensor, torch::Tensor, torch::Tensor) {
+    TORCH_CHECK(false, "Coords2Center: this build has no CPU path; move the tensors to a CUDA device");
+}
+
 }  // namespace
 
 PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
+    m.def("CoordsTranslateGPU_forward", &CoordsTranslateGPU_forward, "CoordsTranslate gpu forward");
+    m.def("CoordsTranslateGPU_backward", &CoordsTranslateGPU_backward, "CoordsTranslate gpu backward");
+    m.def("CoordsRotateGPU_forward", &CoordsRotateGPU_forward, "CoordsRotate gpu forward");
+    m.def("CoordsRotateGPU_backward", &CoordsRotateGPU_backward, "CoordsRotate gpu backward");
+    m.def("Coords2CenterGPU_forward", &Coords2CenterGPU_forward, "Coords2Center gpu forward");
+    m.def("Coords2CenterGPU_backward", &Coords2CenterGPU_backward, "Coords2Center gpu backward");
+    m.def("CoordsTranslate_forward", &no_cpu_transform, "not available: no CPU path");
+    m.def("CoordsTranslate_backward", &no_cpu_transform, "not available: no CPU path");
+    m.def("CoordsRotate_forward", &no_cpu_transform, "not available: no CPU path");
+    m.def("CoordsRotate_backward", &no_cpu_transform, "not available: no CPU path");
+    m.def("Coords2Center_forward", &no_cpu_center, "not available: no CPU path");
+    m.def("Coords2Center_backward", &no_cpu_center, "not available: no CPU path");
+    m.def("getBBox", &getBBox, "per-chain bounding box (GPU)");
     m.def("Angles2Coords_forward", &Angles2Coords_forward, "Angles2Coords forward");
     m.def("Angles2Coords_backward", &Angles2Coords_backward, "Angles2Coords backward");
     m.def("Angles2Coords_save", &Angles2Coords_save, "Angles2Coords save");

@@ -341,4 +341,47 @@ int tpl_rmsd_backward_f64(const double *grad_rmsd, const double *src, const doub
                            grad_src, stream);
 }
 
+// ------------------------------------------------------------- CoordsTransform
+#define TPL_TRANSFORM_ENTRIES(T, SFX)                                                                              \
+    int tpl_coords_translate_##SFX(const T *in, T *out, const T *translation, const int32_t *num_atoms, int batch, \
+                                   int atoms_stride, void *stream) {                                               \
+        if (batch < 0 || atoms_stride < 0) return TPL_ERR_ARGUMENT;                                                \
+        if (batch == 0 || atoms_stride == 0) return TPL_OK;                                                        \
+        if (!in || !out || !num_atoms) return TPL_ERR_ARGUMENT;                                                    \
+        return coords_shift<T>(in, out, translation, 0, num_atoms, batch, atoms_stride, (cudaStream_t)stream);     \
+    }                                                                                                              \
+    int tpl_coords_rotate_##SFX(const T *in, T *out, const T *rotation, int transpose, const int32_t *num_atoms,   \
+                                int batch, int atoms_stride, void *stream) {                                       \
+        if (batch < 0 || atoms_stride < 0) return TPL_ERR_ARGUMENT;                                                \
+        if (batch == 0 || atoms_stride == 0) return TPL_OK;                                                        \
+        if (!in || !out || !rotation || !num_atoms) return TPL_ERR_ARGUMENT;                                       \
+        return coords_rotate<T>(in, out, rotation, transpose, num_atoms, batch, atoms_stride, (cudaStream_t)stream); \
+    }                                                                                                              \
+    int tpl_coords_center_##SFX(const T *in, T *center, const int32_t *num_atoms, int batch, int atoms_stride,     \
+                                void *stream) {                                                                    \
+        if (batch < 0 || atoms_stride < 0) return TPL_ERR_ARGUMENT;                                                \
+        if (batch == 0) return TPL_OK;                                                                             \
+        if (!center || !num_atoms || (atoms_stride > 0 && !in)) return TPL_ERR_ARGUMENT;                           \
+        return coords_center<T>(in, center, num_atoms, batch, atoms_stride, (cudaStream_t)stream);                 \
+    }                                                                                                              \
+    int tpl_coords_center_backward_##SFX(const T *grad_center, T *grad_in, const int32_t *num_atoms, int batch,    \
+                                         int atoms_stride, void *stream) {                                         \
+        if (batch < 0 || atoms_stride < 0) return TPL_ERR_ARGUMENT;                                                \
+        if (batch == 0 || atoms_stride == 0) return TPL_OK;                                                        \
+        if (!grad_center || !grad_in || !num_atoms) return TPL_ERR_ARGUMENT;                                       \
+        return coords_shift<T>(nullptr, grad_in, grad_center, 1, num_atoms, batch, atoms_stride,                   \
+                               (cudaStream_t)stream);                                                              \
+    }                                                                                                              \
+    int tpl_coords_bbox_##SFX(const T *in, T *lo, T *hi, const int32_t *num_atoms, int batch, int atoms_stride,    \
+                              void *stream) {                                                                      \
+        if (batch < 0 || atoms_stride < 0) return TPL_ERR_ARGUMENT;                                                \
+        if (batch == 0) return TPL_OK;                                                                             \
+        if (!lo || !hi || !num_atoms || (atoms_stride > 0 && !in)) return TPL_ERR_ARGUMENT;                        \
+        return coords_bbox<T>(in, lo, hi, num_atoms, batch, atoms_stride, (cudaStream_t)stream);                   \
+    }
+
+TPL_TRANSFORM_ENTRIES(float, f32)
+TPL_TRANSFORM_ENTRIES(double, f64)
+#undef TPL_TRANSFORM_ENTRIES
+
 }  // extern "C"

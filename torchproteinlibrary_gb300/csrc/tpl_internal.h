@@ -85,6 +85,18 @@ int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const uns
                  const void *angles, void *ws, int B, int L, int maxA, const tpl_options &opt, cudaStream_t st);
 int num_atoms_host(const char *seq);
 
+// CoordsTransform launchers (tpl_transform.cu); T = float or double.
+template <typename T>
+int coords_shift(const T *in, T *out, const T *add, int scale_by_count, const int *num_atoms, int B, int stride,
+                 cudaStream_t st);
+template <typename T>
+int coords_rotate(const T *in, T *out, const T *R, int transpose, const int *num_atoms, int B, int stride,
+                  cudaStream_t st);
+template <typename T>
+int coords_center(const T *in, T *center, const int *num_atoms, int B, int stride, cudaStream_t st);
+template <typename T>
+int coords_bbox(const T *in, T *lo, T *hi, const int *num_atoms, int B, int stride, cudaStream_t st);
+
 // Coords2RMSD launchers (tpl_rmsd.cu).
 int rmsd_forward(bool f64, const void *src, const void *dst, const int *num_atoms, int B, int stride, int center,
                  void *rmsd, void *ut, double *centroids, void *ws, cudaStream_t st);

@@ -1,0 +1,256 @@
+// CoordsTransform on the GPU (sm_103a): translate, rotate, centre and bounding box
+// of batched coordinate rows [B, 3 * atoms_stride]; atoms at and past num_atoms[b]
+// are written as zeros, as the reference's zero-initialised outputs leave them.
+//
+// Reference: Layers/FullAtomModel/TransformCUDAKernels.cu:4-107 launches one block
+// per atom index with one thread per chain (<<<atoms_stride, batch_size>>>, so
+// batch_size <= 1024) and sums each centroid serially in one thread; the bounding
+// box runs on the CPU (Layers/FullAtomModel/CoordsTransform/
+// coordsTransform_interface.cpp:175-200, Math/nUtil.cpp:27-57).  Here the
+// elementwise transforms are flat, coalesced, 16-byte-vectorised passes over the
+// whole batch (HBM-bound: 2 x 12 B per atom in FP32), and centroid and box are
+// block reductions, one CTA per chain.
+#include <cfloat>
+#include <cmath>
+
+#include "tpl_internal.h"
+
+namespace tpl {
+namespace {
+
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+    static constexpr int n = 4;
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+    static constexpr int n = 2;
+};
+
+template <typename T>
+__device__ __forceinline__ void load16(const T *p, T (&v)[Vec16<T>::n]) {
+    const typename Vec16<T>::type x = *reinterpret_cast<const typename Vec16<T>::type *>(p);
+    memcpy(v, &x, sizeof(x));
+}
+template <typename T>
+__device__ __forceinline__ void store16(T *p, const T (&v)[Vec16<T>::n]) {
+    typename Vec16<T>::type x;
+    memcpy(&x, v, sizeof(x));
+    *reinterpret_cast<typename Vec16<T>::type *>(p) = x;
+}
+
+// out[b, e] = (in ? in[b, e] : 0) + (add ? add[b, e % 3] * (scale_by_count ? 1 / n_b : 1) : 0)
+// for e < 3 n_b, 0 after.  Covers translate (add = T), its backward (add = null),
+// and the centre's backward (in = null, add = dL/dcentre, scaled by 1 / n_b).
+struct ShiftArgs {
+    const void *in;
+    void *out;
+    const void *add;
+    const int *num_atoms;
+    long long total;  // B * row
+    int row;          // 3 * atoms_stride
+    int scale_by_count;
+};
+
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(256) shift_kernel(ShiftArgs a) {
+    constexpr int N = VEC ? Vec16<T>::n : 1;
+    const T *in = static_cast<const T *>(a.in);
+    T *out = static_cast<T *>(a.out);
+    const T *add = static_cast<const T *>(a.add);
+    const long long step = (long long)gridDim.x * blockDim.x;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v * N < a.total; v += step) {
+        const long long e0 = v * N;
+        T x[Vec16<T>::n];
+        if (VEC && in) load16(in + e0, x);
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            const long long e = e0 + k;
+            if (!VEC && in) x[k] = in[e];
+            if (!VEC && !in) x[k] = T(0);
+            if (VEC && !in) x[k] = T(0);
+            const long long b = e / a.row;
+            const int i = (int)(e - b * a.row);
+            const int n = a.num_atoms[b];
+            T y = T(0);
+            if (i < 3 * n) {
+                y = x[k];
+                if (add) {
+                    T s = add[3 * b + i % 3];
+                    if (a.scale_by_count) s = s / T(n);
+                    y += s;
+                }
+            }
+            x[k] = y;
+        }
+        if (VEC) {
+            store16(out + e0, x);
+        } else {
+            out[e0] = x[0];
+        }
+    }
+}
+
+// out[b, atom] = R_b x (or R_b^T x) for atom < n_b, 0 after; R row-major [B, 3, 3].
+template <typename T>
+__global__ void __launch_bounds__(256) rotate_kernel(const T *in, T *out, const T *R, const int *num_atoms,
+                                                     long long atoms, int stride, int transpose) {
+    const long long step = (long long)gridDim.x * blockDim.x;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < atoms; t += step) {
+        const long long b = t / stride;
+        const int i = (int)(t - b * stride);
+        const T *x = in + 3 * t;
+        T *y = out + 3 * t;
+        if (i >= num_atoms[b]) {
+            y[0] = y[1] = y[2] = T(0);
+            continue;
+        }
+        const T *m = R + 9 * b;
+        const T x0 = x[0], x1 = x[1], x2 = x[2];
+        if (transpose) {
+            y[0] = m[0] * x0 + m[3] * x1 + m[6] * x2;
+            y[1] = m[1] * x0 + m[4] * x1 + m[7] * x2;
+            y[2] = m[2] * x0 + m[5] * x1 + m[8] * x2;
+        } else {
+            y[0] = m[0] * x0 + m[1] * x1 + m[2] * x2;
+            y[1] = m[3] * x0 + m[4] * x1 + m[5] * x2;
+            y[2] = m[6] * x0 + m[7] * x1 + m[8] * x2;
+        }
+    }
+}
+
+constexpr int kReduceThreads = 256;
+
+template <typename R, typename Op>
+__device__ __forceinline__ R block_reduce(R v, Op op, R *s_warp) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, off));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) s_warp[w] = v;
+    __syncthreads();
+    R r = s_warp[0];
+    for (int k = 1; k < kReduceThreads / 32; k++) r = op(r, s_warp[k]);
+    __syncthreads();  // s_warp is reused by the next reduction
+    return r;
+}
+
+// Centroid of the first n_b atoms of chain b = blockIdx.x (FP64 accumulation);
+// 0 for an empty chain.
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) center_kernel(const T *in, T *center, const int *num_atoms,
+                                                                int stride) {
+    __shared__ double s_warp[kReduceThreads / 32];
+    const int b = blockIdx.x;
+    const int n = min(num_atoms[b], stride);  // a count past the row is clamped to it
+    const T *x = in + (size_t)b * 3 * stride;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < n; i += kReduceThreads) {
+        s[0] += (double)x[3 * i];
+        s[1] += (double)x[3 * i + 1];
+        s[2] += (double)x[3 * i + 2];
+    }
+    auto add = [](double p, double q) { return p + q; };
+    for (int c = 0; c < 3; c++) {
+        const double t = block_reduce<double>(s[c], add, s_warp);
+        if (threadIdx.x == 0) center[3 * b + c] = n > 0 ? (T)(t / n) : T(0);
+    }
+}
+
+// Axis-aligned bounding box of the first n_b atoms of chain b: lo = min, hi = max
+// per coordinate (+inf / -inf for an empty chain, as Math/nUtil.cpp:27-57).
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) bbox_kernel(const T *in, T *lo, T *hi, const int *num_atoms,
+                                                              int stride) {
+    __shared__ T s_warp[kReduceThreads / 32];
+    const int b = blockIdx.x;
+    const int n = min(num_atoms[b], stride);
+    const T *x = in + (size_t)b * 3 * stride;
+    const T inf = (T)INFINITY;
+    T mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf};
+    for (int i = threadIdx.x; i < n; i += kReduceThreads)
+        for (int c = 0; c < 3; c++) {
+            const T v = x[3 * i + c];
+            mn[c] = v < mn[c] ? v : mn[c];
+            mx[c] = v > mx[c] ? v : mx[c];
+        }
+    auto fmin_ = [](T p, T q) { return q < p ? q : p; };
+    auto fmax_ = [](T p, T q) { return q > p ? q : p; };
+    for (int c = 0; c < 3; c++) {
+        const T a = block_reduce<T>(mn[c], fmin_, s_warp);
+        const T z = block_reduce<T>(mx[c], fmax_, s_warp);
+        if (threadIdx.x == 0) {
+            lo[3 * b + c] = a;
+            hi[3 * b + c] = z;
+        }
+    }
+}
+
+int grid_for(long long items, int threads) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    long long g = (items + threads - 1) / threads;
+    const long long cap = (long long)sms * 8;  // a few waves of 256-thread CTAs, grid-stride beyond
+    if (g > cap) g = cap;
+    return g < 1 ? 1 : (int)g;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+
+template <typename T>
+int coords_shift(const T *in, T *out, const T *add, int scale_by_count, const int *num_atoms, int B, int stride,
+                 cudaStream_t st) {
+    if (B == 0 || stride == 0) return TPL_OK;
+    ShiftArgs a{in, out, add, num_atoms, (long long)B * 3 * stride, 3 * stride, scale_by_count};
+    const bool vec = aligned16(out) && (!in || aligned16(in)) && (a.total % Vec16<T>::n == 0);
+    if (vec) {
+        shift_kernel<T, true><<<grid_for(a.total / Vec16<T>::n, 256), 256, 0, st>>>(a);
+    } else {
+        shift_kernel<T, false><<<grid_for(a.total, 256), 256, 0, st>>>(a);
+    }
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+template <typename T>
+int coords_rotate(const T *in, T *out, const T *R, int transpose, const int *num_atoms, int B, int stride,
+                  cudaStream_t st) {
+    if (B == 0 || stride == 0) return TPL_OK;
+    const long long atoms = (long long)B * stride;
+    rotate_kernel<T><<<grid_for(atoms, 256), 256, 0, st>>>(in, out, R, num_atoms, atoms, stride, transpose);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+template <typename T>
+int coords_center(const T *in, T *center, const int *num_atoms, int B, int stride, cudaStream_t st) {
+    if (B == 0) return TPL_OK;
+    center_kernel<T><<<B, kReduceThreads, 0, st>>>(in, center, num_atoms, stride);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+template <typename T>
+int coords_bbox(const T *in, T *lo, T *hi, const int *num_atoms, int B, int stride, cudaStream_t st) {
+    if (B == 0) return TPL_OK;
+    bbox_kernel<T><<<B, kReduceThreads, 0, st>>>(in, lo, hi, num_atoms, stride);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+template int coords_shift<float>(const float *, float *, const float *, int, const int *, int, int, cudaStream_t);
+template int coords_shift<double>(const double *, double *, const double *, int, const int *, int, int, cudaStream_t);
+template int coords_rotate<float>(const float *, float *, const float *, int, const int *, int, int, cudaStream_t);
+template int coords_rotate<double>(const double *, double *, const double *, int, const int *, int, int, cudaStream_t);
+template int coords_center<float>(const float *, float *, const int *, int, int, cudaStream_t);
+template int coords_center<double>(const double *, double *, const int *, int, int, cudaStream_t);
+template int coords_bbox<float>(const float *, float *, float *, const int *, int, int, cudaStream_t);
+template int coords_bbox<double>(const double *, double *, double *, const int *, int, int, cudaStream_t);
+
+}  // namespace tpl
