@@ -43,7 +43,8 @@ typedef enum tpl_status {
     TPL_ERR_LOOKBACK_TIMEOUT = -6,  /* a bounded device wait gave up: inter-tile look-back or bulk copy */
     TPL_ERR_ATOMS = -7,             /* a chain needs more atom slots than max_atoms */
     TPL_ERR_UNSUPPORTED = -8,       /* option combination without a compiled kernel */
-    TPL_ERR_TOO_LARGE = -9          /* problem exceeds the fixed scratch of tpl_a2b_forward_f32_noalloc */
+    TPL_ERR_TOO_LARGE = -9,         /* problem exceeds the fixed scratch of tpl_a2b_forward_f32_noalloc */
+    TPL_ERR_ATOM_TYPE = -10         /* a (residue, atom) name pair outside the 11-type table */
 } tpl_status;
 
 /* Tuning knobs.  A NULL options pointer, or a zero field, selects the tuned default. */
@@ -236,6 +237,32 @@ int tpl_coords_bbox_f32(const float *in, float *lo, float *hi, const int32_t *nu
                         int atoms_stride, void *stream);
 int tpl_coords_bbox_f64(const double *in, double *lo, double *hi, const int32_t *num_atoms, int batch,
                         int atoms_stride, void *stream);
+
+/* ------------------------------------------------------------- Coords2TypedCoords
+ * Replaces Coords2TypedCoords_forward / _backward (Layers/FullAtomModel/
+ * Coords2TypedCoords/coords2typedcoords_interface.cpp; atom types of
+ * ProtUtil::get11AtomType, Math/nUtil.cpp:567-703), which run on the CPU.
+ * Forward: the first num_atoms[b] atoms of coords [batch, 3 * in_stride] (names
+ * res_names / atom_names [batch, in_stride, 4] bytes, as Angles2Coords writes them)
+ * regrouped by type, stable within a type, into out [batch, 3 * out_stride];
+ * num_atoms_of_type / offsets int32 [batch, 11]; atom_indexes int32
+ * [batch, out_stride] (typed slot -> input atom).  Unused slots are zero.  An
+ * unknown name pair is left out and records TPL_ERR_ATOM_TYPE in the workspace
+ * (>= 64 bytes, zeroed once; read back with tpl_workspace_status).
+ * Backward: grad_flat [batch, 3 * in_stride] = grad_typed scattered back through
+ * atom_indexes, zero elsewhere. */
+int tpl_typed_coords_forward_f32(const float *coords, const uint8_t *res_names, const uint8_t *atom_names,
+                                 const int32_t *num_atoms, int batch, int in_stride, int out_stride, float *out,
+                                 int32_t *num_atoms_of_type, int32_t *offsets, int32_t *atom_indexes,
+                                 void *workspace, size_t workspace_bytes, void *stream);
+int tpl_typed_coords_forward_f64(const double *coords, const uint8_t *res_names, const uint8_t *atom_names,
+                                 const int32_t *num_atoms, int batch, int in_stride, int out_stride, double *out,
+                                 int32_t *num_atoms_of_type, int32_t *offsets, int32_t *atom_indexes,
+                                 void *workspace, size_t workspace_bytes, void *stream);
+int tpl_typed_coords_backward_f32(const float *grad_typed, float *grad_flat, const int32_t *num_atoms_of_type,
+                                  const int32_t *atom_indexes, int batch, int in_stride, int out_stride, void *stream);
+int tpl_typed_coords_backward_f64(const double *grad_typed, double *grad_flat, const int32_t *num_atoms_of_type,
+                                  const int32_t *atom_indexes, int batch, int in_stride, int out_stride, void *stream);
 
 /* Diagnostics (no counterpart in the reference): s[i], c[i] = sin, cos of a[i] as
  * the FP32 Angles2Backbone kernels evaluate them (Cody-Waite reduction by pi/2 and

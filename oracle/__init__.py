@@ -288,3 +288,85 @@ def rotation_from_u(u: np.ndarray) -> np.ndarray:
                   [2 * (q[1] * q[3] - q[0] * q[2]), 2 * (q[2] * q[3] + q[0] * q[1]),
                    q[0] ** 2 - q[1] ** 2 - q[2] ** 2 + q[3] ** 2]]
     return out
+
+
+# ----------------------------------------------------------- Coords2TypedCoords
+# Restatement of ProtUtil::get11AtomType (Math/nUtil.cpp:567-703, terminal = false,
+# 0-based as it returns) and of Coords2TypedCoords_forward / _backward
+# (Layers/FullAtomModel/Coords2TypedCoords/coords2typedcoords_interface.cpp).
+_TYPE_GROUPS = {
+    0: ["CYSSG", "METSD", "MSESE"],
+    1: ["ASNND2", "GLNNE2"],
+    2: ["HISND1", "HISNE2", "TRPNE1"],
+    3: ["ARGNH1", "ARGNH2", "ARGNE"],
+    4: ["LYSNZ"],
+    5: ["ACEO", "ASNOD1", "GLNOE1"],
+    6: ["SEROG", "THROG1", "TYROH"],
+    7: ["ASPOD1", "ASPOD2", "GLUOE1", "GLUOE2"],
+    8: ["ARGCZ", "ASPCG", "GLUCD", "ACEC", "ASNCG", "GLNCD"],
+    9: ["HISCD2", "HISCE1", "HISCG", "PHECD1", "PHECD2", "PHECE1", "PHECE2", "PHECG", "PHECZ",
+        "TRPCD1", "TRPCD2", "TRPCE2", "TRPCE3", "TRPCG", "TRPCH2", "TRPCZ2", "TRPCZ3",
+        "TYRCD1", "TYRCD2", "TYRCE1", "TYRCE2", "TYRCG", "TYRCZ"],
+    10: ["ALACB", "ARGCB", "ARGCG", "ARGCD", "ASNCB", "ASPCB", "GLNCB", "GLNCG", "GLUCB", "GLUCG", "HISCB",
+         "ILECB", "ILECD1", "ILECG1", "ILECG2", "LEUCB", "LEUCD1", "LEUCD2", "LEUCG",
+         "LYSCB", "LYSCD", "LYSCG", "LYSCE", "METCB", "METCE", "METCG", "MSECB", "MSECE", "MSECG",
+         "PHECB", "PROCB", "PROCG", "PROCD", "SERCB", "THRCG2", "TRPCB", "TYRCB",
+         "VALCB", "VALCG1", "VALCG2", "ACECH3", "THRCB", "CYSCB"],
+}
+_FULL_NAME_TYPE = {name: t for t, names in _TYPE_GROUPS.items() for name in names}
+
+
+def atom_type_11(res: str, atom: str) -> int:
+    """0-based atom type, or -1 where the reference throws."""
+    atom = "".join(atom.split())
+    if atom == "O":
+        return 5
+    if atom in ("OXT", "OT2"):
+        return 7
+    if atom == "N":
+        return 1
+    if atom == "C":
+        return 8
+    if atom == "CA":
+        return 10
+    return _FULL_NAME_TYPE.get(res + atom, -1)
+
+
+def _name(slot) -> str:
+    b = bytes(slot)
+    return b.split(b"\0", 1)[0].decode("ascii")
+
+
+def typed_coords(coords: np.ndarray, res_names: np.ndarray, atom_names: np.ndarray, num_atoms, out_stride=None):
+    """(typed [B, 3 out_stride], num_atoms_of_type [B, 11], offsets [B, 11], atom_indexes [B, out_stride])."""
+    coords = np.asarray(coords)
+    B = coords.shape[0]
+    S = out_stride if out_stride is not None else int(max(num_atoms)) if B else 0
+    typed = np.zeros((B, 3 * S), dtype=coords.dtype)
+    counts = np.zeros((B, 11), dtype=np.int32)
+    offsets = np.zeros((B, 11), dtype=np.int32)
+    index = np.zeros((B, S), dtype=np.int32)
+    for b in range(B):
+        n = int(num_atoms[b])
+        types = [atom_type_11(_name(res_names[b, j]), _name(atom_names[b, j])) for j in range(n)]
+        for t in types:
+            counts[b, t] += 1
+        offsets[b, 1:] = np.cumsum(counts[b])[:-1]
+        added = np.zeros(11, dtype=np.int64)
+        for j, t in enumerate(types):
+            slot = offsets[b, t] + added[t]
+            typed[b, 3 * slot:3 * slot + 3] = coords[b, 3 * j:3 * j + 3]
+            index[b, slot] = j
+            added[t] += 1
+    return typed, counts, offsets, index
+
+
+def typed_coords_backward(grad_typed: np.ndarray, counts, index, in_stride: int) -> np.ndarray:
+    grad_typed = np.asarray(grad_typed)
+    B = grad_typed.shape[0]
+    out = np.zeros((B, 3 * in_stride), dtype=grad_typed.dtype)
+    for b in range(B):
+        for s in range(int(np.sum(counts[b]))):
+            j = index[b, s]
+            out[b, 3 * j:3 * j + 3] = grad_typed[b, 3 * s:3 * s + 3]
+    return out

@@ -1,2 +1,3 @@
 from .Angles2Coords import Angles2Coords
 from .CoordsTransform import *
+from .Coords2TypedCoords import *

@@ -52,6 +52,10 @@ _SIGNATURES = {
     "tpl_coords_center_backward_f64": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
     "tpl_coords_bbox_f32": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp]),
     "tpl_coords_bbox_f64": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp]),
+    "tpl_typed_coords_forward_f32": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "tpl_typed_coords_forward_f64": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "tpl_typed_coords_backward_f32": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _vp]),
+    "tpl_typed_coords_backward_f64": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _vp]),
     "tpl_rmsd_forward_f32": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tpl_rmsd_forward_f64": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tpl_rmsd_backward_f32": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp]),

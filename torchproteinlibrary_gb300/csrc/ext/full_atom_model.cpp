@@ -1,6 +1,8 @@
-// _FullAtomModel extension module: the reference's Angles2Coords entry points
-// (Layers/FullAtomModel/main.cpp:13-16, Angles2Coords/angles2coords_interface.cpp)
-// over the libtpl_gb300 C ABI.
+// _FullAtomModel extension module: the reference's Angles2Coords, CoordsTransform
+// and Coords2TypedCoords entry points (Layers/FullAtomModel/main.cpp,
+// Angles2Coords/angles2coords_interface.cpp, CoordsTransform/
+// coordsTransformGPU_interface.cpp, Coords2TypedCoords/
+// coords2typedcoords_interface.cpp) over the libtpl_gb300 C ABI.
 //
 // Differences from the reference, all deliberate:
 //  * The compute runs on CUDA tensors (float32: batched kernels, float64: FP64
@@ -324,6 +326,83 @@ void getBBox(torch::Tensor input_coords, torch::Tensor a, torch::Tensor b, torch
     check_status(s, "getBBox");
 }
 
+// ---------------------------------------------------------- Coords2TypedCoords
+// Reference entry points (Layers/FullAtomModel/Coords2TypedCoords/
+// coords2typedcoords_interface.cpp), on CUDA tensors.  Typed rows hold
+// output_coords.size(1) / 3 slots (the reference sizes them by max(num_atoms)).
+void Coords2TypedCoords_forward(torch::Tensor input_coords, torch::Tensor res_names, torch::Tensor atom_names,
+                                torch::Tensor num_atoms, torch::Tensor output_coords, torch::Tensor num_atoms_of_type,
+                                torch::Tensor offsets, torch::Tensor atom_indexes) {
+    check_coords(input_coords, "input_coords");
+    TORCH_CHECK(input_coords.dim() == 2 && input_coords.size(1) % 3 == 0, "coordinates must be [batch, 3 * atoms]");
+    const int64_t B = input_coords.size(0), S_in = input_coords.size(1) / 3;
+    for (auto *t : {&res_names, &atom_names}) {
+        TORCH_CHECK(t->is_cuda() && t->device() == input_coords.device() && t->scalar_type() == torch::kByte &&
+                        t->is_contiguous() && t->numel() == B * S_in * 4,
+                    "res_names / atom_names must be contiguous uint8 [batch, atoms, 4] on the coordinates' device");
+    }
+    check_num_atoms(num_atoms, input_coords);
+    check_same(output_coords, input_coords, "output_coords");
+    TORCH_CHECK(output_coords.dim() == 2 && output_coords.size(0) == B && output_coords.size(1) % 3 == 0,
+                "output_coords must be [batch, 3 * max_atoms]");
+    const int64_t S_out = output_coords.size(1) / 3;
+    for (auto *t : {&num_atoms_of_type, &offsets})
+        TORCH_CHECK(t->is_cuda() && t->scalar_type() == torch::kInt && t->is_contiguous() && t->numel() == B * 11,
+                    "num_atoms_of_type / offsets must be contiguous int32 [batch, 11] on the device");
+    TORCH_CHECK(atom_indexes.is_cuda() && atom_indexes.scalar_type() == torch::kInt && atom_indexes.is_contiguous() &&
+                    atom_indexes.numel() == B * S_out,
+                "atom_indexes must be contiguous int32 [batch, max_atoms] on the device");
+    const at::cuda::CUDAGuard guard(input_coords.device());
+    auto ws = status_ws(input_coords.device());
+    const bool f64 = input_coords.scalar_type() == torch::kDouble;
+    int s;
+    if (f64)
+        s = tpl_typed_coords_forward_f64(input_coords.data_ptr<double>(), res_names.data_ptr<uint8_t>(),
+                                         atom_names.data_ptr<uint8_t>(), num_atoms.data_ptr<int32_t>(), (int)B,
+                                         (int)S_in, (int)S_out, output_coords.data_ptr<double>(),
+                                         num_atoms_of_type.data_ptr<int32_t>(), offsets.data_ptr<int32_t>(),
+                                         atom_indexes.data_ptr<int32_t>(), ws.data_ptr(), ws.nbytes(),
+                                         stream_of(input_coords));
+    else
+        s = tpl_typed_coords_forward_f32(input_coords.data_ptr<float>(), res_names.data_ptr<uint8_t>(),
+                                         atom_names.data_ptr<uint8_t>(), num_atoms.data_ptr<int32_t>(), (int)B,
+                                         (int)S_in, (int)S_out, output_coords.data_ptr<float>(),
+                                         num_atoms_of_type.data_ptr<int32_t>(), offsets.data_ptr<int32_t>(),
+                                         atom_indexes.data_ptr<int32_t>(), ws.data_ptr(), ws.nbytes(),
+                                         stream_of(input_coords));
+    check_status(s, "Coords2TypedCoords_forward");
+}
+
+void Coords2TypedCoords_backward(torch::Tensor grad_typed_coords, torch::Tensor grad_flat_coords,
+                                 torch::Tensor num_atoms_of_type, torch::Tensor offsets, torch::Tensor atom_indexes) {
+    (void)offsets;  // the typed slots are addressed through atom_indexes
+    check_coords(grad_typed_coords, "grad_typed_coords");
+    check_same(grad_flat_coords, grad_typed_coords, "grad_flat_coords");
+    TORCH_CHECK(grad_typed_coords.dim() == 2 && grad_flat_coords.dim() == 2 &&
+                    grad_typed_coords.size(0) == grad_flat_coords.size(0) && grad_typed_coords.size(1) % 3 == 0 &&
+                    grad_flat_coords.size(1) % 3 == 0,
+                "gradients must be [batch, 3 * atoms]");
+    const int64_t B = grad_typed_coords.size(0), S_out = grad_typed_coords.size(1) / 3,
+                  S_in = grad_flat_coords.size(1) / 3;
+    TORCH_CHECK(num_atoms_of_type.is_cuda() && num_atoms_of_type.scalar_type() == torch::kInt &&
+                    num_atoms_of_type.is_contiguous() && num_atoms_of_type.numel() == B * 11,
+                "num_atoms_of_type must be contiguous int32 [batch, 11] on the device");
+    TORCH_CHECK(atom_indexes.is_cuda() && atom_indexes.scalar_type() == torch::kInt && atom_indexes.is_contiguous() &&
+                    atom_indexes.numel() == B * S_out,
+                "atom_indexes must be contiguous int32 [batch, max_atoms] on the device");
+    const at::cuda::CUDAGuard guard(grad_typed_coords.device());
+    int s;
+    if (grad_typed_coords.scalar_type() == torch::kDouble)
+        s = tpl_typed_coords_backward_f64(grad_typed_coords.data_ptr<double>(), grad_flat_coords.data_ptr<double>(),
+                                          num_atoms_of_type.data_ptr<int32_t>(), atom_indexes.data_ptr<int32_t>(),
+                                          (int)B, (int)S_in, (int)S_out, stream_of(grad_typed_coords));
+    else
+        s = tpl_typed_coords_backward_f32(grad_typed_coords.data_ptr<float>(), grad_flat_coords.data_ptr<float>(),
+                                          num_atoms_of_type.data_ptr<int32_t>(), atom_indexes.data_ptr<int32_t>(),
+                                          (int)B, (int)S_in, (int)S_out, stream_of(grad_typed_coords));
+    check_status(s, "Coords2TypedCoords_backward");
+}
+
 void no_cpu_transform(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
     TORCH_CHECK(false, "CoordsTransform: this build has no CPU path; move the tensors to a CUDA device");
 }
@@ -347,6 +426,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Coords2Center_forward", &no_cpu_center, "not available: no CPU path");
     m.def("Coords2Center_backward", &no_cpu_center, "not available: no CPU path");
     m.def("getBBox", &getBBox, "per-chain bounding box (GPU)");
+    m.def("Coords2TypedCoords_forward", &Coords2TypedCoords_forward, "Coords2TypedCoords forward (GPU)");
+    m.def("Coords2TypedCoords_backward", &Coords2TypedCoords_backward, "Coords2TypedCoords backward (GPU)");
     m.def("Angles2Coords_forward", &Angles2Coords_forward, "Angles2Coords forward");
     m.def("Angles2Coords_backward", &Angles2Coords_backward, "Angles2Coords backward");
     m.def("Angles2Coords_save", &Angles2Coords_save, "Angles2Coords save");

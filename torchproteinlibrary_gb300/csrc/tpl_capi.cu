@@ -120,6 +120,7 @@ const char *tpl_status_string(int status) {
         case TPL_ERR_ATOMS: return "chain has more atoms than max_atoms";
         case TPL_ERR_UNSUPPORTED: return "unsupported option combination";
         case TPL_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
+        case TPL_ERR_ATOM_TYPE: return "a (residue, atom) name pair has no atom type";
     }
     return "unknown status";
 }
@@ -379,6 +380,40 @@ int tpl_rmsd_backward_f64(const double *grad_rmsd, const double *src, const doub
         if (!lo || !hi || !num_atoms || (atoms_stride > 0 && !in)) return TPL_ERR_ARGUMENT;                        \
         return coords_bbox<T>(in, lo, hi, num_atoms, batch, atoms_stride, (cudaStream_t)stream);                   \
     }
+
+// ---------------------------------------------------------- Coords2TypedCoords
+#define TPL_TYPED_ENTRIES(T, SFX, F64)                                                                             \
+    int tpl_typed_coords_forward_##SFX(const T *coords, const uint8_t *res_names, const uint8_t *atom_names,       \
+                                       const int32_t *num_atoms, int batch, int in_stride, int out_stride, T *out, \
+                                       int32_t *num_atoms_of_type, int32_t *offsets, int32_t *atom_indexes,        \
+                                       void *workspace, size_t workspace_bytes, void *stream) {                    \
+        if (batch < 0 || in_stride < 0 || out_stride < 0) return TPL_ERR_ARGUMENT;                                 \
+        if (batch == 0) return TPL_OK;                                                                             \
+        if (!num_atoms || !num_atoms_of_type || !offsets) return TPL_ERR_ARGUMENT;                                 \
+        if ((in_stride > 0 && (!coords || !res_names || !atom_names)) || (out_stride > 0 && (!out || !atom_indexes))) \
+            return TPL_ERR_ARGUMENT;                                                                               \
+        if (((uintptr_t)res_names & 3u) || ((uintptr_t)atom_names & 3u)) return TPL_ERR_ARGUMENT;                 \
+        int s = check_ws(workspace, workspace_bytes, sizeof(WsHeader));                                            \
+        if (s) return s;                                                                                           \
+        return typed_forward(F64, coords, reinterpret_cast<const uint32_t *>(res_names),                           \
+                             reinterpret_cast<const uint32_t *>(atom_names), num_atoms, batch, in_stride,          \
+                             out_stride, out, num_atoms_of_type, offsets, atom_indexes, workspace,                 \
+                             (cudaStream_t)stream);                                                                \
+    }                                                                                                              \
+    int tpl_typed_coords_backward_##SFX(const T *grad_typed, T *grad_flat, const int32_t *num_atoms_of_type,       \
+                                        const int32_t *atom_indexes, int batch, int in_stride, int out_stride,     \
+                                        void *stream) {                                                            \
+        if (batch < 0 || in_stride < 0 || out_stride < 0) return TPL_ERR_ARGUMENT;                                 \
+        if (batch == 0) return TPL_OK;                                                                             \
+        if (!num_atoms_of_type || (in_stride > 0 && !grad_flat) || (out_stride > 0 && (!grad_typed || !atom_indexes))) \
+            return TPL_ERR_ARGUMENT;                                                                               \
+        return typed_backward(F64, grad_typed, grad_flat, num_atoms_of_type, atom_indexes, batch, in_stride,       \
+                              out_stride, (cudaStream_t)stream);                                                   \
+    }
+
+TPL_TYPED_ENTRIES(float, f32, false)
+TPL_TYPED_ENTRIES(double, f64, true)
+#undef TPL_TYPED_ENTRIES
 
 TPL_TRANSFORM_ENTRIES(float, f32)
 TPL_TRANSFORM_ENTRIES(double, f64)

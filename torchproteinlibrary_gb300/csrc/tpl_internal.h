@@ -97,6 +97,13 @@ int coords_center(const T *in, T *center, const int *num_atoms, int B, int strid
 template <typename T>
 int coords_bbox(const T *in, T *lo, T *hi, const int *num_atoms, int B, int stride, cudaStream_t st);
 
+// Coords2TypedCoords launchers (tpl_typed.cu); ws holds at least a WsHeader.
+int typed_forward(bool f64, const void *coords, const uint32_t *res_names, const uint32_t *atom_names,
+                  const int *num_atoms, int B, int in_stride, int out_stride, void *out, int *n_of_type, int *offsets,
+                  int *atom_index, void *ws, cudaStream_t st);
+int typed_backward(bool f64, const void *grad_typed, void *grad_flat, const int *n_of_type, const int *atom_index,
+                   int B, int in_stride, int out_stride, cudaStream_t st);
+
 // Coords2RMSD launchers (tpl_rmsd.cu).
 int rmsd_forward(bool f64, const void *src, const void *dst, const int *num_atoms, int B, int stride, int center,
                  void *rmsd, void *ut, double *centroids, void *ws, cudaStream_t st);

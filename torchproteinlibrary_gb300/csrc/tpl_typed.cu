@@ -1,0 +1,240 @@
+// Coords2TypedCoords on the GPU (sm_103a): atoms regrouped by the 11 atom types of
+// ProtUtil::get11AtomType (Math/nUtil.cpp:567-703), stable within a type.
+//
+// Reference: Layers/FullAtomModel/Coords2TypedCoords/coords2typedcoords_interface.cpp
+// runs on the CPU, one OpenMP task per chain, with string compares per atom.  Here
+// one CTA per chain classifies its atoms from the packed 4-byte name words that
+// Angles2Coords writes, counts them per type, and scatters coordinates in a stable
+// order: per 256-atom tile, one warp ballot per type gives each atom its rank among
+// the atoms of its type before it.  The backward is the inverse gather.  Integer and
+// byte work only; coordinates are copied unchanged.
+#include <cstdint>
+
+#include "tpl_internal.h"
+
+namespace tpl {
+namespace {
+
+constexpr int kTypes = 11;
+constexpr int kTypedThreads = 256;
+
+// Name word: the bytes of a NUL-padded 4-byte name slot, little-endian.
+constexpr uint32_t nm(const char *s) {
+    uint32_t w = 0;
+    for (int i = 0; i < 4 && s[i]; i++) w |= (uint32_t)(unsigned char)s[i] << (8 * i);
+    return w;
+}
+
+struct TypedName {
+    uint32_t res, atom;
+    int type;
+};
+
+// Residue-specific types (0-based, as get11AtomType returns them); the
+// residue-agnostic backbone names are handled first in atom_type().
+__device__ const TypedName kTypedNames[] = {
+    // 0: sulfur / selenium
+    {nm("CYS"), nm("SG"), 0}, {nm("MET"), nm("SD"), 0}, {nm("MSE"), nm("SE"), 0},
+    // 1: amide N
+    {nm("ASN"), nm("ND2"), 1}, {nm("GLN"), nm("NE2"), 1},
+    // 2: aromatic N
+    {nm("HIS"), nm("ND1"), 2}, {nm("HIS"), nm("NE2"), 2}, {nm("TRP"), nm("NE1"), 2},
+    // 3: guanidine N
+    {nm("ARG"), nm("NH1"), 3}, {nm("ARG"), nm("NH2"), 3}, {nm("ARG"), nm("NE"), 3},
+    // 4: N with three hydrogens
+    {nm("LYS"), nm("NZ"), 4},
+    // 5: carbonyl / amide O
+    {nm("ACE"), nm("O"), 5}, {nm("ASN"), nm("OD1"), 5}, {nm("GLN"), nm("OE1"), 5},
+    // 6: hydroxyl O
+    {nm("SER"), nm("OG"), 6}, {nm("THR"), nm("OG1"), 6}, {nm("TYR"), nm("OH"), 6},
+    // 7: carboxyl O
+    {nm("ASP"), nm("OD1"), 7}, {nm("ASP"), nm("OD2"), 7}, {nm("GLU"), nm("OE1"), 7}, {nm("GLU"), nm("OE2"), 7},
+    // 8: sp2 C
+    {nm("ARG"), nm("CZ"), 8}, {nm("ASP"), nm("CG"), 8}, {nm("GLU"), nm("CD"), 8}, {nm("ACE"), nm("C"), 8},
+    {nm("ASN"), nm("CG"), 8}, {nm("GLN"), nm("CD"), 8},
+    // 9: aromatic C
+    {nm("HIS"), nm("CD2"), 9}, {nm("HIS"), nm("CE1"), 9}, {nm("HIS"), nm("CG"), 9},
+    {nm("PHE"), nm("CD1"), 9}, {nm("PHE"), nm("CD2"), 9}, {nm("PHE"), nm("CE1"), 9}, {nm("PHE"), nm("CE2"), 9},
+    {nm("PHE"), nm("CG"), 9}, {nm("PHE"), nm("CZ"), 9},
+    {nm("TRP"), nm("CD1"), 9}, {nm("TRP"), nm("CD2"), 9}, {nm("TRP"), nm("CE2"), 9}, {nm("TRP"), nm("CE3"), 9},
+    {nm("TRP"), nm("CG"), 9}, {nm("TRP"), nm("CH2"), 9}, {nm("TRP"), nm("CZ2"), 9}, {nm("TRP"), nm("CZ3"), 9},
+    {nm("TYR"), nm("CD1"), 9}, {nm("TYR"), nm("CD2"), 9}, {nm("TYR"), nm("CE1"), 9}, {nm("TYR"), nm("CE2"), 9},
+    {nm("TYR"), nm("CG"), 9}, {nm("TYR"), nm("CZ"), 9},
+    // 10: sp3 C
+    {nm("ALA"), nm("CB"), 10}, {nm("ARG"), nm("CB"), 10}, {nm("ARG"), nm("CG"), 10}, {nm("ARG"), nm("CD"), 10},
+    {nm("ASN"), nm("CB"), 10}, {nm("ASP"), nm("CB"), 10}, {nm("GLN"), nm("CB"), 10}, {nm("GLN"), nm("CG"), 10},
+    {nm("GLU"), nm("CB"), 10}, {nm("GLU"), nm("CG"), 10}, {nm("HIS"), nm("CB"), 10},
+    {nm("ILE"), nm("CB"), 10}, {nm("ILE"), nm("CD1"), 10}, {nm("ILE"), nm("CG1"), 10}, {nm("ILE"), nm("CG2"), 10},
+    {nm("LEU"), nm("CB"), 10}, {nm("LEU"), nm("CD1"), 10}, {nm("LEU"), nm("CD2"), 10}, {nm("LEU"), nm("CG"), 10},
+    {nm("LYS"), nm("CB"), 10}, {nm("LYS"), nm("CD"), 10}, {nm("LYS"), nm("CG"), 10}, {nm("LYS"), nm("CE"), 10},
+    {nm("MET"), nm("CB"), 10}, {nm("MET"), nm("CE"), 10}, {nm("MET"), nm("CG"), 10},
+    {nm("MSE"), nm("CB"), 10}, {nm("MSE"), nm("CE"), 10}, {nm("MSE"), nm("CG"), 10}, {nm("PHE"), nm("CB"), 10},
+    {nm("PRO"), nm("CB"), 10}, {nm("PRO"), nm("CG"), 10}, {nm("PRO"), nm("CD"), 10}, {nm("SER"), nm("CB"), 10},
+    {nm("THR"), nm("CG2"), 10}, {nm("TRP"), nm("CB"), 10}, {nm("TYR"), nm("CB"), 10},
+    {nm("VAL"), nm("CB"), 10}, {nm("VAL"), nm("CG1"), 10}, {nm("VAL"), nm("CG2"), 10},
+    {nm("ACE"), nm("CH3"), 10}, {nm("THR"), nm("CB"), 10}, {nm("CYS"), nm("CB"), 10},
+};
+constexpr int kTypedNameCount = sizeof(kTypedNames) / sizeof(TypedName);
+
+// Drop the space bytes of a name word (the reference erases whitespace from the
+// atom name before comparing) and stop at the first NUL.
+__device__ __forceinline__ uint32_t squeeze(uint32_t w) {
+    uint32_t out = 0;
+    int k = 0;
+    for (int i = 0; i < 4; i++) {
+        const uint32_t c = (w >> (8 * i)) & 0xffu;
+        if (c == 0) break;
+        if (c == ' ' || (c >= 9 && c <= 13)) continue;
+        out |= c << (8 * k++);
+    }
+    return out;
+}
+
+// The 0-based type of an atom, or -1 for a name pair the reference rejects.
+__device__ __forceinline__ int atom_type(uint32_t res, uint32_t atom) {
+    atom = squeeze(atom);
+    res = res & 0x00ffffffu;  // the residue is its 3-letter code
+    if (atom == nm("O")) return 5;  // not a terminal oxygen (the reference's call passes false)
+    if (atom == nm("OXT") || atom == nm("OT2")) return 7;
+    if (atom == nm("N")) return 1;
+    if (atom == nm("C")) return 8;
+    if (atom == nm("CA")) return 10;
+    for (int i = 0; i < kTypedNameCount; i++)
+        if (kTypedNames[i].res == res && kTypedNames[i].atom == atom) return kTypedNames[i].type;
+    return -1;
+}
+
+// Input rows hold in_stride atoms (coordinates and names); typed rows and atom
+// indexes hold out_stride slots.
+template <typename T>
+__global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coords, const uint32_t *res_names,
+                                                                  const uint32_t *atom_names, const int *num_atoms,
+                                                                  int in_stride, int out_stride, T *out,
+                                                                  int *n_of_type, int *offsets, int *atom_index,
+                                                                  WsHeader *hdr) {
+    constexpr int NW = kTypedThreads / 32;
+    __shared__ int s_count[kTypes], s_off[kTypes], s_base[kTypes];
+    __shared__ int s_wc[kTypes][NW];
+    const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int n = max(0, min(num_atoms[b], min(in_stride, out_stride)));
+    const size_t row = (size_t)b * in_stride, orow = (size_t)b * out_stride;
+    if (tid < kTypes) {
+        s_count[tid] = 0;
+        s_base[tid] = 0;
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += kTypedThreads) {
+        const int t = atom_type(res_names[row + j], atom_names[row + j]);
+        if (t >= 0) atomicAdd(&s_count[t], 1);
+        else atomicCAS(&hdr->status, 0u, (unsigned)TPL_ERR_ATOM_TYPE);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int o = 0;
+        for (int k = 0; k < kTypes; k++) {
+            s_off[k] = o;
+            o += s_count[k];
+        }
+    }
+    __syncthreads();
+    if (tid < kTypes) {
+        n_of_type[(size_t)b * kTypes + tid] = s_count[tid];
+        offsets[(size_t)b * kTypes + tid] = s_off[tid];
+    }
+    const int ntyped = s_off[kTypes - 1] + s_count[kTypes - 1];
+    // stable scatter, one tile of kTypedThreads atoms at a time
+    for (int j0 = 0; j0 < n; j0 += kTypedThreads) {
+        const int j = j0 + tid;
+        const int t = j < n ? atom_type(res_names[row + j], atom_names[row + j]) : -1;
+        int rank = 0;
+        const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+        for (int k = 0; k < kTypes; k++) {
+            const unsigned m = __ballot_sync(0xffffffffu, t == k);
+            if (t == k) rank = __popc(m & below);
+            if (lane == 0) s_wc[k][w] = __popc(m);
+        }
+        __syncthreads();
+        if (t >= 0) {
+            int before = s_base[t];
+            for (int v = 0; v < w; v++) before += s_wc[t][v];
+            const int slot = s_off[t] + before + rank;
+            const T *src = coords + 3 * (row + j);
+            T *dst = out + 3 * (orow + slot);
+            dst[0] = src[0];
+            dst[1] = src[1];
+            dst[2] = src[2];
+            atom_index[orow + slot] = j;
+        }
+        __syncthreads();
+        if (tid < kTypes)
+            for (int v = 0; v < NW; v++) s_base[tid] += s_wc[tid][v];
+        __syncthreads();
+    }
+    // slots past the typed atoms are zero, as in the reference's zero-filled outputs
+    for (int s = ntyped + tid; s < out_stride; s += kTypedThreads) {
+        T *dst = out + 3 * (orow + s);
+        dst[0] = dst[1] = dst[2] = T(0);
+        atom_index[orow + s] = 0;
+    }
+}
+
+// grad_flat[atom_index[s]] = grad_typed[s] for the typed slots, zero elsewhere;
+// grad_flat rows hold in_stride atoms, grad_typed rows out_stride slots.
+template <typename T>
+__global__ void __launch_bounds__(kTypedThreads) typed_bwd_kernel(const T *grad_typed, T *grad_flat,
+                                                                  const int *n_of_type, const int *atom_index,
+                                                                  int in_stride, int out_stride) {
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const size_t row = (size_t)b * in_stride, orow = (size_t)b * out_stride;
+    int ntyped = 0;
+    for (int k = 0; k < kTypes; k++) ntyped += n_of_type[(size_t)b * kTypes + k];
+    ntyped = max(0, min(ntyped, out_stride));
+    for (int e = tid; e < 3 * in_stride; e += kTypedThreads) grad_flat[3 * row + e] = T(0);
+    __syncthreads();
+    for (int s = tid; s < ntyped; s += kTypedThreads) {
+        const int j = atom_index[orow + s];
+        if (j < 0 || j >= in_stride) continue;
+        const T *src = grad_typed + 3 * (orow + s);
+        T *dst = grad_flat + 3 * (row + j);
+        dst[0] = src[0];
+        dst[1] = src[1];
+        dst[2] = src[2];
+    }
+}
+
+}  // namespace
+
+int typed_forward(bool f64, const void *coords, const uint32_t *res_names, const uint32_t *atom_names,
+                  const int *num_atoms, int B, int in_stride, int out_stride, void *out, int *n_of_type, int *offsets,
+                  int *atom_index, void *ws, cudaStream_t st) {
+    if (B == 0) return TPL_OK;
+    WsHeader *hdr = reinterpret_cast<WsHeader *>(ws);
+    if (f64)
+        typed_fwd_kernel<double><<<B, kTypedThreads, 0, st>>>(static_cast<const double *>(coords), res_names,
+                                                             atom_names, num_atoms, in_stride, out_stride,
+                                                             static_cast<double *>(out), n_of_type, offsets,
+                                                             atom_index, hdr);
+    else
+        typed_fwd_kernel<float><<<B, kTypedThreads, 0, st>>>(static_cast<const float *>(coords), res_names, atom_names,
+                                                            num_atoms, in_stride, out_stride,
+                                                            static_cast<float *>(out), n_of_type, offsets, atom_index,
+                                                            hdr);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+int typed_backward(bool f64, const void *grad_typed, void *grad_flat, const int *n_of_type, const int *atom_index,
+                   int B, int in_stride, int out_stride, cudaStream_t st) {
+    if (B == 0) return TPL_OK;
+    if (f64)
+        typed_bwd_kernel<double><<<B, kTypedThreads, 0, st>>>(static_cast<const double *>(grad_typed),
+                                                             static_cast<double *>(grad_flat), n_of_type, atom_index,
+                                                             in_stride, out_stride);
+    else
+        typed_bwd_kernel<float><<<B, kTypedThreads, 0, st>>>(static_cast<const float *>(grad_typed),
+                                                            static_cast<float *>(grad_flat), n_of_type, atom_index,
+                                                            in_stride, out_stride);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+}  // namespace tpl
