@@ -44,7 +44,8 @@ typedef enum tpl_status {
     TPL_ERR_ATOMS = -7,             /* a chain needs more atom slots than max_atoms */
     TPL_ERR_UNSUPPORTED = -8,       /* option combination without a compiled kernel */
     TPL_ERR_TOO_LARGE = -9,         /* problem exceeds the fixed scratch of tpl_a2b_forward_f32_noalloc */
-    TPL_ERR_ATOM_TYPE = -10         /* a (residue, atom) name pair outside the 11-type table */
+    TPL_ERR_ATOM_TYPE = -10,        /* a (residue, atom) name pair outside the 11-type table */
+    TPL_ERR_IO = -11                /* a file could not be opened */
 } tpl_status;
 
 /* Tuning knobs.  A NULL options pointer, or a zero field, selects the tuned default. */
@@ -263,6 +264,21 @@ int tpl_typed_coords_backward_f32(const float *grad_typed, float *grad_flat, con
                                   const int32_t *atom_indexes, int batch, int in_stride, int out_stride, void *stream);
 int tpl_typed_coords_backward_f64(const double *grad_typed, double *grad_flat, const int32_t *num_atoms_of_type,
                                   const int32_t *atom_indexes, int batch, int in_stride, int out_stride, void *stream);
+
+/* ------------------------------------------------------------------- PDB reading
+ * Host functions (no GPU), the reader of PDB2CoordsUnordered
+ * (Layers/FullAtomModel/PDB2Coords/pdb2coords_interface.cpp:75-127, parsing of
+ * Layers/FullAtomModel/cPDBLoader.cpp:25-55): heavy-atom ATOM records (atom names
+ * starting with C, N, O or S), coordinates parsed as float and widened to double,
+ * names in NUL-padded 4-byte slots.  tpl_pdb_count_atoms gives one file's count;
+ * tpl_pdb_read_batch fills rows of max_atoms atoms per file (coords
+ * [batch, 3 max_atoms], names [batch, max_atoms, 4], res_nums [batch, max_atoms];
+ * rows zero-padded) using `threads` host threads (0 = all cores).  It returns
+ * TPL_ERR_IO if a file cannot be opened and TPL_ERR_ATOMS if a file holds more than
+ * max_atoms atoms (num_atoms still reports the full count). */
+int tpl_pdb_count_atoms(const char *filename, int32_t *num_atoms);
+int tpl_pdb_read_batch(const char *const *filenames, int batch, int max_atoms, double *coords, uint8_t *chain_names,
+                       uint8_t *res_names, int32_t *res_nums, uint8_t *atom_names, int32_t *num_atoms, int threads);
 
 /* Diagnostics (no counterpart in the reference): s[i], c[i] = sin, cos of a[i] as
  * the FP32 Angles2Backbone kernels evaluate them (Cody-Waite reduction by pi/2 and

@@ -370,3 +370,43 @@ def typed_coords_backward(grad_typed: np.ndarray, counts, index, in_stride: int)
             j = index[b, s]
             out[b, 3 * j:3 * j + 3] = grad_typed[b, 3 * s:3 * s + 3]
     return out
+
+
+# ------------------------------------------------------------------ PDB reading
+def pdb_read(filename: str, impl: str = "port"):
+    """Heavy-atom ATOM records of a PDB file as the reference's cPDBLoader reads them
+    (Layers/FullAtomModel/cPDBLoader.cpp:25-55): (coords [n, 3] f64, chain_names,
+    res_names, atom_names as lists of str, res_nums int32 [n]).  impl="ref" runs the
+    reference's own reader (oracle/_ref); "port" restates it: a line whose first four
+    characters are "ATOM", atom name = columns 13-16 trimmed and starting with
+    C/N/O/S, x/y/z = columns 31-38/39-46/47-54 read as float32, residue name =
+    columns 18-20, chain = column 22, residue number = columns 23-26."""
+    if impl == "ref":
+        lib = ref()
+        lib.ref_pdb_read.restype = ctypes.c_int
+        lib.ref_pdb_read.argtypes = [ctypes.c_char_p, ctypes.c_int, _dp, ctypes.c_char_p, ctypes.c_char_p, _ip,
+                                     ctypes.c_char_p]
+        n = lib.ref_pdb_read(filename.encode(), 0, None, None, None, None, None)
+        if n < 0:
+            raise RuntimeError(f"reference PDB reader failed on {filename}")
+        coords = np.zeros((max(n, 1), 3))
+        names = [ctypes.create_string_buffer(4 * max(n, 1)) for _ in range(3)]
+        nums = np.zeros(max(n, 1), dtype=np.int32)
+        lib.ref_pdb_read(filename.encode(), n, _ptr(coords, _dp), names[0], names[1], _ptr(nums, _ip), names[2])
+        dec = [[buf.raw[4 * j:4 * j + 4].split(b"\0", 1)[0].decode() for j in range(n)] for buf in names]
+        return coords[:n], dec[0], dec[1], dec[2], nums[:n]
+    coords, chains, res, atoms, nums = [], [], [], [], []
+    with open(filename) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            if not line.startswith("ATOM"):
+                continue
+            name = line[12:16].strip()
+            if not name or name[0] not in "CNOS":
+                continue
+            coords.append([float(np.float32(line[k:k + 8])) for k in (30, 38, 46)])
+            res.append(line[17:20].strip())
+            chains.append(line[21:22].strip())
+            nums.append(int(line[22:26]))
+            atoms.append(name)
+    return np.array(coords, dtype=np.float64).reshape(-1, 3), chains, res, atoms, np.array(nums, dtype=np.int32)

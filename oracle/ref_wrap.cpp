@@ -12,6 +12,7 @@
  * Angles2Coords interface already uses OpenMP over chains
  * (angles2coords_interface.cpp:27,92).
  */
+#include <cctype>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -20,6 +21,7 @@
 
 #include "cBackboneProteinCPUKernels.hpp"
 #include "cConformation.h"
+#include "cPDBLoader.h"
 #include "nUtil.h"
 
 std::string StringUtil::string_format(const std::string fmt, ...) {
@@ -38,6 +40,20 @@ std::string ProtUtil::convertRes1to3(char r) {
     const char *p = std::strchr(one, r);
     if (!p || !r) throw std::string("Unknown residue name");
     return std::string(three[p - one]);
+}
+
+// Math/nUtil.cpp:119-123: whitespace stripped from both ends.
+std::string StringUtil::trim(const std::string &s) {
+    size_t a = 0, b = s.size();
+    while (a < b && std::isspace((unsigned char)s[a])) a++;
+    while (b > a && std::isspace((unsigned char)s[b - 1])) b--;
+    return s.substr(a, b - a);
+}
+
+// Math/nUtil.cpp:166-171: C, N, O or S as the first character.
+bool ProtUtil::isHeavyAtom(std::string &atom_name) {
+    const char c = atom_name.empty() ? '\0' : atom_name[0];
+    return c == 'C' || c == 'N' || c == 'O' || c == 'S';
 }
 
 extern "C" {
@@ -116,4 +132,25 @@ int ref_a2c_backward(double *grad_atoms, double *grad_angles, const unsigned cha
     return err;
 }
 
+
+// The reference's PDB reader (cPDBLoader, as PDB2CoordsUnordered uses it): fills up
+// to max_atoms atoms (coords xyz, names as NUL-padded 4-byte slots, residue
+// numbers) and returns the file's heavy-atom count, or -1 if it cannot be read.
+int ref_pdb_read(const char *filename, int max_atoms, double *coords, char *chain_names, char *res_names,
+                 int *res_nums, char *atom_names) {
+    try {
+        cPDBLoader pdb{std::string(filename)};
+        const int n = (int)pdb.r.size();
+        for (int j = 0; j < n && j < max_atoms; j++) {
+            for (int k = 0; k < 3; k++) coords[3 * j + k] = pdb.r[j].v[k];
+            std::strncpy(chain_names + 4 * j, pdb.chain_names[j].c_str(), 4);
+            std::strncpy(res_names + 4 * j, pdb.res_names[j].c_str(), 4);
+            std::strncpy(atom_names + 4 * j, pdb.atom_names[j].c_str(), 4);
+            res_nums[j] = pdb.res_nums[j];
+        }
+        return n;
+    } catch (...) {
+        return -1;
+    }
+}
 }  // extern "C"

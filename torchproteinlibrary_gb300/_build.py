@@ -29,7 +29,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["tpl_a2b.cu", "tpl_a2b_chain.cu", "tpl_a2c.cu", "tpl_rmsd.cu", "tpl_transform.cu", "tpl_typed.cu", "tpl_capi.cu", "tpl_noalloc.cu"]
+CU_SOURCES = ["tpl_a2b.cu", "tpl_a2b_chain.cu", "tpl_a2c.cu", "tpl_rmsd.cu", "tpl_transform.cu", "tpl_typed.cu", "tpl_pdb.cpp", "tpl_capi.cu", "tpl_noalloc.cu"]
 EXTENSIONS = {"_ReducedModel": "ext/reduced_model.cpp", "_FullAtomModel": "ext/full_atom_model.cpp",
               "_RMSD": "ext/rmsd.cpp"}
 

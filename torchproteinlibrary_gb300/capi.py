@@ -56,6 +56,8 @@ _SIGNATURES = {
     "tpl_typed_coords_forward_f64": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tpl_typed_coords_backward_f32": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _vp]),
     "tpl_typed_coords_backward_f64": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _vp]),
+    "tpl_pdb_count_atoms": (_i, [ctypes.c_char_p, _vp]),
+    "tpl_pdb_read_batch": (_i, [ctypes.POINTER(ctypes.c_char_p), _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i]),
     "tpl_rmsd_forward_f32": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tpl_rmsd_forward_f64": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
     "tpl_rmsd_backward_f32": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp]),

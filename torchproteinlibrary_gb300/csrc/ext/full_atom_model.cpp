@@ -16,7 +16,10 @@
 #include <c10/cuda/CUDAStream.h>
 #include <torch/extension.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <cstring>
+#include <vector>
 #include <map>
 #include <mutex>
 #include <string>
@@ -403,6 +406,47 @@ void Coords2TypedCoords_backward(torch::Tensor grad_typed_coords, torch::Tensor 
     check_status(s, "Coords2TypedCoords_backward");
 }
 
+// ------------------------------------------------------------------ PDB reading
+// PDB2CoordsUnordered (Layers/FullAtomModel/PDB2Coords/pdb2coords_interface.cpp:
+// 75-127): host tensors, resized in place to the largest file's atom count, as the
+// reference does.  The parsing is the C ABI's tpl_pdb_read_batch (host threads).
+void PDB2CoordsUnordered(torch::Tensor filenames, torch::Tensor coords, torch::Tensor chain_names,
+                         torch::Tensor res_names, torch::Tensor res_nums, torch::Tensor atom_names,
+                         torch::Tensor num_atoms) {
+    TORCH_CHECK(!filenames.is_cuda() && filenames.scalar_type() == torch::kByte && filenames.dim() == 2,
+                "filenames must be a CPU uint8 [batch, max_len] tensor of NUL-terminated paths");
+    TORCH_CHECK(!coords.is_cuda() && coords.scalar_type() == torch::kDouble, "coords must be a CPU float64 tensor");
+    for (auto *t : {&chain_names, &res_names, &atom_names})
+        TORCH_CHECK(!t->is_cuda() && t->scalar_type() == torch::kByte, "names must be CPU uint8 tensors");
+    TORCH_CHECK(!res_nums.is_cuda() && res_nums.scalar_type() == torch::kInt, "res_nums must be a CPU int32 tensor");
+    TORCH_CHECK(!num_atoms.is_cuda() && num_atoms.scalar_type() == torch::kInt && num_atoms.is_contiguous(),
+                "num_atoms must be a contiguous CPU int32 tensor");
+    const int64_t B = filenames.size(0);
+    TORCH_CHECK(num_atoms.numel() == B, "num_atoms must hold one count per file");
+    auto fn = filenames.contiguous();
+    std::vector<std::string> names(B);
+    std::vector<const char *> ptrs(B);
+    int32_t max_atoms = 0;
+    for (int64_t b = 0; b < B; b++) {
+        const char *row = reinterpret_cast<const char *>(fn.data_ptr<uint8_t>()) + b * fn.size(1);
+        names[b] = std::string(row, strnlen(row, (size_t)fn.size(1)));
+        ptrs[b] = names[b].c_str();
+        int32_t n = 0;
+        check_status(tpl_pdb_count_atoms(ptrs[b], &n), ("PDB2CoordsUnordered: " + names[b]).c_str());
+        max_atoms = std::max(max_atoms, n);
+    }
+    coords.resize_({B, 3 * (int64_t)max_atoms});
+    chain_names.resize_({B, max_atoms, 4});
+    res_names.resize_({B, max_atoms, 4});
+    res_nums.resize_({B, max_atoms});
+    atom_names.resize_({B, max_atoms, 4});
+    const int s = tpl_pdb_read_batch(ptrs.data(), (int)B, max_atoms, coords.data_ptr<double>(),
+                                     chain_names.data_ptr<uint8_t>(), res_names.data_ptr<uint8_t>(),
+                                     res_nums.data_ptr<int32_t>(), atom_names.data_ptr<uint8_t>(),
+                                     num_atoms.data_ptr<int32_t>(), 0);
+    check_status(s, "PDB2CoordsUnordered");
+}
+
 void no_cpu_transform(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
     TORCH_CHECK(false, "CoordsTransform: this build has no CPU path; move the tensors to a CUDA device");
 }
@@ -426,6 +470,7 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Coords2Center_forward", &no_cpu_center, "not available: no CPU path");
     m.def("Coords2Center_backward", &no_cpu_center, "not available: no CPU path");
     m.def("getBBox", &getBBox, "per-chain bounding box (GPU)");
+    m.def("PDB2CoordsUnordered", &PDB2CoordsUnordered, "Convert PDB to coordinates in the PDB order");
     m.def("Coords2TypedCoords_forward", &Coords2TypedCoords_forward, "Coords2TypedCoords forward (GPU)");
     m.def("Coords2TypedCoords_backward", &Coords2TypedCoords_backward, "Coords2TypedCoords backward (GPU)");
     m.def("Angles2Coords_forward", &Angles2Coords_forward, "Angles2Coords forward");

@@ -121,6 +121,7 @@ const char *tpl_status_string(int status) {
         case TPL_ERR_UNSUPPORTED: return "unsupported option combination";
         case TPL_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
         case TPL_ERR_ATOM_TYPE: return "a (residue, atom) name pair has no atom type";
+        case TPL_ERR_IO: return "a file could not be opened";
     }
     return "unknown status";
 }
