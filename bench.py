@@ -212,9 +212,9 @@ def run_ours(args):
     sweep_rows = None
     if args.rpt:
         rm.set_options(args.rpt, 0, 0, 0, args.cta)
-        rm.set_backward_options(args.bwd_rpt)
+        rm.set_backward_options(args.bwd_rpt, args.bwd_buffers)
         tuned = {"residues_per_thread": args.rpt, "threads_per_cta": args.cta, "fp64_carry_min_len": 0,
-                 "backward_coords": {"residues_per_thread": args.bwd_rpt}}
+                 "backward_coords": {"residues_per_thread": args.bwd_rpt, "copy_buffers": args.bwd_buffers}}
     else:
         tuned = autotune.tune(ang, lengths, up, use_cache=False)
         if not args.no_extras:
@@ -563,6 +563,7 @@ def main():
     ap.add_argument("--rpt", type=int, default=0,
                     help="residues per thread; 0 = autotune (the default)")
     ap.add_argument("--bwd-rpt", type=int, default=4, help="residues per lane of the coordinate backward (with --rpt)")
+    ap.add_argument("--bwd-buffers", type=int, default=1, help="chunk buffers of the coordinate backward (with --rpt)")
     ap.add_argument("--cta", type=int, default=0, help="0 = warp tiles, 128 = CTA tiles, 32 = one warp per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")

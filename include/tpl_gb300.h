@@ -62,6 +62,9 @@ typedef struct tpl_options {
     int renormalize;           /* 0 = default (on), 1 = on, -1 = off: Newton-Schulz renormalisation
                                   of scan aggregates */
     int max_ctas;              /* cap on persistent CTAs; 0 = occupancy-derived */
+    int copy_buffers;          /* chunk buffers of tpl_a2b_backward_coords_f32: 0 = default (1),
+                                  1 = copy then evaluate, 2 = the next chunk's bulk copies in flight
+                                  while a chunk is evaluated (residues_per_thread 4 only) */
 } tpl_options;
 
 /* Human-readable text for a tpl_status value (host). */

@@ -410,7 +410,7 @@ def test_sincos_error_bound(built):
     assert np.abs(sv * sv + cv * cv - 1.0).max() <= 3e-7
 
 
-def run_gpu_coords_backward(rm, ang, lengths, g, rpt):
+def run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers=0):
     """Forward with the current options, then the backward from its coordinates."""
     dev = torch.device("cuda")
     a = torch.tensor(ang, dtype=torch.float32, device=dev)
@@ -420,7 +420,7 @@ def run_gpu_coords_backward(rm, ang, lengths, g, rpt):
     coords = torch.full((B, 9 * L), float("nan"), device=dev)
     rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
     gi = torch.full((B, 3, L), float("nan"), device=dev)
-    rm.set_backward_options(rpt)
+    rm.set_backward_options(rpt, buffers)
     try:
         rm.Angles2BackboneGPU_backward_coords(gi, torch.tensor(g, dtype=torch.float32, device=dev), coords, ln, ws)
     finally:
@@ -429,14 +429,15 @@ def run_gpu_coords_backward(rm, ang, lengths, g, rpt):
     return coords.double().cpu().numpy(), gi.double().cpu().numpy()
 
 
-@pytest.mark.parametrize("rpt", [4, 8])
+@pytest.mark.parametrize("rpt,buffers", [(4, 1), (4, 2), (8, 1)])
 @pytest.mark.parametrize("L", [1000, 1001, 258])
-def test_backward_from_coordinates_matches_oracle(rm, rpt, L):
+def test_backward_from_coordinates_matches_oracle(rm, rpt, buffers, L):
     """The float32 backward from the forward's output coordinates (bulk-copied chunk
-    rows when L % 4 == 0, plain loads otherwise) against the oracle."""
+    rows when L % 4 == 0, single or double buffered; plain loads otherwise) against
+    the oracle."""
     lens = [L, L - 1, 257, 256, 255, 129, 128, 127, 2, 1, 0]
     ang, lengths, g = make_case(len(lens), L, 500 + L + rpt, lengths=lens)
-    c, gi = run_gpu_coords_backward(rm, ang, lengths, g, rpt)
+    c, gi = run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers)
     rc, rg = oracle_ref(ang, lengths, g, True)
     check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
 

@@ -114,7 +114,8 @@ def sweep(ang, lengths, up, candidates=CANDIDATES, carry_thresholds=(0,), steps=
     return out
 
 
-COORDS_BWD_CANDIDATES = (4, 8)  # residues per lane of the backward from coordinates
+# backward from coordinates: (residues per lane, chunk buffers)
+COORDS_BWD_CANDIDATES = ((4, 1), (4, 2), (8, 1))
 
 
 def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, steps=5):
@@ -122,7 +123,7 @@ def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, st
     value (the forward runs once with the current options); returns a list of dicts
     with the gradient error against the FP64 form."""
     rm = load_extension("_ReducedModel")
-    saved = rm.get_backward_options()
+    saved = tuple(rm.get_backward_options())
     B, _, L = ang.shape
     ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=ang.device)
     coords = torch.empty(B, 9 * L, device=ang.device)
@@ -130,8 +131,8 @@ def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, st
     gang = torch.empty(B, 3, L, device=ang.device)
     out = []
     try:
-        for c in candidates:
-            rm.set_backward_options(c)
+        for c, nb in candidates:
+            rm.set_backward_options(c, nb)
             for _ in range(2):
                 rm.Angles2BackboneGPU_backward_coords(gang, up, coords, lengths, ws)
             e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -141,9 +142,10 @@ def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, st
             e[1].record()
             torch.cuda.synchronize(ang.device)
             _, _, grel = _errors(rm, ang, lengths, up, coords, gang)
-            out.append({"residues_per_thread": c, "bwd_ms": e[0].elapsed_time(e[1]) / steps, "grad_max_rel": grel})
+            out.append({"residues_per_thread": c, "copy_buffers": nb, "bwd_ms": e[0].elapsed_time(e[1]) / steps,
+                        "grad_max_rel": grel})
     finally:
-        rm.set_backward_options(saved)
+        rm.set_backward_options(*saved)
     return out
 
 
@@ -169,7 +171,8 @@ def tune(ang, lengths, up, use_cache=True, steps=5):
         if use_cache:
             _save_cache(cache)
     rm.set_options(best["residues_per_thread"], best["fp64_carry_min_len"], 0, 0, best["threads_per_cta"])
-    rm.set_backward_options(best["backward_coords"]["residues_per_thread"])
+    bc = best["backward_coords"]
+    rm.set_backward_options(bc["residues_per_thread"], bc.get("copy_buffers", 0))
     tune.last_sweep = rows
     tune.last_backward_sweep = brows
     return best

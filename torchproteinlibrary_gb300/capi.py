@@ -20,7 +20,7 @@ _sz = ctypes.c_size_t
 
 class tpl_options(ctypes.Structure):
     _fields_ = [("residues_per_thread", _i), ("threads_per_cta", _i), ("fp64_carry_min_len", _i),
-                ("renormalize", _i), ("max_ctas", _i)]
+                ("renormalize", _i), ("max_ctas", _i), ("copy_buffers", _i)]
 
 
 _SIGNATURES = {

@@ -101,6 +101,7 @@ void Angles2BackboneGPU_backward(torch::Tensor gradInput, torch::Tensor gradOutp
 // Not a reference entry point: the Python layer calls it with the coordinates it
 // saved; Angles2BackboneGPU_backward above keeps the reference's signature.
 int g_bwd_rpt = 0;  // residues per lane of the coordinate backward: 0 (= 4), 4 or 8
+int g_bwd_buffers = 0;  // chunk buffers of the coordinate backward: 0 (= 1), 1 or 2
 
 void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor gradOutput, torch::Tensor output_coords,
                                         torch::Tensor angles_length, torch::Tensor A) {
@@ -120,16 +121,20 @@ void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor g
     const at::cuda::CUDAGuard guard(gradInput.device());
     tpl_options o = g_opt;
     o.residues_per_thread = g_bwd_rpt;
+    o.copy_buffers = g_bwd_buffers;
     const int s = tpl_a2b_backward_coords_f32(gradInput.data_ptr<float>(), gradOutput.data_ptr<float>(),
                                               output_coords.data_ptr<float>(), angles_length.data_ptr<int32_t>(),
                                               A.data_ptr(), A.nbytes(), (int)B, (int)L, &o, stream_of(gradInput));
     check_status(s, "Angles2BackboneGPU_backward_coords");
 }
 
-void set_backward_options(int64_t residues_per_thread) {
+void set_backward_options(int64_t residues_per_thread, int64_t copy_buffers) {
     TORCH_CHECK(residues_per_thread == 0 || residues_per_thread == 4 || residues_per_thread == 8,
                 "residues_per_thread of the coordinate backward must be 0, 4 or 8");
+    TORCH_CHECK(copy_buffers >= 0 && copy_buffers <= 2 && !(copy_buffers == 2 && residues_per_thread == 8),
+                "copy_buffers of the coordinate backward must be 0, 1 or 2 (2 with 4 residues per lane)");
     g_bwd_rpt = (int)residues_per_thread;
+    g_bwd_buffers = (int)copy_buffers;
 }
 
 void no_cpu_path(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
@@ -152,7 +157,7 @@ int64_t workspace_status(torch::Tensor A) {
 void set_options(int64_t residues_per_thread, int64_t fp64_carry_min_len, int64_t renormalize, int64_t max_ctas,
                  int64_t threads_per_cta) {
     tpl_options o = {(int)residues_per_thread, (int)threads_per_cta, (int)fp64_carry_min_len, (int)renormalize,
-                     (int)max_ctas};
+                     (int)max_ctas, g_opt.copy_buffers};
     TORCH_CHECK(o.threads_per_cta == 0 || o.threads_per_cta == 128 || o.threads_per_cta == 32,
                 "threads_per_cta must be 0 (warp tiles), 128 (CTA tiles) or 32 (one warp per chain)");
     TORCH_CHECK(o.threads_per_cta != 32 || o.residues_per_thread == 0 || o.residues_per_thread == 4 ||
@@ -184,7 +189,9 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("get_options", &get_options, "current tuning knobs");
     m.def("Angles2BackboneGPU_backward_coords", &Angles2BackboneGPU_backward_coords,
           "float32 backward from the forward's output coordinates");
-    m.def("set_backward_options", &set_backward_options, "residues per lane of the coordinate backward",
-          py::arg("residues_per_thread") = 0);
-    m.def("get_backward_options", []() { return (int64_t)g_bwd_rpt; }, "residues per lane of the coordinate backward");
+    m.def("set_backward_options", &set_backward_options,
+          "residues per lane and chunk buffers of the coordinate backward", py::arg("residues_per_thread") = 0,
+          py::arg("copy_buffers") = 0);
+    m.def("get_backward_options", []() { return std::vector<int64_t>{g_bwd_rpt, g_bwd_buffers}; },
+          "residues per lane and chunk buffers of the coordinate backward");
 }

@@ -639,20 +639,25 @@ __device__ __forceinline__ void fetch_residue(const float *seg, float *buf, int 
         }
 }
 
-template <int C>
-__global__ void __launch_bounds__(32 * kWarpsPerCta, C >= 8 ? 3 : 5) a2b_bwd_coords_kernel(ChainArgs a) {
+constexpr int coords_min_blocks(int C, int NB) { return C * NB >= 16 ? 1 : (C * NB >= 8 ? 3 : 5); }
+
+// NB = 1: each chunk's copies are issued and waited for in turn.  NB = 2: two
+// buffer pairs; the copies of the next chunk are in flight while a chunk is
+// evaluated.
+template <int C, int NB>
+__global__ void __launch_bounds__(32 * kWarpsPerCta, coords_min_blocks(C, NB)) a2b_bwd_coords_kernel(ChainArgs a) {
     constexpr int CH = 32 * C, SEG = 9 * C;
     extern __shared__ __align__(16) float s_dyn[];
-    __shared__ __align__(8) uint64_t s_bar[kWarpsPerCta];
+    __shared__ __align__(8) uint64_t s_bar[kWarpsPerCta][NB];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x * kWarpsPerCta + w;
     if (b >= a.B) return;  // warps are independent
-    float *sx = s_dyn + w * 64 * SEG;  // coordinates of the chunk, contiguous as in the row
-    float *sg = sx + 32 * SEG;         // dL/dx of the chunk
-    const float *xs = sx + lane * SEG, *gs = sg + lane * SEG;
-    uint64_t *bar = &s_bar[w];
+    // per buffer: coordinates of a chunk (contiguous as in the row), then its dL/dx
+    float *sbase = s_dyn + (size_t)w * NB * 64 * SEG;
+    uint64_t *bars = s_bar[w];
     const bool vec = a.vec != 0;
-    if (vec && lane == 0) mbar_init(bar);
+    if (vec && lane == 0)
+        for (int i = 0; i < NB; i++) mbar_init(&bars[i]);
     __syncwarp();
     const int len = checked_length(a, b, lane);
     const float *xin = a.coords + (size_t)b * 9 * a.L;
@@ -666,20 +671,36 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, C >= 8 ? 3 : 5) a2b_bwd_coo
 
     float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, oc[3] = {0.f, 0.f, 0.f};  // sums after the chunk
     float nN[3] = {0.f, 0.f, 0.f};  // N of the first residue after the chunk (world)
-    unsigned phase = 0;
-    for (int k = nchunk - 1; k >= 0; k--) {
+    // chunk kk into buffer q: whole residues up to a multiple of 4 (inside the row
+    // since L % 4 == 0), by lane 0
+    auto issue = [&](int kk, int q) {
+        if (lane == 0) {
+            const int n4 = (min(CH, len - kk * CH) + 3) & ~3;
+            float *bx = sbase + (size_t)q * 64 * SEG;
+            bulk_load_pair(bx, xin + (size_t)9 * kk * CH, bx + 32 * SEG, gin + (size_t)9 * kk * CH, 36u * (unsigned)n4,
+                           &bars[q]);
+        }
+    };
+    unsigned parity = 0;  // bit q: parity of buffer q's pending phase
+    if (vec && NB == 2 && nchunk > 0) issue(nchunk - 1, 0);
+    for (int k = nchunk - 1, it = 0; k >= 0; k--, it++) {
         const int s0 = k * CH;
         const int nreal = min(CH, len - s0);
-        __syncwarp();  // the previous chunk's reads of both buffers are done
+        const int q = NB == 2 ? (it & 1) : 0;
+        float *sx = sbase + (size_t)q * 64 * SEG;
+        float *sg = sx + 32 * SEG;
+        const float *xs = sx + lane * SEG, *gs = sg + lane * SEG;
+        __syncwarp();  // the previous chunk's reads of its buffers are done
         if (vec) {
-            // whole residues up to a multiple of 4 (inside the row since L % 4 == 0)
-            const unsigned bytes = 36u * (unsigned)((nreal + 3) & ~3);
-            if (lane == 0) bulk_load_pair(sx, xin + (size_t)9 * s0, sg, gin + (size_t)9 * s0, bytes, bar);
-            const bool ok = mbar_wait(bar, phase);
-            phase ^= 1u;
+            if (NB == 1) issue(k, 0);
+            else if (k > 0) issue(k - 1, q ^ 1);  // prefetch: the other buffer held the previous chunk
+            const bool ok = mbar_wait(&bars[q], (parity >> q) & 1u);
+            parity ^= 1u << q;
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) record_error(a.hdr, TPL_ERR_LOOKBACK_TIMEOUT);
-                (void)mbar_wait(bar, phase ^ 1u);  // bounded: let the copies in flight land before exiting
+                // bounded: let the copies in flight land before exiting
+                (void)mbar_wait(&bars[q], ((parity >> q) & 1u) ^ 1u);
+                if (NB == 2 && k > 0) (void)mbar_wait(&bars[q ^ 1], (parity >> (q ^ 1)) & 1u);
                 return;
             }
         } else {
@@ -939,12 +960,12 @@ int a2b_backward_coords(float *grad_angles, const float *grad_coords, const floa
     a.grad_coords = grad_coords;
     a.vec = (L % 4 == 0) && aligned16(coords) && aligned16(grad_angles) && aligned16(grad_coords);
     const int C = opt.residues_per_thread > 0 ? opt.residues_per_thread : 4;
+    const int NB = opt.copy_buffers > 0 ? opt.copy_buffers : 1;
     constexpr int smem4 = kWarpsPerCta * 64 * 36 * (int)sizeof(float);
     constexpr int smem8 = kWarpsPerCta * 64 * 72 * (int)sizeof(float);
-    switch (C) {
-        case 4: return launch_chain(a2b_bwd_coords_kernel<4>, smem4, B, a, st);
-        case 8: return launch_chain(a2b_bwd_coords_kernel<8>, smem8, B, a, st);
-    }
+    if (C == 4 && NB == 1) return launch_chain(a2b_bwd_coords_kernel<4, 1>, smem4, B, a, st);
+    if (C == 4 && NB == 2) return launch_chain(a2b_bwd_coords_kernel<4, 2>, 2 * smem4, B, a, st);
+    if (C == 8 && NB == 1) return launch_chain(a2b_bwd_coords_kernel<8, 1>, smem8, B, a, st);
     return TPL_ERR_UNSUPPORTED;
 }
 

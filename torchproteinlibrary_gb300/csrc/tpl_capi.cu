@@ -92,6 +92,7 @@ bool options_ok(const tpl_options &o) {
     if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128 || o.threads_per_cta == 32)) return false;
     if (o.threads_per_cta == 32 && !(r == 0 || r == 4 || r == 8)) return false;
     if (o.max_ctas < 0) return false;
+    if (o.copy_buffers < 0 || o.copy_buffers > 2) return false;
     return true;
 }
 
@@ -191,6 +192,8 @@ int tpl_a2b_backward_coords_f32(float *grad_angles, const float *grad_coords, co
     if (batch < 0 || max_len < 0) return TPL_ERR_ARGUMENT;
     const tpl_options o = resolve(opt);
     if (!(o.residues_per_thread == 0 || o.residues_per_thread == 4 || o.residues_per_thread == 8))
+        return TPL_ERR_ARGUMENT;
+    if (o.copy_buffers < 0 || o.copy_buffers > 2 || (o.copy_buffers == 2 && o.residues_per_thread == 8))
         return TPL_ERR_ARGUMENT;
     if (batch == 0 || max_len == 0) return TPL_OK;
     if (!grad_angles || !grad_coords || !coords || !lengths) return TPL_ERR_ARGUMENT;
