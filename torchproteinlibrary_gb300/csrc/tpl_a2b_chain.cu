@@ -91,6 +91,44 @@ __device__ __forceinline__ void sincos_fast(float a, float *s, float *c) {
     *c = cc;
 }
 
+// Two angles at once with the paired FP32 instructions of sm_100+ (FFMA2 / FMUL2:
+// two lanes of arithmetic per issue).  Same method as sincos_fast, except that the
+// reduction rounds with the 1.5 * 2^23 shift: t = a * 2/pi + 1.5 * 2^23 rounds to an
+// integer in the FMA, k = t - 1.5 * 2^23 exactly, and the low bits of t's pattern
+// are k mod 4, so no float-to-integer conversion is needed.  Valid for |a| <= 1e4.
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+
+__device__ __forceinline__ void quadrant(float sr, float cr, int t_bits, float *s, float *c) {
+    const int q = t_bits & 3;  // a = r + q pi/2 (mod 2 pi)
+    float ss = (q & 1) ? cr : sr;
+    float cc = (q & 1) ? sr : cr;
+    ss = __int_as_float(__float_as_int(ss) ^ ((q & 2) << 30));
+    cc = __int_as_float(__float_as_int(cc) ^ (((q + 1) & 2) << 30));
+    *s = ss;
+    *c = cc;
+}
+
+__device__ __forceinline__ void sincos_fast2(float a0, float a1, float *s0, float *c0, float *s1, float *c1) {
+    constexpr float kShift = 12582912.0f;  // 1.5 * 2^23
+    const float2 a = make_float2(a0, a1);
+    const float2 t = __ffma2_rn(a, f2(0.636619772367581343f), f2(kShift));
+    const float2 k = __fadd2_rn(t, f2(-kShift));
+    float2 r = __ffma2_rn(k, f2(-1.57079637050628662f), a);
+    r = __ffma2_rn(k, f2(4.37113900018624283e-8f), r);
+    const float2 r2 = __fmul2_rn(r, r);
+    float2 ps = __ffma2_rn(r2, f2(2.7557319223985891e-6f), f2(-1.9841269841269841e-4f));
+    ps = __ffma2_rn(ps, r2, f2(8.3333333333333333e-3f));
+    ps = __ffma2_rn(ps, r2, f2(-1.6666666666666667e-1f));
+    const float2 sr = __ffma2_rn(__fmul2_rn(ps, r2), r, r);
+    float2 pc = __ffma2_rn(r2, f2(-2.7557319223985891e-7f), f2(2.4801587301587302e-5f));
+    pc = __ffma2_rn(pc, r2, f2(-1.3888888888888889e-3f));
+    pc = __ffma2_rn(pc, r2, f2(4.1666666666666667e-2f));
+    pc = __ffma2_rn(pc, r2, f2(-0.5f));
+    const float2 cr = __ffma2_rn(pc, r2, f2(1.0f));
+    quadrant(sr.x, cr.x, __float_as_int(t.x), s0, c0);
+    quadrant(sr.y, cr.y, __float_as_int(t.y), s1, c1);
+}
+
 __device__ __forceinline__ void sincos_poly(float a, float *s, float *c) {
     if (fabsf(a) > 1.0e4f) {
         sincosf(a, s, c);
@@ -153,13 +191,18 @@ template <bool FAST>
 __device__ __forceinline__ void walk4(const BondConsts &bc, Frame<float> &f, const float (&a0)[4],
                                       const float (&a1)[4], const float (&a2)[4], float *seg) {
     float buf[36];
+    float so[4], co[4];  // omega pairs (residues 0-1, 2-3)
+    if (FAST) {
+        sincos_fast2(a2[0], a2[1], &so[0], &co[0], &so[1], &co[1]);
+        sincos_fast2(a2[2], a2[3], &so[2], &co[2], &so[3], &co[3]);
+    }
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         float s0, c0, s1, c1, s2, c2;
         if (FAST) {
-            sincos_fast(a0[r], &s0, &c0);
-            sincos_fast(a1[r], &s1, &c1);
-            sincos_fast(a2[r], &s2, &c2);
+            sincos_fast2(a0[r], a1[r], &s0, &c0, &s1, &c1);
+            s2 = so[r];
+            c2 = co[r];
         } else {
             sincos_poly(a0[r], &s0, &c0);
             sincos_poly(a1[r], &s1, &c1);
@@ -879,9 +922,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, coords_min_blocks(C, NB)) a
 }
 
 // Sincos check kernel for the tests: s[i], c[i] = sincos_poly(a[i]).
+// Even elements through the paired form (the kernels' fast path), odd elements
+// through sincos_poly; |a| > 1e4 always through sincos_poly.
 __global__ void sincos_poly_kernel(const float *a, float *s, float *c, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) sincos_poly(a[i], s + i, c + i);
+    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    const float x0 = a[i], x1 = i + 1 < n ? a[i + 1] : 0.f;
+    if (fabsf(x0) <= 1.0e4f && fabsf(x1) <= 1.0e4f) {
+        float s1, c1;
+        sincos_fast2(x0, x1, s + i, c + i, &s1, &c1);
+        if (i + 1 < n) {
+            sincos_poly(x1, s + i + 1, c + i + 1);
+        }
+    } else {
+        sincos_poly(x0, s + i, c + i);
+        if (i + 1 < n) sincos_poly(x1, s + i + 1, c + i + 1);
+    }
 }
 
 template <int C>
@@ -971,7 +1027,7 @@ int a2b_backward_coords(float *grad_angles, const float *grad_coords, const floa
 
 int sincos_poly_f32(const float *a, float *s, float *c, int n, cudaStream_t st) {
     if (n <= 0) return TPL_OK;
-    sincos_poly_kernel<<<(n + 255) / 256, 256, 0, st>>>(a, s, c, n);
+    sincos_poly_kernel<<<((n + 1) / 2 + 255) / 256, 256, 0, st>>>(a, s, c, n);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
