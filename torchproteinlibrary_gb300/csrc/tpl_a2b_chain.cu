@@ -184,6 +184,56 @@ __device__ __forceinline__ void load4(const float *row, int j, int len, bool vec
     }
 }
 
+// A frame with rows 0 and 1 held as pairs (one paired-FP32 instruction updates both
+// rows) and row 2 as scalars: c[j] = (R[0][j], R[1][j]), r2[j] = R[2][j].
+struct PairFrame {
+    float2 c[3];
+    float r2[3];
+    float2 p;
+    float p2;
+};
+
+__device__ __forceinline__ PairFrame to_pair(const Frame<float> &f) {
+    PairFrame g;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        g.c[j] = make_float2(f.r[j], f.r[3 + j]);
+        g.r2[j] = f.r[6 + j];
+    }
+    g.p = make_float2(f.p[0], f.p[1]);
+    g.p2 = f.p[2];
+    return g;
+}
+__device__ __forceinline__ void from_pair(const PairFrame &g, Frame<float> &f) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        f.r[j] = g.c[j].x;
+        f.r[3 + j] = g.c[j].y;
+        f.r[6 + j] = g.r2[j];
+    }
+    f.p[0] = g.p.x;
+    f.p[1] = g.p.y;
+    f.p[2] = g.p2;
+}
+
+// apply_joint (tpl_common.cuh) on a PairFrame: 9 paired and 9 scalar operations.
+__device__ __forceinline__ void apply_joint_pair(PairFrame &f, float cb, float sb, float d, float ca, float sa) {
+    const float2 c0 = f.c[0], c1 = f.c[1], c2 = f.c[2];
+    const float2 n0 = __ffma2_rn(c0, f2(cb), __fmul2_rn(c2, f2(-sb)));
+    const float2 n2 = __ffma2_rn(c0, f2(sb), __fmul2_rn(c2, f2(cb)));
+    f.p = __ffma2_rn(f2(d), n0, f.p);
+    f.c[0] = n0;
+    f.c[1] = __ffma2_rn(c1, f2(ca), __fmul2_rn(n2, f2(sa)));
+    f.c[2] = __ffma2_rn(n2, f2(ca), __fmul2_rn(c1, f2(-sa)));
+    const float e0 = f.r2[0], e1 = f.r2[1], e2 = f.r2[2];
+    const float m0 = fmaf(e0, cb, -e2 * sb);
+    const float m2 = fmaf(e0, sb, e2 * cb);
+    f.p2 = fmaf(d, m0, f.p2);
+    f.r2[0] = m0;
+    f.r2[1] = fmaf(e1, ca, m2 * sa);
+    f.r2[2] = fmaf(m2, ca, -e1 * sa);
+}
+
 // Four residues of a lane's walk: composes their 12 joints onto f and writes the
 // lane-local N, CA, C positions (36 floats, 9 float4s) to seg.  FAST: every angle
 // is known to be within the range of sincos_fast.
@@ -191,19 +241,34 @@ template <bool FAST>
 __device__ __forceinline__ void walk4(const BondConsts &bc, Frame<float> &f, const float (&a0)[4],
                                       const float (&a1)[4], const float (&a2)[4], float *seg) {
     float buf[36];
-    float so[4], co[4];  // omega pairs (residues 0-1, 2-3)
     if (FAST) {
+        float so[4], co[4];  // omega pairs (residues 0-1, 2-3)
         sincos_fast2(a2[0], a2[1], &so[0], &co[0], &so[1], &co[1]);
         sincos_fast2(a2[2], a2[3], &so[2], &co[2], &so[3], &co[3]);
+        PairFrame g = to_pair(f);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            float s0, c0, s1, c1;
+            sincos_fast2(a0[r], a1[r], &s0, &c0, &s1, &c1);
+            buf[9 * r] = g.p.x; buf[9 * r + 1] = g.p.y; buf[9 * r + 2] = g.p2;
+            apply_joint_pair(g, bc.cb[0], bc.sb[0], bc.d[0], c0, s0);
+            buf[9 * r + 3] = g.p.x; buf[9 * r + 4] = g.p.y; buf[9 * r + 5] = g.p2;
+            apply_joint_pair(g, bc.cb[1], bc.sb[1], bc.d[1], c1, s1);
+            buf[9 * r + 6] = g.p.x; buf[9 * r + 7] = g.p.y; buf[9 * r + 8] = g.p2;
+            apply_joint_pair(g, bc.cb[2], bc.sb[2], bc.d[2], co[r], so[r]);
+#pragma unroll
+            for (int q = 0; q < 9; q++)  // flush the float4s this residue completed
+                if (4 * q + 3 <= 9 * r + 8 && 4 * q + 3 > 9 * r - 1)
+                    *reinterpret_cast<float4 *>(seg + 4 * q) =
+                        make_float4(buf[4 * q], buf[4 * q + 1], buf[4 * q + 2], buf[4 * q + 3]);
+        }
+        from_pair(g, f);
+        return;
     }
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         float s0, c0, s1, c1, s2, c2;
-        if (FAST) {
-            sincos_fast2(a0[r], a1[r], &s0, &c0, &s1, &c1);
-            s2 = so[r];
-            c2 = co[r];
-        } else {
+        {
             sincos_poly(a0[r], &s0, &c0);
             sincos_poly(a1[r], &s1, &c1);
             sincos_poly(a2[r], &s2, &c2);
