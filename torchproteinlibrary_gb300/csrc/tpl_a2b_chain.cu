@@ -423,7 +423,7 @@ __device__ __forceinline__ int checked_length(const ChainArgs &a, int b, int lan
     return len;
 }
 
-constexpr int fwd_min_blocks(int C) { return C >= 8 ? 5 : 6; }
+constexpr int fwd_min_blocks(int C) { return C >= 8 ? 5 : 7; }
 constexpr int bwd_min_blocks(int C) { return C >= 8 ? 2 : 4; }
 
 template <int C>
