@@ -451,6 +451,33 @@ def time_a2c(dev, steps=10, seed=1004):
     maxA = max(na)
     res = {}
     outs = {}
+    # threads per chain of the float32 kernels: time each, keep the fastest
+    sweep = []
+    for nt in (128, 256, 512):
+        fm.set_options(nt)
+        a = ang.contiguous()
+        c = torch.empty(B, 3 * maxA, device=dev)
+        ga = torch.empty_like(a)
+        gup0 = torch.ones(B, 3 * maxA, device=dev)
+        for _ in range(2):
+            fm.Angles2Coords_forward(seq, a, c, torch.empty(0, dtype=torch.uint8, device=dev),
+                                     torch.empty(0, dtype=torch.uint8, device=dev))
+            fm.Angles2Coords_backward(gup0, ga, seq, a)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        for _ in range(steps):
+            fm.Angles2Coords_forward(seq, a, c, torch.empty(0, dtype=torch.uint8, device=dev),
+                                     torch.empty(0, dtype=torch.uint8, device=dev))
+        e[1].record()
+        for _ in range(steps):
+            fm.Angles2Coords_backward(gup0, ga, seq, a)
+        e[2].record()
+        torch.cuda.synchronize(dev)
+        sweep.append({"threads_per_cta": nt, "fwd_ms": e[0].elapsed_time(e[1]) / steps,
+                      "bwd_ms": e[1].elapsed_time(e[2]) / steps})
+    best_nt = min(sweep, key=lambda r: r["fwd_ms"] + r["bwd_ms"])["threads_per_cta"]
+    fm.set_options(best_nt)
+    res["threads_per_chain_sweep"] = sweep
     for name, dt in (("f32", torch.float32), ("f64", torch.float64)):
         a = ang.to(dt)
         c = torch.empty(B, 3 * maxA, dtype=dt, device=dev)
@@ -493,6 +520,7 @@ def time_training_step(dev, steps=10, seed=1004):
     backward through both, all through the public autograd layers, inputs resident.
     FP32 batched kernels vs FP64 kernels, with the FP32 gradient's error against FP64."""
     import torch
+    from torchproteinlibrary_gb300 import load_extension
     from torchproteinlibrary_gb300.FullAtomModel import Angles2Coords
     from torchproteinlibrary_gb300.RMSD import Coords2RMSD
 
@@ -533,6 +561,51 @@ def time_training_step(dev, steps=10, seed=1004):
         ms = e0.elapsed_time(e1) / n
         res[name] = {"residues_per_s": float(lens.sum()) / (ms / 1e3), "ms_per_step": ms, "loss": float(loss)}
         grads[name] = x.grad.double()
+        # the same four launches (Angles2Coords forward, Coords2RMSD forward with
+        # centring, their backwards with dL/drmsd = 1/B) through the extension entry
+        # points, captured once in a CUDA graph and replayed: the step's device time
+        fm = load_extension("_FullAtomModel")
+        rm_ = load_extension("_RMSD")
+        seq = a2c._prepare(seqs, dev)[0]
+        xd = x.detach()
+        maxA = target.shape[1] // 3
+        c = torch.empty(B, 3 * maxA, dtype=dt, device=dev)
+        e_u8 = torch.empty(0, dtype=torch.uint8, device=dev)
+        out = torch.empty(B, dtype=dt, device=dev)
+        UT = torch.empty(B, 3, 3, dtype=dt, device=dev)
+        cent = torch.empty(B, 6, dtype=torch.float64, device=dev)
+        g_r = torch.full((B,), 1.0 / B, dtype=dt, device=dev)
+        g_c = torch.empty_like(c)
+        g_a = torch.empty_like(xd)
+
+        def raw_step():
+            fm.Angles2Coords_forward(seq, xd, c, e_u8, e_u8)
+            rm_.Coords2RMSDGPU_forward_centering(c, target, out, na, UT, cent)
+            rm_.Coords2RMSDGPU_backward(g_r, c, target, na, out, UT, cent, g_c, 1)
+            fm.Angles2Coords_backward(g_c, g_a, seq, xd)
+
+        st_ = torch.cuda.Stream(device=dev)
+        st_.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(st_):
+            for _ in range(3):
+                raw_step()
+        torch.cuda.current_stream(dev).wait_stream(st_)
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            raw_step()
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        e0.record()
+        for _ in range(n):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        gms = e0.elapsed_time(e1) / n
+        res[name]["graph_ms_per_step"] = gms
+        res[name]["graph_residues_per_s"] = float(lens.sum()) / (gms / 1e3)
+        res[name]["graph_grad_max_rel_vs_eager"] = float((g_a.double() - grads[name]).abs().max() /
+                                                         grads[name].abs().max())
     res["batched_vs_fp64"] = res["f32"]["residues_per_s"] / res["f64"]["residues_per_s"]
     res["grad_max_rel_f32_vs_f64"] = float((grads["f32"] - grads["f64"]).abs().max() / grads["f64"].abs().max())
     res["workload"] = ("training step: Angles2Coords + Coords2RMSD loss (mean) fwd+bwd, 256 chains x U{50..500} "

@@ -155,7 +155,9 @@ size_t tpl_a2c_workspace_bytes(int batch, int max_len, int max_atoms, const tpl_
  *   res_names, atom_names  [batch, max_atoms, 4] uint8 NUL-padded names, or both NULL
  *              to skip them (they depend on the sequences only)
  * Unknown letters, chains longer than max_len or with more than max_atoms atoms are
- * reported through the workspace status; such chains are zeroed. */
+ * reported through the workspace status; such chains are zeroed.  One CTA walks a
+ * chain: opt->threads_per_cta 0 or 256 (the default) or 512 threads with one residue
+ * each, or 128 threads with two residues each (float32; float64 always uses 128 x 1). */
 int tpl_a2c_forward_f32(const uint8_t *sequences, int seq_stride, const float *angles, float *coords,
                         uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes, int batch,
                         int max_len, int max_atoms, const tpl_options *opt, void *stream);

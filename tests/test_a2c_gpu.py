@@ -69,8 +69,9 @@ def test_golden_fp64(fm):
     check(c, gi, d["coords"], d["grad_angles"], na, COORD_TOL_F64, GRAD_TOL_F64)
 
 
-@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
-def test_random_batch_matches_oracle(fm, dtype):
+@pytest.mark.parametrize("dtype,threads", [(torch.float32, 0), (torch.float32, 128), (torch.float32, 512),
+                                           (torch.float64, 0)])
+def test_random_batch_matches_oracle(fm, dtype, threads):
     rng = np.random.default_rng(31)
     seqs = ["".join(rng.choice(list(AA), rng.integers(1, 300))) for _ in range(7)] + ["G", "P", "W", AA]
     L = 300
@@ -87,7 +88,11 @@ def test_random_batch_matches_oracle(fm, dtype):
     else:
         a_ref = ang
     rg = oracle.a2c_backward(g, a_ref, seqs)
-    c, rn, an, na2, gi = run_gpu(fm, ang, seqs, g, dtype)
+    fm.set_options(threads)
+    try:
+        c, rn, an, na2, gi = run_gpu(fm, ang, seqs, g, dtype)
+    finally:
+        fm.set_options(0)
     np.testing.assert_array_equal(rn, rrn)
     np.testing.assert_array_equal(an, ran)
     tol = (COORD_TOL_F32, GRAD_TOL_F32) if dtype == torch.float32 else (COORD_TOL_F64, GRAD_TOL_F64)
@@ -249,5 +254,10 @@ def test_config4_ragged_fp32_vs_fp64(fm):
     c64, _, _, na, _ = run_gpu(fm, ang, seqs, None, torch.float64)
     g = rng.standard_normal(c64.shape).astype(np.float32).astype(np.float64)
     c64, _, _, _, g64 = run_gpu(fm, ang, seqs, g, torch.float64)
-    c32, _, _, _, g32 = run_gpu(fm, ang, seqs, g, torch.float32)
-    check(c32, g32, c64, g64, na, COORD_TOL_F32, GRAD_TOL_F32)
+    for threads in (0, 128, 512):
+        fm.set_options(threads)
+        try:
+            c32, _, _, _, g32 = run_gpu(fm, ang, seqs, g, torch.float32)
+        finally:
+            fm.set_options(0)
+        check(c32, g32, c64, g64, na, COORD_TOL_F32, GRAD_TOL_F32)

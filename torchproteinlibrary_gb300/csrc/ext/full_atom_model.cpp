@@ -28,6 +28,9 @@
 
 namespace {
 
+// Tuning knobs of the Angles2Coords kernels (threads_per_cta 0 / 256, 512 or 128).
+tpl_options g_a2c_opt = {};
+
 void check_status(int s, const char *what) {
     TORCH_CHECK(s == TPL_OK, what, ": ", tpl_status_string(s), " (", s, ")");
 }
@@ -88,11 +91,11 @@ void Angles2Coords_forward(torch::Tensor sequences, torch::Tensor input_angles, 
     if (input_angles.scalar_type() == torch::kFloat) {
         s = tpl_a2c_forward_f32(seq.data_ptr<uint8_t>(), (int)seq.size(1), input_angles.data_ptr<float>(),
                                 output_coords.data_ptr<float>(), rn, an, ws.data_ptr(), ws.nbytes(), (int)B, (int)L,
-                                (int)maxA, nullptr, st);
+                                (int)maxA, &g_a2c_opt, st);
     } else if (input_angles.scalar_type() == torch::kDouble) {
         s = tpl_a2c_forward_f64(seq.data_ptr<uint8_t>(), (int)seq.size(1), input_angles.data_ptr<double>(),
                                 output_coords.data_ptr<double>(), rn, an, ws.data_ptr(), ws.nbytes(), (int)B, (int)L,
-                                (int)maxA, nullptr, st);
+                                (int)maxA, &g_a2c_opt, st);
     } else {
         TORCH_CHECK(false, "input_angles must be float32 or float64");
     }
@@ -122,11 +125,11 @@ void Angles2Coords_backward(torch::Tensor grad_atoms, torch::Tensor grad_angles,
     if (input_angles.scalar_type() == torch::kFloat) {
         s = tpl_a2c_backward_f32(grad_angles.data_ptr<float>(), grad_atoms.data_ptr<float>(), seq.data_ptr<uint8_t>(),
                                  (int)seq.size(1), input_angles.data_ptr<float>(), ws.data_ptr(), ws.nbytes(), (int)B,
-                                 (int)L, (int)maxA, nullptr, st);
+                                 (int)L, (int)maxA, &g_a2c_opt, st);
     } else if (input_angles.scalar_type() == torch::kDouble) {
         s = tpl_a2c_backward_f64(grad_angles.data_ptr<double>(), grad_atoms.data_ptr<double>(),
                                  seq.data_ptr<uint8_t>(), (int)seq.size(1), input_angles.data_ptr<double>(),
-                                 ws.data_ptr(), ws.nbytes(), (int)B, (int)L, (int)maxA, nullptr, st);
+                                 ws.data_ptr(), ws.nbytes(), (int)B, (int)L, (int)maxA, &g_a2c_opt, st);
     } else {
         TORCH_CHECK(false, "input_angles must be float32 or float64");
     }
@@ -471,6 +474,17 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Coords2Center_backward", &no_cpu_center, "not available: no CPU path");
     m.def("getBBox", &getBBox, "per-chain bounding box (GPU)");
     m.def("PDB2CoordsUnordered", &PDB2CoordsUnordered, "Convert PDB to coordinates in the PDB order");
+    m.def(
+        "set_options",
+        [](int64_t threads_per_cta) {
+            TORCH_CHECK(threads_per_cta == 0 || threads_per_cta == 128 || threads_per_cta == 256 ||
+                            threads_per_cta == 512,
+                        "threads_per_cta of Angles2Coords must be 0, 128, 256 or 512");
+            g_a2c_opt.threads_per_cta = (int)threads_per_cta;
+        },
+        "Angles2Coords float32 kernels: threads per chain (0 = 256; 256 or 512 = 1 residue each; 128 = 2 each)",
+        py::arg("threads_per_cta") = 0);
+    m.def("get_options", []() { return (int64_t)g_a2c_opt.threads_per_cta; }, "Angles2Coords threads per chain");
     m.def("Coords2TypedCoords_forward", &Coords2TypedCoords_forward, "Coords2TypedCoords forward (GPU)");
     m.def("Coords2TypedCoords_backward", &Coords2TypedCoords_backward, "Coords2TypedCoords backward (GPU)");
     m.def("Angles2Coords_forward", &Angles2Coords_forward, "Angles2Coords forward");

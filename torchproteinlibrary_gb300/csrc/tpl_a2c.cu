@@ -640,7 +640,13 @@ int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *
     }
     A2cArgs<float> a{seq, seq_stride, (const float *)angles, (float *)coords, res_names, atom_names,
                      nullptr, nullptr, (WsHeader *)ws, L, maxA};
-    return launch_a2c_fwd<float, 2, 128>(a, B, renorm, st);
+    // threads_per_cta: 128 = 128 threads x 2 residues; 0 / 256 (default) or 512 = one
+    // residue per thread
+    switch (opt.threads_per_cta) {
+        case 128: return launch_a2c_fwd<float, 2, 128>(a, B, renorm, st);
+        case 512: return launch_a2c_fwd<float, 1, 512>(a, B, renorm, st);
+    }
+    return launch_a2c_fwd<float, 1, 256>(a, B, renorm, st);
 }
 
 int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const unsigned char *seq, int seq_stride,
@@ -654,7 +660,11 @@ int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const uns
     }
     A2cArgs<float> a{seq, seq_stride, (const float *)angles, nullptr, nullptr, nullptr, (float *)grad_angles,
                      (const float *)grad_coords, (WsHeader *)ws, L, maxA};
-    return launch_a2c_bwd<float, 2, 128>(a, B, renorm, st);
+    switch (opt.threads_per_cta) {
+        case 128: return launch_a2c_bwd<float, 2, 128>(a, B, renorm, st);
+        case 512: return launch_a2c_bwd<float, 1, 512>(a, B, renorm, st);
+    }
+    return launch_a2c_bwd<float, 1, 256>(a, B, renorm, st);
 }
 
 int num_atoms_host(const char *seq) {

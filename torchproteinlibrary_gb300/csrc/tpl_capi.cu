@@ -234,12 +234,17 @@ size_t tpl_a2c_workspace_bytes(int batch, int max_len, int max_atoms, const tpl_
     return sizeof(WsHeader);
 }
 
+// Angles2Coords reads only threads_per_cta (0 / 128, 256 or 512) and renormalize.
+static bool a2c_options_ok(const tpl_options &o) {
+    return o.threads_per_cta == 0 || o.threads_per_cta == 128 || o.threads_per_cta == 256 || o.threads_per_cta == 512;
+}
+
 static int a2c_fwd_common(bool f64, const uint8_t *sequences, int seq_stride, const void *angles, void *coords,
                           uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes,
                           int batch, int max_len, int max_atoms, const tpl_options *opt, void *stream) {
     if (batch < 0 || max_len < 0 || max_atoms < 0 || seq_stride <= 0) return TPL_ERR_ARGUMENT;
     const tpl_options o = resolve(opt);
-    if (!options_ok(o)) return TPL_ERR_ARGUMENT;
+    if (!a2c_options_ok(o)) return TPL_ERR_ARGUMENT;
     if (batch == 0) return TPL_OK;
     if (!sequences || (!angles && max_len > 0) || (!coords && max_atoms > 0)) return TPL_ERR_ARGUMENT;
     if ((res_names == nullptr) != (atom_names == nullptr)) return TPL_ERR_ARGUMENT;
@@ -255,7 +260,7 @@ static int a2c_bwd_common(bool f64, void *grad_angles, const void *grad_coords, 
                           int max_len, int max_atoms, const tpl_options *opt, void *stream) {
     if (batch < 0 || max_len < 0 || max_atoms < 0 || seq_stride <= 0) return TPL_ERR_ARGUMENT;
     const tpl_options o = resolve(opt);
-    if (!options_ok(o)) return TPL_ERR_ARGUMENT;
+    if (!a2c_options_ok(o)) return TPL_ERR_ARGUMENT;
     if (batch == 0) return TPL_OK;
     if (!sequences || ((!angles || !grad_angles) && max_len > 0) || (!grad_coords && max_atoms > 0))
         return TPL_ERR_ARGUMENT;

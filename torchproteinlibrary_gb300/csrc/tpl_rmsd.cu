@@ -6,9 +6,12 @@
 // Python loop of .item() calls (TorchProteinLibrary/RMSD/Coords2RMSD/Coords2RMSD.py:40-62).
 //
 // Here one CTA per chain does everything in one launch: optional centring, the
-// correlation R_ab = sum x_a y_b and R2 = sum |x|^2 + |y|^2 accumulated in FP64,
-// the 4x4 matrix T (same layout as the reference), its largest eigenpair by cyclic
-// Jacobi rotations in FP64 on one thread, U from the unit quaternion, UT = U^T and
+// correlation R_ab = sum x_a y_b and R2 = sum |x|^2 + |y|^2 (per-thread partial sums
+// in the coordinate type, about N / 256 atoms each, reduced across the block in
+// FP64: GB300's FP64 rate is a small fraction of its FP32 rate),
+// the 4x4 matrix T (same layout as the reference), its largest eigenpair by the
+// characteristic-polynomial method on one warp in FP64 (key_eigen_warp), U from the
+// unit quaternion, UT = U^T and
 // rmsd = sqrt((R2 - 2 |lambda_max| + 1e-10) / N).  The backward is one launch:
 // dL/dx_i = g (x_i - UT y_i) / (rmsd N) on the centred coordinates.
 #include <cmath>
@@ -46,45 +49,77 @@ __device__ __forceinline__ double block_sum(double v, double *s_red) {
     return r;
 }
 
-// Largest eigenpair of a symmetric 4x4 matrix by cyclic Jacobi rotations
-// (Golub & Van Loan, Matrix Computations, 8.5).  a is destroyed.
-__device__ void jacobi4_max(double a[4][4], double &lam, double q[4]) {
-    double v[4][4];
+__device__ __forceinline__ double det3(double a, double b, double c, double d, double e, double f, double g, double h,
+                                       double k) {
+    return a * (e * k - f * h) - b * (d * k - f * g) + c * (d * h - e * g);
+}
+
+// Largest eigenpair of the 4x4 key matrix K (symmetric and traceless) by its
+// characteristic polynomial, as in Theobald's quaternion-characteristic-polynomial
+// method (Acta Cryst. A61, 478, 2005): det(K - l I) = l^4 + c2 l^2 + c1 l + c0 with,
+// by Newton's identities for a traceless matrix, c2 = -tr(K^2)/2, c1 = -tr(K^3)/3,
+// c0 = det K.  Newton's method from e0 >= l_max (e0 = (sum |x|^2 + |y|^2) / 2)
+// descends monotonically to the largest root.  The eigenvector is the largest row
+// of the cofactor matrix of K - l_max I (rank one for a simple root), one cofactor
+// per lane.  Executed by a full warp; every lane returns lam and the unit q (q = 1, 0,
+// 0, 0 when every cofactor vanishes).
+__device__ void key_eigen_warp(const double (&K)[4][4], double e0, double &lam, double (&q)[4]) {
+    const int lane = threadIdx.x & 31;
+    double t2 = 0.0, t3 = 0.0;
     for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) v[i][j] = i == j ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 32; sweep++) {
-        double off = 0.0;
-        for (int p = 0; p < 4; p++)
-            for (int r = p + 1; r < 4; r++) off += a[p][r] * a[p][r];
-        if (off < 1e-30) break;
-        for (int p = 0; p < 3; p++)
-            for (int r = p + 1; r < 4; r++) {
-                if (fabs(a[p][r]) < 1e-300) continue;
-                const double theta = (a[r][r] - a[p][p]) / (2.0 * a[p][r]);
-                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 4; k++) {  // columns p, r
-                    const double akp = a[k][p], akr = a[k][r];
-                    a[k][p] = c * akp - s * akr;
-                    a[k][r] = s * akp + c * akr;
-                }
-                for (int k = 0; k < 4; k++) {  // rows p, r
-                    const double apk = a[p][k], ark = a[r][k];
-                    a[p][k] = c * apk - s * ark;
-                    a[r][k] = s * apk + c * ark;
-                }
-                for (int k = 0; k < 4; k++) {
-                    const double vkp = v[k][p], vkr = v[k][r];
-                    v[k][p] = c * vkp - s * vkr;
-                    v[k][r] = s * vkp + c * vkr;
-                }
-            }
+        for (int j = 0; j < 4; j++) {
+            double k2 = 0.0;  // (K^2)_ij
+            for (int m = 0; m < 4; m++) k2 = fma(K[i][m], K[m][j], k2);
+            t2 = fma(K[i][j], K[i][j], t2);
+            t3 = fma(k2, K[j][i], t3);
+        }
+    const double c0 = K[0][0] * det3(K[1][1], K[1][2], K[1][3], K[2][1], K[2][2], K[2][3], K[3][1], K[3][2], K[3][3]) -
+                      K[0][1] * det3(K[1][0], K[1][2], K[1][3], K[2][0], K[2][2], K[2][3], K[3][0], K[3][2], K[3][3]) +
+                      K[0][2] * det3(K[1][0], K[1][1], K[1][3], K[2][0], K[2][1], K[2][3], K[3][0], K[3][1], K[3][3]) -
+                      K[0][3] * det3(K[1][0], K[1][1], K[1][2], K[2][0], K[2][1], K[2][2], K[3][0], K[3][1], K[3][2]);
+    const double c2 = -0.5 * t2, c1 = -t3 / 3.0;
+    double l = e0;
+    for (int it = 0; it < 64; it++) {
+        const double P = fma(fma(fma(l, l, c2), l, c1), l, c0);
+        const double dP = fma(fma(4.0 * l, l, 2.0 * c2), l, c1);
+        if (!(dP != 0.0)) break;
+        const double d = P / dP;
+        l -= d;
+        if (fabs(d) <= 1e-13 * fabs(l)) break;
     }
+    lam = l;
+    // cofactor (i, j) of M = K - l I on lane 4 i + j
+    double cof = 0.0;
+    if (lane < 16) {
+        const int i = lane >> 2, j = lane & 3;
+        double m[9];
+        int t = 0;
+        for (int r = 0; r < 4; r++)
+            if (r != i)
+                for (int c = 0; c < 4; c++)
+                    if (c != j) m[t++] = K[r][c] - (r == c ? l : 0.0);
+        cof = det3(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
+        if ((i + j) & 1) cof = -cof;
+    }
+    // squared norm of the row of this lane (lanes 4 i .. 4 i + 3)
+    double nrm = cof * cof;
+    nrm += __shfl_xor_sync(0xffffffffu, nrm, 1);
+    nrm += __shfl_xor_sync(0xffffffffu, nrm, 2);
     int best = 0;
-    for (int i = 1; i < 4; i++)
-        if (a[i][i] > a[best][best]) best = i;
-    lam = a[best][best];
-    for (int k = 0; k < 4; k++) q[k] = v[k][best];
+    double bn = __shfl_sync(0xffffffffu, nrm, 0);
+    for (int i = 1; i < 4; i++) {
+        const double v = __shfl_sync(0xffffffffu, nrm, 4 * i);
+        if (v > bn) {
+            bn = v;
+            best = i;
+        }
+    }
+    const double inv = bn > 1e-300 ? 1.0 / sqrt(bn) : 0.0;
+    for (int k = 0; k < 4; k++) q[k] = __shfl_sync(0xffffffffu, cof, 4 * best + k) * inv;
+    if (!(bn > 1e-300)) {
+        q[0] = 1.0;
+        q[1] = q[2] = q[3] = 0.0;
+    }
 }
 
 template <typename T>
@@ -101,42 +136,45 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
     const T *y = a.dst + (size_t)b * 3 * a.atoms_stride;
     double c[6] = {0, 0, 0, 0, 0, 0};
     if (a.center) {
-        double sx[6] = {0, 0, 0, 0, 0, 0};
+        T sx[6] = {0, 0, 0, 0, 0, 0};
         for (int i = tid; i < n; i += kRmsdThreads)
             for (int k = 0; k < 3; k++) {
-                sx[k] += (double)x[3 * i + k];
-                sx[3 + k] += (double)y[3 * i + k];
+                sx[k] += x[3 * i + k];
+                sx[3 + k] += y[3 * i + k];
             }
         for (int k = 0; k < 6; k++) {
-            const double s = block_sum(sx[k], s_red);
+            const double s = block_sum((double)sx[k], s_red);
             if (tid == 0) s_c[k] = n > 0 ? s / n : 0.0;
         }
         __syncthreads();
         for (int k = 0; k < 6; k++) c[k] = s_c[k];
     }
-    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // R (row-major) and R2
+    T ct[6];
+    for (int k = 0; k < 6; k++) ct[k] = (T)c[k];
+    T acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // R (row-major) and R2
     for (int i = tid; i < n; i += kRmsdThreads) {
-        double xi[3], yi[3];
+        T xi[3], yi[3];
         for (int k = 0; k < 3; k++) {
-            xi[k] = (double)x[3 * i + k] - c[k];
-            yi[k] = (double)y[3 * i + k] - c[3 + k];
+            xi[k] = x[3 * i + k] - ct[k];
+            yi[k] = y[3 * i + k] - ct[3 + k];
         }
         for (int p = 0; p < 3; p++)
             for (int q = 0; q < 3; q++) acc[3 * p + q] = fma(xi[p], yi[q], acc[3 * p + q]);
         acc[9] += xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2] + yi[0] * yi[0] + yi[1] * yi[1] + yi[2] * yi[2];
     }
     double tot[10];
-    for (int k = 0; k < 10; k++) tot[k] = block_sum(acc[k], s_red);
-    if (tid == 0) {
+    for (int k = 0; k < 10; k++) tot[k] = block_sum((double)acc[k], s_red);
+    if (tid < 32) {
         const double *R = tot;
         // quaternion matrix, same layout as the reference (coords2rmsd_interface.cpp:146-149)
-        double F[4][4] = {
+        const double F[4][4] = {
             {R[0] + R[4] + R[8], R[5] - R[7], R[6] - R[2], R[1] - R[3]},
             {R[5] - R[7], R[0] - R[4] - R[8], R[1] + R[3], R[2] + R[6]},
             {R[6] - R[2], R[1] + R[3], -R[0] + R[4] - R[8], R[5] + R[7]},
             {R[1] - R[3], R[2] + R[6], R[5] + R[7], -R[0] - R[4] + R[8]}};
         double lam, q[4];
-        jacobi4_max(F, lam, q);
+        key_eigen_warp(F, 0.5 * tot[9], lam, q);
+        if (tid != 0) return;
         // rotation from the unit quaternion (coords2rmsd_interface.cpp:36-46)
         double U[9];
         U[0] = q[0] * q[0] + q[1] * q[1] - q[2] * q[2] - q[3] * q[3];
@@ -165,23 +203,23 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_bwd_kernel(RmsdArgs<T> a) {
     const T *x = a.src + (size_t)b * 3 * a.atoms_stride;
     const T *y = a.dst + (size_t)b * 3 * a.atoms_stride;
     T *gx = a.grad_src + (size_t)b * 3 * a.atoms_stride;
-    double c[6] = {0, 0, 0, 0, 0, 0};
+    T c[6] = {0, 0, 0, 0, 0, 0};
     if (a.center && a.centroids)
-        for (int k = 0; k < 6; k++) c[k] = a.centroids[6 * b + k];
+        for (int k = 0; k < 6; k++) c[k] = (T)a.centroids[6 * b + k];
     const T *ut = a.ut + (size_t)9 * b;
-    double U[9];
-    for (int k = 0; k < 9; k++) U[k] = (double)ut[k];
-    const double r = (double)a.rmsd[b];
-    const double scale = (n > 0 && r > 0.0) ? (double)a.grad_rmsd[b] / (r * (double)n) : 0.0;
+    T U[9];
+    for (int k = 0; k < 9; k++) U[k] = ut[k];
+    const T r = a.rmsd[b];
+    const T scale = (n > 0 && r > T(0)) ? a.grad_rmsd[b] / (r * (T)n) : T(0);
     for (int i = tid; i < a.atoms_stride; i += kRmsdThreads) {
         if (i < n) {
-            double xi[3], yi[3];
+            T xi[3], yi[3];
             for (int k = 0; k < 3; k++) {
-                xi[k] = (double)x[3 * i + k] - c[k];
-                yi[k] = (double)y[3 * i + k] - c[3 + k];
+                xi[k] = x[3 * i + k] - c[k];
+                yi[k] = y[3 * i + k] - c[3 + k];
             }
             for (int k = 0; k < 3; k++)
-                gx[3 * i + k] = (T)(scale * (xi[k] - (U[3 * k] * yi[0] + U[3 * k + 1] * yi[1] + U[3 * k + 2] * yi[2])));
+                gx[3 * i + k] = scale * (xi[k] - (U[3 * k] * yi[0] + U[3 * k + 1] * yi[1] + U[3 * k + 2] * yi[2]));
         } else {
             gx[3 * i] = gx[3 * i + 1] = gx[3 * i + 2] = T(0);
         }
