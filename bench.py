@@ -220,7 +220,7 @@ def run_ours(args):
         if not args.no_extras:
             # FP64 inter-tile carry threshold sweep (-1 = never FP64)
             # (on warp tiles of 256 residues: the one-warp-per-chain scheme has no inter-tile carry)
-            sweep_rows = autotune.sweep(ang, lengths, up, candidates=[(8, 0)],
+            sweep_rows = autotune.sweep(ang, lengths, up, candidates=[(8, 1)],
                                         carry_thresholds=(128, 256, 512, -1), steps=5)
             rm.set_options(tuned["residues_per_thread"], tuned["fp64_carry_min_len"], 0, 0,
                            tuned["threads_per_cta"])
@@ -310,8 +310,8 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm",
                      "kernel": "a2b_bwd_coords_kernel" if dom == "backward" else
-                               {0: "a2b_fwd_w_kernel", 128: "a2b_fwd_f32_kernel", 32: "a2b_fwd_chain_kernel"}[
-                                   tuned["threads_per_cta"]],
+                               {1: "a2b_fwd_w_kernel", 128: "a2b_fwd_f32_kernel", 32: "a2b_fwd_chain_kernel",
+                                0: "a2b_fwd_chain_kernel (automatic)"}[tuned["threads_per_cta"]],
                      "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes_per_launch": dom_bytes,
@@ -637,7 +637,7 @@ def main():
                     help="residues per thread; 0 = autotune (the default)")
     ap.add_argument("--bwd-rpt", type=int, default=4, help="residues per lane of the coordinate backward (with --rpt)")
     ap.add_argument("--bwd-buffers", type=int, default=1, help="chunk buffers of the coordinate backward (with --rpt)")
-    ap.add_argument("--cta", type=int, default=0, help="0 = warp tiles, 128 = CTA tiles, 32 = one warp per chain (with --rpt)")
+    ap.add_argument("--cta", type=int, default=0, help="0 = automatic, 1 = warp tiles, 128 = CTA tiles, 32 = one warp per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
     args = ap.parse_args()

@@ -52,11 +52,15 @@ typedef enum tpl_status {
 typedef struct tpl_options {
     int residues_per_thread;   /* residues each thread scans serially: 1, 2, 4 or 8 (4 or 8 when
                                   threads_per_cta = 32) */
-    int threads_per_cta;       /* scan scheme: 0 = warp-granular tiles of 32 R residues joined by
-                                  look-back; 128 = CTA tiles of 128 R residues; 32 = one warp walks
-                                  a whole chain in chunks of 32 R residues (no look-back; the
-                                  forward records the chain frame every 128 residues in the
-                                  workspace and the backward starts from those records) */
+    int threads_per_cta;       /* scan scheme of Angles2Backbone FP32: 0 = automatic (one warp per
+                                  chain when the batch has at least two chains per SM and
+                                  residues_per_thread is 0, 4 or 8; warp tiles otherwise);
+                                  32 = one warp walks a whole chain in chunks of 32 R residues (no
+                                  look-back; the forward records the chain frame every 128
+                                  residues in the workspace and the backward starts from those
+                                  records); 1 = warp-granular tiles of 32 R residues joined by
+                                  look-back; 128 = CTA tiles of 128 R residues.  Angles2Coords
+                                  reads it as its threads per chain (0 = 256, 128, 256, 512). */
     int fp64_carry_min_len;    /* chains at least this long compose inter-tile carries in FP64;
                                   0 = default (always), -1 = never */
     int renormalize;           /* 0 = default (on), 1 = on, -1 = off: Newton-Schulz renormalisation

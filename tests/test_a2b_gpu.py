@@ -99,8 +99,8 @@ def test_fp64_plain_matches_oracle(rm, B, L, seed):
     check(c, gi, rc, rg, lengths, L, COORD_TOL_F64, GRAD_TOL_F64)
 
 
-@pytest.mark.parametrize("rpt,cta", [(1, 0), (2, 0), (4, 0), (8, 0), (1, 128), (4, 128), (8, 128), (4, 32),
-                                      (8, 32)])
+@pytest.mark.parametrize("rpt,cta", [(1, 1), (2, 1), (4, 1), (8, 1), (1, 128), (4, 128), (8, 128), (4, 32),
+                                      (8, 32), (0, 0)])
 def test_tile_shapes_and_lookback(rm, rpt, cta):
     """Chains of 1000 residues split into up to 32 warp tiles (R=1: 32-residue tiles)
     or CTA tiles (128 R residues, one tile at R=8), or walked by one warp per chain
@@ -124,7 +124,7 @@ def test_fp64_carry_threshold_and_renorm_off(rm):
     ang, lengths, g = make_case(B, L, 77, lengths=[600, 450, 300, 20])
     rc, rg = oracle_ref(ang, lengths, g, True)
     for carry, renorm, ctol in [(-1, 0, COORD_TOL_F32), (256, 0, COORD_TOL_F32), (0, -1, 5e-3)]:
-        rm.set_options(1, carry, renorm, 0)
+        rm.set_options(1, carry, renorm, 0, 1)
         try:
             c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
         finally:
@@ -132,7 +132,7 @@ def test_fp64_carry_threshold_and_renorm_off(rm):
         check(c, gi, rc, rg, lengths, L, ctol, GRAD_TOL_F32)
 
 
-@pytest.mark.parametrize("rpt,cta", [(0, 0), (8, 32), (4, 32)])
+@pytest.mark.parametrize("rpt,cta", [(0, 1), (8, 32), (4, 32)])
 def test_padding_nan_does_not_leak(rm, rpt, cta):
     B, L = 4, 64
     ang, lengths, g = make_case(B, L, 9, lengths=[64, 30, 1, 0])
@@ -193,7 +193,7 @@ def test_lookback_timeout_is_reported(rm, built):
     a = torch.rand(B, 3, L, device=dev)
     ln = torch.full((B,), L, dtype=torch.int32, device=dev)
     out = torch.zeros(B, 9 * L, device=dev)
-    rm.set_options(4, 0, 0, 0)  # 128-residue warp tiles: 3 tiles per chain
+    rm.set_options(4, 0, 0, 0, 1)  # 128-residue warp tiles: 3 tiles per chain
     try:
         ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
         ws[4 * 8:4 * 9].view(torch.int32).fill_(1)  # WsHeader.test_skip_publish

@@ -22,8 +22,8 @@ import torch
 from . import load_extension
 
 CANDIDATES = [
-    # (residues_per_thread, threads_per_cta)  threads_per_cta 0 = warp tiles
-    (1, 0), (2, 0), (4, 0), (8, 0), (2, 128), (4, 128), (8, 128),
+    # (residues_per_thread, threads_per_cta)  threads_per_cta 1 = warp tiles, 128 = CTA tiles
+    (1, 1), (2, 1), (4, 1), (8, 1), (2, 128), (4, 128), (8, 128),
     # threads_per_cta 32 = one warp per chain, chunks of 32 R residues
     (4, 32), (8, 32),
 ]

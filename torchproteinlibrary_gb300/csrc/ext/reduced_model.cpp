@@ -158,8 +158,9 @@ void set_options(int64_t residues_per_thread, int64_t fp64_carry_min_len, int64_
                  int64_t threads_per_cta) {
     tpl_options o = {(int)residues_per_thread, (int)threads_per_cta, (int)fp64_carry_min_len, (int)renormalize,
                      (int)max_ctas, g_opt.copy_buffers};
-    TORCH_CHECK(o.threads_per_cta == 0 || o.threads_per_cta == 128 || o.threads_per_cta == 32,
-                "threads_per_cta must be 0 (warp tiles), 128 (CTA tiles) or 32 (one warp per chain)");
+    TORCH_CHECK(o.threads_per_cta == 0 || o.threads_per_cta == 1 || o.threads_per_cta == 128 ||
+                    o.threads_per_cta == 32,
+                "threads_per_cta must be 0 (automatic), 1 (warp tiles), 128 (CTA tiles) or 32 (one warp per chain)");
     TORCH_CHECK(o.threads_per_cta != 32 || o.residues_per_thread == 0 || o.residues_per_thread == 4 ||
                     o.residues_per_thread == 8,
                 "one warp per chain takes residues_per_thread 4 or 8");

@@ -24,6 +24,7 @@
 // forward positions (angles are 3x smaller than coordinates), scans (G, S)
 // backwards over threads, warps and tiles (tiles handed out last-first), and
 // evaluates the three joint gradients of each residue.
+#include <algorithm>
 #include <cstdio>
 
 #include "tpl_common.cuh"
@@ -1299,21 +1300,49 @@ struct A2bShape {
     bool warp;  // warp-granular tiles (default) or CTA tiles of NT threads
 };
 
-// threads_per_cta = 0: warp-granular tiles of 32 R residues (default).
-// threads_per_cta = 128: CTA tiles of 128 R residues with block-wide scans.
+// threads_per_cta = 1 (or 0 when the automatic choice is not one warp per chain):
+// warp-granular tiles of 32 R residues.  threads_per_cta = 128: CTA tiles of 128 R
+// residues with block-wide scans.
 static A2bShape a2b_shape(const tpl_options &opt, bool backward) {
     (void)backward;
     A2bShape s;
     s.R = opt.residues_per_thread > 0 ? opt.residues_per_thread : 4;
-    s.warp = opt.threads_per_cta == 0;
+    s.warp = opt.threads_per_cta != 128;
     s.NT = s.warp ? 32 : 128;
     return s;
+}
+
+// threads_per_cta = 0: one warp per chain when the batch alone gives every SM at
+// least two chains (and residues_per_thread allows it), warp tiles otherwise.  The
+// forward and the backward of one shape make the same choice.
+static bool use_chain_scheme(const tpl_options &opt, int B) {
+    if (opt.threads_per_cta == 32) return true;
+    if (opt.threads_per_cta != 0) return false;
+    const int r = opt.residues_per_thread;
+    if (!(r == 0 || r == 4 || r == 8)) return false;
+    static int num_sms = 0;
+    if (!num_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (num_sms <= 0) num_sms = 1;
+    }
+    return B >= 2 * num_sms;
+}
+
+static tpl_options chain_options(const tpl_options &opt) {
+    tpl_options o = opt;
+    o.threads_per_cta = 32;
+    if (o.residues_per_thread == 0) o.residues_per_thread = 8;
+    return o;
 }
 
 int a2b_tile_for(const tpl_options &opt) {
     if (opt.threads_per_cta == 32) return a2b_chain_record_stride();  // one warp per chain: frame records
     A2bShape f = a2b_shape(opt, false);
-    return f.R * f.NT;
+    const int tile = f.R * f.NT;
+    if (opt.threads_per_cta == 0) return std::min(tile, a2b_chain_record_stride());  // either scheme fits
+    return tile;
 }
 
 static A2bArgs make_args(const float *angles, const int32_t *lengths, void *ws, int B, int L, int tile,
@@ -1374,7 +1403,7 @@ static int launch_bwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
 int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, void *ws, int B, int L,
                     const tpl_options &opt, cudaStream_t st) {
     if (B == 0 || L == 0) return TPL_OK;
-    if (opt.threads_per_cta == 32) return a2b_forward_chain(angles, lengths, coords, ws, B, L, opt, st);
+    if (use_chain_scheme(opt, B)) return a2b_forward_chain(angles, lengths, coords, ws, B, L, chain_options(opt), st);
     A2bShape s = a2b_shape(opt, false);
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.coords = coords;
@@ -1399,8 +1428,8 @@ int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, 
 int a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
                      void *ws, int B, int L, const tpl_options &opt, cudaStream_t st) {
     if (B == 0 || L == 0) return TPL_OK;
-    if (opt.threads_per_cta == 32)
-        return a2b_backward_chain(grad_angles, grad_coords, angles, lengths, ws, B, L, opt, st);
+    if (use_chain_scheme(opt, B))
+        return a2b_backward_chain(grad_angles, grad_coords, angles, lengths, ws, B, L, chain_options(opt), st);
     A2bShape s = a2b_shape(opt, true);
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.grad_angles = grad_angles;

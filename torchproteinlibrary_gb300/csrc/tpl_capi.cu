@@ -88,8 +88,9 @@ tpl_options resolve(const tpl_options *opt) {
 bool options_ok(const tpl_options &o) {
     const int r = o.residues_per_thread;
     if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8)) return false;
-    // 0: warp tiles, 128: CTA tiles, 32: one warp per chain (4 or 8 residues per lane)
-    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 128 || o.threads_per_cta == 32)) return false;
+    // 0: automatic, 1: warp tiles, 128: CTA tiles, 32: one warp per chain (4 or 8 residues per lane)
+    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 1 || o.threads_per_cta == 128 || o.threads_per_cta == 32))
+        return false;
     if (o.threads_per_cta == 32 && !(r == 0 || r == 4 || r == 8)) return false;
     if (o.max_ctas < 0) return false;
     if (o.copy_buffers < 0 || o.copy_buffers > 2) return false;
