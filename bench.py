@@ -280,7 +280,7 @@ def run_ours(args):
     value = residues / (ms / 1e3)
 
     if args.no_extras:
-        check = plain = e2e = a2c = train = None
+        check = plain = e2e = a2c = train = transform = None
     else:
         # correctness of this very run against the FP64 plain form on a slice
         check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
@@ -290,6 +290,7 @@ def run_ours(args):
         e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
         a2c = time_a2c(dev)
         train = time_training_step(dev)
+        transform = time_coords_transform(dev)
 
     peak, peak_kind = peaks()
     fwd_ms, bwd_ms = statistics.mean(t_f), statistics.mean(t_b)
@@ -329,6 +330,7 @@ def run_ours(args):
         "plain_fp64": plain,
         "angles2coords": a2c,
         "training_step": train,
+        "coords_transform": transform,
         "accuracy_vs_fp64": check,
     }
     if rank == 0:
@@ -610,6 +612,41 @@ def time_training_step(dev, steps=10, seed=1004):
     res["grad_max_rel_f32_vs_f64"] = float((grads["f32"] - grads["f64"]).abs().max() / grads["f64"].abs().max())
     res["workload"] = ("training step: Angles2Coords + Coords2RMSD loss (mean) fwd+bwd, 256 chains x U{50..500} "
                        "random residues, autograd layers, inputs resident")
+    return res
+
+
+def time_coords_transform(dev, steps=20):
+    """CoordsTransform's elementwise passes on a batch larger than L2: 2048 rows of
+    4000 atoms (98 MB of float32 coordinates per tensor).  Translate and rotate read
+    and write 12 B per atom each; reported as achieved bandwidth against the
+    measured HBM peak."""
+    import torch
+    from torchproteinlibrary_gb300 import load_extension
+
+    fm = load_extension("_FullAtomModel")
+    B, S = 2048, 4000
+    g = torch.Generator(device=dev).manual_seed(7)
+    x = torch.randn(B, 3 * S, device=dev, generator=g)
+    out = torch.empty_like(x)
+    na = torch.full((B,), S, dtype=torch.int32, device=dev)
+    T = torch.randn(B, 3, device=dev, generator=g)
+    R = torch.linalg.qr(torch.randn(B, 3, 3, device=dev, generator=g))[0].contiguous()
+    peak, _ = peaks()
+    res = {"workload": f"{B} rows x {S} atoms, float32", "bytes_per_call": 2 * x.numel() * 4}
+    for name, fn in (("translate", lambda: fm.CoordsTranslateGPU_forward(x, out, T, na)),
+                     ("rotate", lambda: fm.CoordsRotateGPU_forward(x, out, R, na))):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        gbs = res["bytes_per_call"] / (ms / 1e3) / 1e9
+        res[name] = {"ms": ms, "GB/s": gbs, "frac_of_hbm_peak": gbs / peak}
     return res
 
 

@@ -31,28 +31,34 @@ struct Vec16<double> {
     static constexpr int n = 2;
 };
 
+constexpr int kUnroll = 4;  // vectors in flight per thread in the elementwise passes
+
+// 16-byte streaming load / store (data touched once).
 template <typename T>
 __device__ __forceinline__ void load16(const T *p, T (&v)[Vec16<T>::n]) {
-    const typename Vec16<T>::type x = *reinterpret_cast<const typename Vec16<T>::type *>(p);
+    const typename Vec16<T>::type x = __ldcs(reinterpret_cast<const typename Vec16<T>::type *>(p));
     memcpy(v, &x, sizeof(x));
 }
 template <typename T>
 __device__ __forceinline__ void store16(T *p, const T (&v)[Vec16<T>::n]) {
     typename Vec16<T>::type x;
     memcpy(&x, v, sizeof(x));
-    *reinterpret_cast<typename Vec16<T>::type *>(p) = x;
+    __stcs(reinterpret_cast<typename Vec16<T>::type *>(p), x);
 }
 
 // out[b, e] = (in ? in[b, e] : 0) + (add ? add[b, e % 3] * (scale_by_count ? 1 / n_b : 1) : 0)
 // for e < 3 n_b, 0 after.  Covers translate (add = T), its backward (add = null),
 // and the centre's backward (in = null, add = dL/dcentre, scaled by 1 / n_b).
+// Grid: y over rows (strided), x over pieces of a row, so no thread divides by the
+// row length; VEC: 16-byte vectors inside a row (3 * atoms_stride a multiple of the
+// vector width and 16-byte-aligned rows).
 struct ShiftArgs {
     const void *in;
     void *out;
     const void *add;
     const int *num_atoms;
-    long long total;  // B * row
-    int row;          // 3 * atoms_stride
+    int B;
+    int row;  // 3 * atoms_stride
     int scale_by_count;
 };
 
@@ -62,63 +68,83 @@ __global__ void __launch_bounds__(256) shift_kernel(ShiftArgs a) {
     const T *in = static_cast<const T *>(a.in);
     T *out = static_cast<T *>(a.out);
     const T *add = static_cast<const T *>(a.add);
-    const long long step = (long long)gridDim.x * blockDim.x;
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v * N < a.total; v += step) {
-        const long long e0 = v * N;
-        T x[Vec16<T>::n];
-        if (VEC && in) load16(in + e0, x);
+    const int nv = a.row / N;  // vectors per row
+    for (int b = blockIdx.y; b < a.B; b += gridDim.y) {
+        const int n = max(0, min(a.num_atoms[b], a.row / 3)), n3 = 3 * n;
+        T t[3] = {T(0), T(0), T(0)};
+        if (add)
+            for (int k = 0; k < 3; k++) {
+                t[k] = add[3 * (size_t)b + k];
+                if (a.scale_by_count && n > 0) t[k] = t[k] / T(n);
+            }
+        const size_t base = (size_t)b * a.row;
+        // kUnroll independent vectors per thread and step: loads issued before use
+        const int step = gridDim.x * blockDim.x;
+        for (int v0 = blockIdx.x * blockDim.x + threadIdx.x; v0 < nv; v0 += kUnroll * step) {
+            T x[kUnroll][Vec16<T>::n];
 #pragma unroll
-        for (int k = 0; k < N; k++) {
-            const long long e = e0 + k;
-            if (!VEC && in) x[k] = in[e];
-            if (!VEC && !in) x[k] = T(0);
-            if (VEC && !in) x[k] = T(0);
-            const long long b = e / a.row;
-            const int i = (int)(e - b * a.row);
-            const int n = a.num_atoms[b];
-            T y = T(0);
-            if (i < 3 * n) {
-                y = x[k];
-                if (add) {
-                    T s = add[3 * b + i % 3];
-                    if (a.scale_by_count) s = s / T(n);
-                    y += s;
+            for (int u = 0; u < kUnroll; u++) {
+                const int v = v0 + u * step;
+                if (v >= nv) continue;
+                if (VEC) {
+                    if (in) load16(in + base + (size_t)v * N, x[u]);
+                    else
+                        for (int k = 0; k < N; k++) x[u][k] = T(0);
+                } else {
+                    x[u][0] = in ? __ldcs(in + base + v) : T(0);
                 }
             }
-            x[k] = y;
-        }
-        if (VEC) {
-            store16(out + e0, x);
-        } else {
-            out[e0] = x[0];
+#pragma unroll
+            for (int u = 0; u < kUnroll; u++) {
+                const int v = v0 + u * step;
+                if (v >= nv) continue;
+#pragma unroll
+                for (int k = 0; k < N; k++) {
+                    const int e = v * N + k;
+                    x[u][k] = e < n3 ? x[u][k] + t[e % 3] : T(0);
+                }
+                if (VEC) store16(out + base + (size_t)v * N, x[u]);
+                else __stcs(out + base + v, x[u][0]);
+            }
         }
     }
 }
 
 // out[b, atom] = R_b x (or R_b^T x) for atom < n_b, 0 after; R row-major [B, 3, 3].
+// Grid: y over rows (strided), x over atoms of a row.
 template <typename T>
-__global__ void __launch_bounds__(256) rotate_kernel(const T *in, T *out, const T *R, const int *num_atoms,
-                                                     long long atoms, int stride, int transpose) {
-    const long long step = (long long)gridDim.x * blockDim.x;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < atoms; t += step) {
-        const long long b = t / stride;
-        const int i = (int)(t - b * stride);
-        const T *x = in + 3 * t;
-        T *y = out + 3 * t;
-        if (i >= num_atoms[b]) {
-            y[0] = y[1] = y[2] = T(0);
-            continue;
-        }
-        const T *m = R + 9 * b;
-        const T x0 = x[0], x1 = x[1], x2 = x[2];
-        if (transpose) {
-            y[0] = m[0] * x0 + m[3] * x1 + m[6] * x2;
-            y[1] = m[1] * x0 + m[4] * x1 + m[7] * x2;
-            y[2] = m[2] * x0 + m[5] * x1 + m[8] * x2;
-        } else {
-            y[0] = m[0] * x0 + m[1] * x1 + m[2] * x2;
-            y[1] = m[3] * x0 + m[4] * x1 + m[5] * x2;
-            y[2] = m[6] * x0 + m[7] * x1 + m[8] * x2;
+__global__ void __launch_bounds__(256) rotate_kernel(const T *in, T *out, const T *R, const int *num_atoms, int B,
+                                                     int stride, int transpose) {
+    for (int b = blockIdx.y; b < B; b += gridDim.y) {
+        const int n = num_atoms[b];
+        T m[9];
+        for (int k = 0; k < 9; k++) m[k] = R[9 * (size_t)b + (transpose ? 3 * (k % 3) + k / 3 : k)];
+        const T *x = in + (size_t)b * 3 * stride;
+        T *y = out + (size_t)b * 3 * stride;
+        const int step = gridDim.x * blockDim.x;
+        for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < stride; i0 += kUnroll * step) {
+            T v[kUnroll][3];
+#pragma unroll
+            for (int u = 0; u < kUnroll; u++) {  // loads of kUnroll atoms in flight
+                const int i = i0 + u * step;
+                if (i < min(n, stride))
+                    for (int k = 0; k < 3; k++) v[u][k] = __ldcs(x + 3 * i + k);
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; u++) {
+                const int i = i0 + u * step;
+                if (i >= stride) continue;
+                T r0 = T(0), r1 = T(0), r2 = T(0);
+                if (i < n) {
+                    const T x0 = v[u][0], x1 = v[u][1], x2 = v[u][2];
+                    r0 = m[0] * x0 + m[1] * x1 + m[2] * x2;
+                    r1 = m[3] * x0 + m[4] * x1 + m[5] * x2;
+                    r2 = m[6] * x0 + m[7] * x1 + m[8] * x2;
+                }
+                __stcs(y + 3 * i, r0);
+                __stcs(y + 3 * i + 1, r1);
+                __stcs(y + 3 * i + 2, r2);
+            }
         }
     }
 }
@@ -189,18 +215,15 @@ __global__ void __launch_bounds__(kReduceThreads) bbox_kernel(const T *in, T *lo
     }
 }
 
-int grid_for(long long items, int threads) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
-    long long g = (items + threads - 1) / threads;
-    const long long cap = (long long)sms * 8;  // a few waves of 256-thread CTAs, grid-stride beyond
-    if (g > cap) g = cap;
-    return g < 1 ? 1 : (int)g;
+// Row-major 2-D grid: x covers one row's items in 256-thread blocks, y the rows
+// (capped; the kernels stride over the remaining rows).
+dim3 grid_rows(int B, long long items_per_row) {
+    long long gx = (items_per_row + 255) / 256;
+    if (gx < 1) gx = 1;
+    if (gx > 65535) gx = 65535;
+    int gy = B < 1 ? 1 : B;
+    if (gy > 65535) gy = 65535;
+    return dim3((unsigned)gx, (unsigned)gy, 1);
 }
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
@@ -211,12 +234,15 @@ template <typename T>
 int coords_shift(const T *in, T *out, const T *add, int scale_by_count, const int *num_atoms, int B, int stride,
                  cudaStream_t st) {
     if (B == 0 || stride == 0) return TPL_OK;
-    ShiftArgs a{in, out, add, num_atoms, (long long)B * 3 * stride, 3 * stride, scale_by_count};
-    const bool vec = aligned16(out) && (!in || aligned16(in)) && (a.total % Vec16<T>::n == 0);
+    ShiftArgs a{in, out, add, num_atoms, B, 3 * stride, scale_by_count};
+    // 16-byte vectors when every row starts 16-byte aligned and holds whole vectors
+    const bool vec = aligned16(out) && (!in || aligned16(in)) && (a.row % Vec16<T>::n == 0) &&
+                     ((a.row * sizeof(T)) % 16 == 0);
+    const int n = vec ? Vec16<T>::n : 1;
     if (vec) {
-        shift_kernel<T, true><<<grid_for(a.total / Vec16<T>::n, 256), 256, 0, st>>>(a);
+        shift_kernel<T, true><<<grid_rows(B, (a.row / n + kUnroll - 1) / kUnroll), 256, 0, st>>>(a);
     } else {
-        shift_kernel<T, false><<<grid_for(a.total, 256), 256, 0, st>>>(a);
+        shift_kernel<T, false><<<grid_rows(B, (a.row + kUnroll - 1) / kUnroll), 256, 0, st>>>(a);
     }
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
@@ -225,8 +251,8 @@ template <typename T>
 int coords_rotate(const T *in, T *out, const T *R, int transpose, const int *num_atoms, int B, int stride,
                   cudaStream_t st) {
     if (B == 0 || stride == 0) return TPL_OK;
-    const long long atoms = (long long)B * stride;
-    rotate_kernel<T><<<grid_for(atoms, 256), 256, 0, st>>>(in, out, R, num_atoms, atoms, stride, transpose);
+    rotate_kernel<T><<<grid_rows(B, (stride + kUnroll - 1) / kUnroll), 256, 0, st>>>(in, out, R, num_atoms, B, stride,
+                                                                                   transpose);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
