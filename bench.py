@@ -212,9 +212,10 @@ def run_ours(args):
     sweep_rows = None
     if args.rpt:
         rm.set_options(args.rpt, 0, 0, 0, args.cta)
-        rm.set_backward_options(args.bwd_rpt, args.bwd_buffers)
+        rm.set_backward_options(args.bwd_rpt, args.bwd_buffers, args.bwd_cta)
         tuned = {"residues_per_thread": args.rpt, "threads_per_cta": args.cta, "fp64_carry_min_len": 0,
-                 "backward_coords": {"residues_per_thread": args.bwd_rpt, "copy_buffers": args.bwd_buffers}}
+                 "backward_coords": {"residues_per_thread": args.bwd_rpt, "copy_buffers": args.bwd_buffers,
+                                     "threads_per_cta": args.bwd_cta}}
     else:
         tuned = autotune.tune(ang, lengths, up, use_cache=False)
         if not args.no_extras:
@@ -310,8 +311,11 @@ def run_ours(args):
                    "l2": "inputs and outputs larger than L2; no flush", "launch": "CUDA graph per pass",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm",
-                     "kernel": "a2b_bwd_coords_kernel" if dom == "backward" else
+                     "kernel": ("a2b_bwd_coords_ring_kernel"
+                                if tuned.get("backward_coords", {}).get("threads_per_cta") == 4
+                                else "a2b_bwd_coords_kernel") if dom == "backward" else
                                {1: "a2b_fwd_w_kernel", 128: "a2b_fwd_f32_kernel", 32: "a2b_fwd_chain_kernel",
+                                4: "a2b_fwd_ring_kernel",
                                 0: "a2b_fwd_chain_kernel (automatic)"}[tuned["threads_per_cta"]],
                      "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -423,11 +427,36 @@ def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
         step(0)
         torch.cuda.synchronize(dev)
     ms_serial = (time.perf_counter() - t0) * 1e3 / steps
+    # the same copies with no work between them: the floor that the host link sets
+    dev_bufs = [(torch.empty(ang_h.shape, device=dev), torch.empty(len_h.shape, dtype=len_h.dtype, device=dev),
+                 torch.empty(up_h.shape, device=dev), torch.zeros(outs[0][0].shape, device=dev),
+                 torch.zeros(outs[0][1].shape, device=dev)) for _ in range(2)]
+
+    def copies(i):
+        a, ln, u, c, g = dev_bufs[i % 2]
+        out_c, out_g = outs[i % 2]
+        with torch.cuda.stream(streams[i % 2]):
+            a.copy_(ang_h, non_blocking=True)
+            ln.copy_(len_h, non_blocking=True)
+            u.copy_(up_h, non_blocking=True)
+            out_c.copy_(c, non_blocking=True)
+            out_g.copy_(g, non_blocking=True)
+
+    for i in range(2):
+        copies(i)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        copies(i)
+    torch.cuda.synchronize(dev)
+    ms_copies = (time.perf_counter() - t0) * 1e3 / steps
     h2d = ang_np.nbytes + len_np.nbytes + up_np.nbytes
     d2h = outs[0][0].numel() * 4 + outs[0][1].numel() * 4
     return {"value": B * L_RES / (ms / 1e3), "unit": "residues/s", "ms_per_step": ms,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "serial_ms_per_step": ms_serial,
+            "copies_only_ms_per_step": ms_copies,
+            "copies_only_note": "the same pinned copies on the same two streams with no kernels: the host-link floor",
             "api": "torchproteinlibrary_gb300.ReducedModel.Angles2Backbone (autograd), pinned host buffers, "
                    "two streams alternating"}
 
@@ -674,7 +703,8 @@ def main():
                     help="residues per thread; 0 = autotune (the default)")
     ap.add_argument("--bwd-rpt", type=int, default=4, help="residues per lane of the coordinate backward (with --rpt)")
     ap.add_argument("--bwd-buffers", type=int, default=1, help="chunk buffers of the coordinate backward (with --rpt)")
-    ap.add_argument("--cta", type=int, default=0, help="0 = automatic, 1 = warp tiles, 128 = CTA tiles, 32 = one warp per chain (with --rpt)")
+    ap.add_argument("--cta", type=int, default=0, help="0 = automatic, 1 = warp tiles, 128 = CTA tiles, 32 = one warp per chain, 4 = one CTA of four warps per chain (with --rpt)")
+    ap.add_argument("--bwd-cta", type=int, default=0, help="coordinate backward: 0 = automatic, 32 = one warp per chain, 4 = one CTA of four warps per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
     args = ap.parse_args()

@@ -51,14 +51,16 @@ typedef enum tpl_status {
 /* Tuning knobs.  A NULL options pointer, or a zero field, selects the tuned default. */
 typedef struct tpl_options {
     int residues_per_thread;   /* residues each thread scans serially: 1, 2, 4 or 8 (4 or 8 when
-                                  threads_per_cta = 32) */
+                                  threads_per_cta = 32 or 4) */
     int threads_per_cta;       /* scan scheme of Angles2Backbone FP32: 0 = automatic (one warp per
                                   chain when the batch has at least two chains per SM and
                                   residues_per_thread is 0, 4 or 8; warp tiles otherwise);
                                   32 = one warp walks a whole chain in chunks of 32 R residues (no
                                   look-back; the forward records the chain frame every 128
                                   residues in the workspace and the backward starts from those
-                                  records); 1 = warp-granular tiles of 32 R residues joined by
+                                  records); 4 = one CTA of four warps per chain, chunk k on warp
+                                  k % 4, the chain frame handed from warp to warp in shared memory
+                                  (same records); 1 = warp-granular tiles of 32 R residues joined by
                                   look-back; 128 = CTA tiles of 128 R residues.  Angles2Coords
                                   reads it as its threads per chain (0 = 256, 128, 256, 512). */
     int fp64_carry_min_len;    /* chains at least this long compose inter-tile carries in FP64;
@@ -118,7 +120,9 @@ int tpl_a2b_backward_f32(float *grad_angles, const float *grad_coords, const flo
  * same angles and lengths.  It reads 36 B of coordinates per residue instead of
  * 12 B of angles and does a fraction of the arithmetic.  The workspace only needs
  * its status word (>= 64 bytes, zeroed once).  opt->residues_per_thread: 4 (default)
- * or 8 residues per lane. */
+ * or 8 residues per lane; opt->threads_per_cta: 0 (default) or 32 = one warp per
+ * chain, 4 = one CTA of four warps per chain with the carried sums handed from warp
+ * to warp. */
 int tpl_a2b_backward_coords_f32(float *grad_angles, const float *grad_coords, const float *coords,
                                 const int32_t *lengths, void *workspace, size_t workspace_bytes, int batch,
                                 int max_len, const tpl_options *opt, void *stream);

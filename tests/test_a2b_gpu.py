@@ -100,11 +100,12 @@ def test_fp64_plain_matches_oracle(rm, B, L, seed):
 
 
 @pytest.mark.parametrize("rpt,cta", [(1, 1), (2, 1), (4, 1), (8, 1), (1, 128), (4, 128), (8, 128), (4, 32),
-                                      (8, 32), (0, 0)])
+                                      (8, 32), (4, 4), (8, 4), (0, 0)])
 def test_tile_shapes_and_lookback(rm, rpt, cta):
     """Chains of 1000 residues split into up to 32 warp tiles (R=1: 32-residue tiles)
-    or CTA tiles (128 R residues, one tile at R=8), or walked by one warp per chain
-    in chunks of 32 R residues (cta=32); all within tolerance of the oracle."""
+    or CTA tiles (128 R residues, one tile at R=8), or walked in chunks of 32 R
+    residues by one warp per chain (cta=32) or by the four warps of one CTA per
+    chain (cta=4); all within tolerance of the oracle."""
     B, L = 6, 1000
     ang, lengths, g = make_case(B, L, 40 + rpt, lengths=[1000, 999, 129, 128, 127, 1])
     rm.set_options(rpt, 0, 0, 0, cta)
@@ -305,14 +306,18 @@ def test_config3_full_size_against_fp64_form(rm):
     check(c64[idx], g64[idx], rc, rg, lengths[idx], 700, COORD_TOL_F64, GRAD_TOL_F64)
 
 
+@pytest.mark.parametrize("cta", [32, 4])
 @pytest.mark.parametrize("rpt", [4, 8])
-@pytest.mark.parametrize("L", [1001, 258, 1000])
-def test_one_warp_per_chain_ragged_and_unaligned(rm, rpt, L):
-    """One warp per chain over ragged lengths at chunk edges, with rows that are not
-    16-byte aligned (L % 4 != 0: scalar loads and stores) and aligned (float4)."""
+@pytest.mark.parametrize("L", [1001, 258, 1000, 1400])
+def test_one_warp_per_chain_ragged_and_unaligned(rm, rpt, L, cta):
+    """One warp per chain (cta=32) or one CTA of four warps per chain (cta=4) over
+    ragged lengths at chunk edges, with rows that are not 16-byte aligned (L % 4 != 0:
+    scalar loads and stores) and aligned (float4).  L = 1400 is 11 chunks of 128
+    residues (4 per lane) or 6 of 256: the four-warp handoff goes round its ring
+    more than once."""
     lens = [L, L - 1, 257, 256, 255, 129, 128, 127, 1, 0]
     ang, lengths, g = make_case(len(lens), L, 300 + L + rpt, lengths=lens)
-    rm.set_options(rpt, 0, 0, 0, 32)
+    rm.set_options(rpt, 0, 0, 0, cta)
     try:
         c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
     finally:
@@ -324,7 +329,8 @@ def test_one_warp_per_chain_ragged_and_unaligned(rm, rpt, L):
 def test_one_warp_per_chain_mixed_chunk_sizes_through_c_abi(built):
     """The backward starts its chunks from frames the forward recorded every 128
     residues, so a forward with 256-residue chunks and a backward with 128-residue
-    chunks (and the reverse) agree with the oracle."""
+    chunks (and the reverse) agree with the oracle, whether one warp or the four
+    warps of one CTA walked the chain in the forward."""
     from torchproteinlibrary_gb300 import capi
     lib = capi.lib()
     dev = torch.device("cuda")
@@ -334,8 +340,8 @@ def test_one_warp_per_chain_mixed_chunk_sizes_through_c_abi(built):
     a = torch.tensor(ang, dtype=torch.float32, device=dev)
     ln = torch.tensor(lengths, device=dev)
     gt = torch.tensor(g, dtype=torch.float32, device=dev)
-    for cf, cb in [(8, 4), (4, 8)]:
-        of, ob = capi.options(residues_per_thread=cf, threads_per_cta=32), \
+    for cf, tf, cb in [(8, 32, 4), (4, 32, 8), (8, 4, 4), (4, 4, 8)]:
+        of, ob = capi.options(residues_per_thread=cf, threads_per_cta=tf), \
             capi.options(residues_per_thread=cb, threads_per_cta=32)
         n = max(lib.tpl_a2b_workspace_bytes(B, L, ctypes.byref(of)), lib.tpl_a2b_workspace_bytes(B, L, ctypes.byref(ob)))
         ws = torch.zeros(n, dtype=torch.uint8, device=dev)
@@ -351,14 +357,15 @@ def test_one_warp_per_chain_mixed_chunk_sizes_through_c_abi(built):
               GRAD_TOL_F32)
 
 
-def test_one_warp_per_chain_graph_replay(rm):
+@pytest.mark.parametrize("cta", [32, 4])
+def test_one_warp_per_chain_graph_replay(rm, cta):
     dev = torch.device("cuda")
     B, L = 96, 500
     ang, lengths, g = make_case(B, L, 17)
     a = torch.tensor(ang, dtype=torch.float32, device=dev)
     ln = torch.tensor(lengths, device=dev)
     gt = torch.tensor(g, dtype=torch.float32, device=dev)
-    rm.set_options(8, 0, 0, 0, 32)
+    rm.set_options(8, 0, 0, 0, cta)
     try:
         ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
         coords = torch.empty(B, 9 * L, device=dev)
@@ -410,7 +417,7 @@ def test_sincos_error_bound(built):
     assert np.abs(sv * sv + cv * cv - 1.0).max() <= 3e-7
 
 
-def run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers=0):
+def run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers=0, scheme=0):
     """Forward with the current options, then the backward from its coordinates."""
     dev = torch.device("cuda")
     a = torch.tensor(ang, dtype=torch.float32, device=dev)
@@ -420,7 +427,7 @@ def run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers=0):
     coords = torch.full((B, 9 * L), float("nan"), device=dev)
     rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
     gi = torch.full((B, 3, L), float("nan"), device=dev)
-    rm.set_backward_options(rpt, buffers)
+    rm.set_backward_options(rpt, buffers, scheme)
     try:
         rm.Angles2BackboneGPU_backward_coords(gi, torch.tensor(g, dtype=torch.float32, device=dev), coords, ln, ws)
     finally:
@@ -429,15 +436,18 @@ def run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers=0):
     return coords.double().cpu().numpy(), gi.double().cpu().numpy()
 
 
+@pytest.mark.parametrize("scheme", [32, 4, 0])
 @pytest.mark.parametrize("rpt,buffers", [(4, 1), (4, 2), (8, 1)])
-@pytest.mark.parametrize("L", [1000, 1001, 258])
-def test_backward_from_coordinates_matches_oracle(rm, rpt, buffers, L):
+@pytest.mark.parametrize("L", [1000, 1001, 258, 1400])
+def test_backward_from_coordinates_matches_oracle(rm, rpt, buffers, L, scheme):
     """The float32 backward from the forward's output coordinates (bulk-copied chunk
-    rows when L % 4 == 0, single or double buffered; plain loads otherwise) against
-    the oracle."""
+    rows when L % 4 == 0, single or double buffered; plain loads otherwise), by one
+    warp per chain (scheme 32), by the four warps of one CTA per chain with the
+    carried sums handed round them (scheme 4) or as chosen from the length (0),
+    against the oracle."""
     lens = [L, L - 1, 257, 256, 255, 129, 128, 127, 2, 1, 0]
     ang, lengths, g = make_case(len(lens), L, 500 + L + rpt, lengths=lens)
-    c, gi = run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers)
+    c, gi = run_gpu_coords_backward(rm, ang, lengths, g, rpt, buffers, scheme)
     rc, rg = oracle_ref(ang, lengths, g, True)
     check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
 

@@ -2,7 +2,7 @@
 
 Knobs (tpl_options): residues per thread R (the scan tile is 32 R residues for
 warp tiles, 128 R for CTA tiles, a 32 R-residue chunk for one warp per chain),
-the scan scheme (warp tiles, CTA tiles, one warp per chain), the length from
+the scan scheme (warp tiles, CTA tiles, one warp or one CTA per chain), the length from
 which inter-tile carries are composed in FP64, and the residues per lane of the
 backward from coordinates.  For a shape
 (batch, max_len) the tuner times forward+backward of every candidate on
@@ -24,8 +24,9 @@ from . import load_extension
 CANDIDATES = [
     # (residues_per_thread, threads_per_cta)  threads_per_cta 1 = warp tiles, 128 = CTA tiles
     (1, 1), (2, 1), (4, 1), (8, 1), (2, 128), (4, 128), (8, 128),
-    # threads_per_cta 32 = one warp per chain, chunks of 32 R residues
-    (4, 32), (8, 32),
+    # threads_per_cta 32 = one warp per chain, chunks of 32 R residues; 4 = one CTA of four warps
+    # per chain, chunks dealt round the warps
+    (4, 32), (8, 32), (4, 4), (8, 4),
 ]
 COORD_BOUND = 1e-3  # A, against the FP64 form
 
@@ -114,8 +115,9 @@ def sweep(ang, lengths, up, candidates=CANDIDATES, carry_thresholds=(0,), steps=
     return out
 
 
-# backward from coordinates: (residues per lane, chunk buffers)
-COORDS_BWD_CANDIDATES = ((4, 1), (4, 2), (8, 1))
+# backward from coordinates: (residues per lane, chunk buffers, scheme: 32 = one warp per chain,
+# 4 = one CTA of four warps per chain)
+COORDS_BWD_CANDIDATES = ((4, 1, 32), (4, 2, 32), (8, 1, 32), (4, 1, 4), (4, 2, 4), (8, 1, 4))
 
 
 def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, steps=5):
@@ -131,8 +133,8 @@ def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, st
     gang = torch.empty(B, 3, L, device=ang.device)
     out = []
     try:
-        for c, nb in candidates:
-            rm.set_backward_options(c, nb)
+        for c, nb, sch in candidates:
+            rm.set_backward_options(c, nb, sch)
             for _ in range(2):
                 rm.Angles2BackboneGPU_backward_coords(gang, up, coords, lengths, ws)
             e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -142,8 +144,8 @@ def sweep_backward_coords(ang, lengths, up, candidates=COORDS_BWD_CANDIDATES, st
             e[1].record()
             torch.cuda.synchronize(ang.device)
             _, _, grel = _errors(rm, ang, lengths, up, coords, gang)
-            out.append({"residues_per_thread": c, "copy_buffers": nb, "bwd_ms": e[0].elapsed_time(e[1]) / steps,
-                        "grad_max_rel": grel})
+            out.append({"residues_per_thread": c, "copy_buffers": nb, "threads_per_cta": sch,
+                        "bwd_ms": e[0].elapsed_time(e[1]) / steps, "grad_max_rel": grel})
     finally:
         rm.set_backward_options(*saved)
     return out
@@ -155,7 +157,7 @@ def tune(ang, lengths, up, use_cache=True, steps=5):
     (what the float32 layer runs).  The returned dict describes the forward choice
     and carries the backward's under "backward_coords"."""
     rm = load_extension("_ReducedModel")
-    key = f"{torch.cuda.get_device_name(ang.device)}|{_bucket(ang.shape[0], ang.shape[2])}"
+    key = f"{torch.cuda.get_device_name(ang.device)}|{_bucket(ang.shape[0], ang.shape[2])}|v2"
     cache = _load_cache() if use_cache else {}
     rows, brows = [], []
     if key in cache and "backward_coords" in cache[key]:
@@ -172,7 +174,7 @@ def tune(ang, lengths, up, use_cache=True, steps=5):
             _save_cache(cache)
     rm.set_options(best["residues_per_thread"], best["fp64_carry_min_len"], 0, 0, best["threads_per_cta"])
     bc = best["backward_coords"]
-    rm.set_backward_options(bc["residues_per_thread"], bc.get("copy_buffers", 0))
+    rm.set_backward_options(bc["residues_per_thread"], bc.get("copy_buffers", 0), bc.get("threads_per_cta", 0))
     tune.last_sweep = rows
     tune.last_backward_sweep = brows
     return best

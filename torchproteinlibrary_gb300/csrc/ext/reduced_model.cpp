@@ -102,6 +102,7 @@ void Angles2BackboneGPU_backward(torch::Tensor gradInput, torch::Tensor gradOutp
 // saved; Angles2BackboneGPU_backward above keeps the reference's signature.
 int g_bwd_rpt = 0;  // residues per lane of the coordinate backward: 0 (= 4), 4 or 8
 int g_bwd_buffers = 0;  // chunk buffers of the coordinate backward: 0 (= 1), 1 or 2
+int g_bwd_scheme = 0;   // 0 (automatic) or 32 = one warp per chain, 4 = one CTA of four warps per chain
 
 void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor gradOutput, torch::Tensor output_coords,
                                         torch::Tensor angles_length, torch::Tensor A) {
@@ -122,19 +123,24 @@ void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor g
     tpl_options o = g_opt;
     o.residues_per_thread = g_bwd_rpt;
     o.copy_buffers = g_bwd_buffers;
+    o.threads_per_cta = g_bwd_scheme;
     const int s = tpl_a2b_backward_coords_f32(gradInput.data_ptr<float>(), gradOutput.data_ptr<float>(),
                                               output_coords.data_ptr<float>(), angles_length.data_ptr<int32_t>(),
                                               A.data_ptr(), A.nbytes(), (int)B, (int)L, &o, stream_of(gradInput));
     check_status(s, "Angles2BackboneGPU_backward_coords");
 }
 
-void set_backward_options(int64_t residues_per_thread, int64_t copy_buffers) {
+void set_backward_options(int64_t residues_per_thread, int64_t copy_buffers, int64_t threads_per_cta) {
     TORCH_CHECK(residues_per_thread == 0 || residues_per_thread == 4 || residues_per_thread == 8,
                 "residues_per_thread of the coordinate backward must be 0, 4 or 8");
     TORCH_CHECK(copy_buffers >= 0 && copy_buffers <= 2 && !(copy_buffers == 2 && residues_per_thread == 8),
                 "copy_buffers of the coordinate backward must be 0, 1 or 2 (2 with 4 residues per lane)");
+    TORCH_CHECK(threads_per_cta == 0 || threads_per_cta == 32 || threads_per_cta == 4,
+                "threads_per_cta of the coordinate backward must be 0 (automatic), 32 (one warp per chain) or 4 "
+                "(one CTA of four warps per chain)");
     g_bwd_rpt = (int)residues_per_thread;
     g_bwd_buffers = (int)copy_buffers;
+    g_bwd_scheme = (int)threads_per_cta;
 }
 
 void no_cpu_path(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
@@ -159,11 +165,12 @@ void set_options(int64_t residues_per_thread, int64_t fp64_carry_min_len, int64_
     tpl_options o = {(int)residues_per_thread, (int)threads_per_cta, (int)fp64_carry_min_len, (int)renormalize,
                      (int)max_ctas, g_opt.copy_buffers};
     TORCH_CHECK(o.threads_per_cta == 0 || o.threads_per_cta == 1 || o.threads_per_cta == 128 ||
-                    o.threads_per_cta == 32,
-                "threads_per_cta must be 0 (automatic), 1 (warp tiles), 128 (CTA tiles) or 32 (one warp per chain)");
-    TORCH_CHECK(o.threads_per_cta != 32 || o.residues_per_thread == 0 || o.residues_per_thread == 4 ||
-                    o.residues_per_thread == 8,
-                "one warp per chain takes residues_per_thread 4 or 8");
+                    o.threads_per_cta == 32 || o.threads_per_cta == 4,
+                "threads_per_cta must be 0 (automatic), 1 (warp tiles), 128 (CTA tiles), 32 (one warp per chain) "
+                "or 4 (one CTA of four warps per chain)");
+    TORCH_CHECK((o.threads_per_cta != 32 && o.threads_per_cta != 4) || o.residues_per_thread == 0 ||
+                    o.residues_per_thread == 4 || o.residues_per_thread == 8,
+                "one warp or one CTA per chain takes residues_per_thread 4 or 8");
     TORCH_CHECK(o.residues_per_thread == 0 || o.residues_per_thread == 1 || o.residues_per_thread == 2 ||
                     o.residues_per_thread == 4 || o.residues_per_thread == 8,
                 "residues_per_thread must be 0, 1, 2, 4 or 8");
@@ -191,8 +198,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Angles2BackboneGPU_backward_coords", &Angles2BackboneGPU_backward_coords,
           "float32 backward from the forward's output coordinates");
     m.def("set_backward_options", &set_backward_options,
-          "residues per lane and chunk buffers of the coordinate backward", py::arg("residues_per_thread") = 0,
-          py::arg("copy_buffers") = 0);
-    m.def("get_backward_options", []() { return std::vector<int64_t>{g_bwd_rpt, g_bwd_buffers}; },
-          "residues per lane and chunk buffers of the coordinate backward");
+          "residues per lane, chunk buffers and scheme of the coordinate backward",
+          py::arg("residues_per_thread") = 0, py::arg("copy_buffers") = 0, py::arg("threads_per_cta") = 0);
+    m.def("get_backward_options", []() { return std::vector<int64_t>{g_bwd_rpt, g_bwd_buffers, g_bwd_scheme}; },
+          "residues per lane, chunk buffers and scheme of the coordinate backward");
 }

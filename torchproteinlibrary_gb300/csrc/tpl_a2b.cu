@@ -1312,33 +1312,51 @@ static A2bShape a2b_shape(const tpl_options &opt, bool backward) {
     return s;
 }
 
-// threads_per_cta = 0: one warp per chain when the batch alone gives every SM at
-// least two chains (and residues_per_thread allows it), warp tiles otherwise.  The
-// forward and the backward of one shape make the same choice.
-static bool use_chain_scheme(const tpl_options &opt, int B) {
-    if (opt.threads_per_cta == 32) return true;
+static int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// threads_per_cta = 0 picks, from the shape, the scheme that measured fastest on
+// GB300 (4-residue-per-lane and 8-residue-per-lane chunks, one warp or one CTA of
+// four warps per chain, warp tiles; batches of 32 to 16384 chains of 64 to 1000
+// residues):
+//   * max_len >= 384: one CTA of four warps per chain (the chunks of a chain run on
+//     four warps at once), 8 residues per lane from max_len 768 and 4 below;
+//   * shorter chains: one warp per chain with 4 residues per lane when the batch
+//     gives every SM two chains, else one CTA of four warps per chain;
+//   * fewer than two chains per SM and chains over 4096 residues: warp tiles, whose
+//     look-back spreads one chain over many warps.
+// An explicit residues_per_thread of 4 or 8 is kept; 1 or 2 selects warp tiles.
+// The forward and the backward of one shape make the same choice.
+static bool use_chain_scheme(const tpl_options &opt, int B, int L) {
+    if (opt.threads_per_cta == 32 || opt.threads_per_cta == 4) return true;
     if (opt.threads_per_cta != 0) return false;
     const int r = opt.residues_per_thread;
     if (!(r == 0 || r == 4 || r == 8)) return false;
-    static int num_sms = 0;
-    if (!num_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (num_sms <= 0) num_sms = 1;
-    }
-    return B >= 2 * num_sms;
+    return !(B < 2 * num_sms() && L > 4096);
 }
 
-static tpl_options chain_options(const tpl_options &opt) {
+static tpl_options chain_options(const tpl_options &opt, int B, int L) {
     tpl_options o = opt;
-    o.threads_per_cta = 32;
+    if (o.threads_per_cta == 0) {
+        const bool ring = L >= 384 || B < 2 * num_sms();
+        o.threads_per_cta = ring ? 4 : 32;
+        if (o.residues_per_thread == 0) o.residues_per_thread = (ring && L >= 768) ? 8 : 4;
+    }
     if (o.residues_per_thread == 0) o.residues_per_thread = 8;
     return o;
 }
 
 int a2b_tile_for(const tpl_options &opt) {
-    if (opt.threads_per_cta == 32) return a2b_chain_record_stride();  // one warp per chain: frame records
+    if (opt.threads_per_cta == 32 || opt.threads_per_cta == 4)
+        return a2b_chain_record_stride();  // one warp or one CTA per chain: frame records
     A2bShape f = a2b_shape(opt, false);
     const int tile = f.R * f.NT;
     if (opt.threads_per_cta == 0) return std::min(tile, a2b_chain_record_stride());  // either scheme fits
@@ -1403,7 +1421,8 @@ static int launch_bwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
 int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, void *ws, int B, int L,
                     const tpl_options &opt, cudaStream_t st) {
     if (B == 0 || L == 0) return TPL_OK;
-    if (use_chain_scheme(opt, B)) return a2b_forward_chain(angles, lengths, coords, ws, B, L, chain_options(opt), st);
+    if (use_chain_scheme(opt, B, L))
+        return a2b_forward_chain(angles, lengths, coords, ws, B, L, chain_options(opt, B, L), st);
     A2bShape s = a2b_shape(opt, false);
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.coords = coords;
@@ -1428,8 +1447,8 @@ int a2b_forward_f32(const float *angles, const int32_t *lengths, float *coords, 
 int a2b_backward_f32(float *grad_angles, const float *grad_coords, const float *angles, const int32_t *lengths,
                      void *ws, int B, int L, const tpl_options &opt, cudaStream_t st) {
     if (B == 0 || L == 0) return TPL_OK;
-    if (use_chain_scheme(opt, B))
-        return a2b_backward_chain(grad_angles, grad_coords, angles, lengths, ws, B, L, chain_options(opt), st);
+    if (use_chain_scheme(opt, B, L))
+        return a2b_backward_chain(grad_angles, grad_coords, angles, lengths, ws, B, L, chain_options(opt, B, L), st);
     A2bShape s = a2b_shape(opt, true);
     A2bArgs a = make_args(angles, lengths, ws, B, L, s.R * s.NT, opt);
     a.grad_angles = grad_angles;

@@ -735,13 +735,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
     return false;
 }
 
-// Floats 4q..4q+3 of a lane's staged segment, fetched the first time residue r
-// (descending or ascending order alike) needs them.
-template <int C>
+// The float4s 4q..4q+3 of a lane's staged segment that residue r needs, each
+// fetched once when residues are visited in descending (DESC) or ascending order:
+// a float4 shared with the residue visited before is already in buf.
+template <bool DESC>
 __device__ __forceinline__ void fetch_residue(const float *seg, float *buf, int r, bool first) {
 #pragma unroll
     for (int q = (9 * r) / 4; q <= (9 * r + 8) / 4; q++)
-        if (first || q < (9 * (r + 1)) / 4) {
+        if (first || (DESC ? q < (9 * (r + 1)) / 4 : q > (9 * r - 1) / 4)) {
             const float4 v = reinterpret_cast<const float4 *>(seg)[q];
             buf[4 * q] = v.x; buf[4 * q + 1] = v.y; buf[4 * q + 2] = v.z; buf[4 * q + 3] = v.w;
         }
@@ -986,6 +987,345 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, coords_min_blocks(C, NB)) a
     }
 }
 
+// ------------------------------------------------- four warps per chain ("ring")
+// One CTA of kRingWarps warps owns one chain; chunk k belongs to warp k % 4 in the
+// forward and to warp (nchunk - 1 - k) % 4 in the backward, so a chain is split
+// into chunk-sized work items and a batch of equal chains no longer leaves most of
+// the GPU idle in a last partial wave of whole chains.  Each warp does the
+// expensive part of its chunk (walk and scan, or the staged sums) on its own; only
+// a 12-float carry passes between the warps of neighbouring chunks:
+//   forward:  the chain frame at the start of chunk k, from the warp of chunk k-1;
+//   backward: G and S of every atom after chunk k (S about the first N atom of
+//             chunk k+1) and that atom, from the warp of chunk k+1.
+// The carry goes through shared-memory slot k % 4 under named barrier 1 + k % 4
+// (64 threads: the producer warp arrives, the consumer warp syncs).  A slot and
+// its barrier are reused for the handoff into chunk k +- 4 only after the handoff
+// into chunk k completed, since the producer of the later handoff has itself
+// received the three handoffs in between.  Every warp runs every handoff of its
+// chunks whatever happens in them (chunks past the chain, a failed copy), so the
+// arrivals always match the syncs.
+
+constexpr int kRingWarps = 4;
+
+// Literal barrier ids, so that only barriers 1-4 are reserved for the CTA.
+__device__ __forceinline__ void ring_signal(int k) {
+    __syncwarp();
+    __threadfence_block();
+    switch (k & 3) {
+        case 0: asm volatile("bar.arrive 1, 64;" ::: "memory"); break;
+        case 1: asm volatile("bar.arrive 2, 64;" ::: "memory"); break;
+        case 2: asm volatile("bar.arrive 3, 64;" ::: "memory"); break;
+        default: asm volatile("bar.arrive 4, 64;" ::: "memory"); break;
+    }
+}
+__device__ __forceinline__ void ring_wait(int k) {
+    switch (k & 3) {
+        case 0: asm volatile("bar.sync 1, 64;" ::: "memory"); break;
+        case 1: asm volatile("bar.sync 2, 64;" ::: "memory"); break;
+        case 2: asm volatile("bar.sync 3, 64;" ::: "memory"); break;
+        default: asm volatile("bar.sync 4, 64;" ::: "memory"); break;
+    }
+}
+
+template <int C>
+__global__ void __launch_bounds__(32 * kRingWarps, fwd_min_blocks(C)) a2b_fwd_ring_kernel(ChainArgs a) {
+    constexpr int CH = 32 * C, SEG = 9 * C, SP = SEG + 4;
+    extern __shared__ __align__(16) float s_dyn[];
+    __shared__ __align__(16) float s_ring[kRingWarps][12];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = blockIdx.x;  // one CTA per chain: the grid is the batch
+    float *stage = s_dyn + w * 32 * SP;
+    float *seg = stage + lane * SP;
+    const int len = checked_length(a, b, lane);
+    const float *ang = a.angles + (size_t)b * 3 * a.L;
+    float *out = a.coords + (size_t)b * 9 * a.L;
+    ChainRecord *rec = a.rec + (size_t)b * a.nrec;
+    const bool vec = a.vec != 0;
+    const int nchunk = (a.L + CH - 1) / CH;
+
+#pragma unroll 1
+    for (int k = w; k < nchunk; k += kRingWarps) {
+        const int s0 = k * CH;
+        const int nout = min(CH, a.L - s0);
+        const bool live = s0 < len;
+        const int j0 = s0 + C * lane;
+        Frame<float> E, tot;
+        frame_identity(E);
+        frame_identity(tot);
+        if (live) {
+            const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg);
+            E = warp_exclusive_total(t, lane, a.renorm, tot);
+        }
+        Frame<float> F;  // chain frame at the chunk start
+        if (k == 0) {
+            frame_identity(F);
+        } else {
+            ring_wait(k);
+            frame_load(F, s_ring[k & 3]);
+        }
+        if (k + 1 < nchunk) {
+            Frame<float> Fn = compose(F, tot);
+            if (a.renorm) renormalize(Fn);
+            if (lane == 0) frame_store(s_ring[(k + 1) & 3], Fn);
+            ring_signal(k + 1);
+        }
+        float *dst = out + (size_t)9 * s0;
+        if (!live) {
+            zero_floats(dst, 9 * nout, lane, vec);
+            continue;
+        }
+        const Frame<float> P = compose(F, E);
+        if ((C * lane) % kRecordStride == 0 && j0 < len) frame_store(rec[j0 / kRecordStride].f, P);
+        map_positions<C>(seg, P, j0, len);
+        __syncwarp();
+        store_chunk<SEG, SP>(dst, stage, 9 * nout, lane, vec);
+        __syncwarp();  // the warp's next chunk rewrites the staging buffer
+    }
+}
+
+// Backward from the coordinates with the ring split of a2b_bwd_coords_kernel: the
+// same per-chunk evaluation, with the carried sums received from the warp of the
+// next chunk instead of kept in registers.
+template <int C, int NB>
+__global__ void __launch_bounds__(32 * kRingWarps, coords_min_blocks(C, NB)) a2b_bwd_coords_ring_kernel(ChainArgs a) {
+    constexpr int CH = 32 * C, SEG = 9 * C;
+    extern __shared__ __align__(16) float s_dyn[];
+    __shared__ __align__(8) uint64_t s_bar[kRingWarps][NB];
+    __shared__ __align__(16) float s_ring[kRingWarps][12];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = blockIdx.x;
+    float *sbase = s_dyn + (size_t)w * NB * 64 * SEG;
+    uint64_t *bars = s_bar[w];
+    const bool vec = a.vec != 0;
+    if (vec && lane == 0)
+        for (int i = 0; i < NB; i++) mbar_init(&bars[i]);
+    __syncwarp();
+    const int len = checked_length(a, b, lane);
+    const float *xin = a.coords + (size_t)b * 9 * a.L;
+    const float *gin = a.grad_coords + (size_t)b * 9 * a.L;
+    float *gout = a.grad_angles + (size_t)b * 3 * a.L;
+    const float inv_d0 = 1.f / a.bc.d[0], inv_d1 = 1.f / a.bc.d[1], inv_d2 = 1.f / a.bc.d[2];
+
+    const int nchunk = (len + CH - 1) / CH;
+    if (w == kRingWarps - 1) {  // gradient rows past the last chunk that holds residues are zero
+        const int s_end = min(a.L, nchunk * CH);
+        for (int k = 0; k < 3; k++)
+            zero_floats(gout + (size_t)k * a.L + s_end, a.L - s_end, lane, vec && (s_end % 4 == 0));
+    }
+    auto issue = [&](int kk, int q) {
+        if (lane == 0) {
+            const int n4 = (min(CH, len - kk * CH) + 3) & ~3;
+            float *bx = sbase + (size_t)q * 64 * SEG;
+            bulk_load_pair(bx, xin + (size_t)9 * kk * CH, bx + 32 * SEG, gin + (size_t)9 * kk * CH, 36u * (unsigned)n4,
+                           &bars[q]);
+        }
+    };
+    unsigned parity = 0;  // bit q: parity of buffer q's pending phase
+    bool failed = false;  // a bulk copy timed out: the remaining chunks only pass the carry on
+    const int first = nchunk - 1 - w;
+    if (vec && NB == 2 && first >= 0) issue(first, 0);
+#pragma unroll 1
+    for (int k = first, it = 0; k >= 0; k -= kRingWarps, it++) {
+        const int s0 = k * CH;
+        const int nreal = min(CH, len - s0);
+        const int q = NB == 2 ? (it & 1) : 0;
+        float *sx = sbase + (size_t)q * 64 * SEG;
+        float *sg = sx + 32 * SEG;
+        const float *xs = sx + lane * SEG, *gs = sg + lane * SEG;
+        __syncwarp();  // the previous chunk's reads of its buffers are done
+        if (vec && !failed) {
+            if (NB == 1) issue(k, 0);
+            else if (k - kRingWarps >= 0) issue(k - kRingWarps, q ^ 1);
+            const bool ok = mbar_wait(&bars[q], (parity >> q) & 1u);
+            parity ^= 1u << q;
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) record_error(a.hdr, TPL_ERR_LOOKBACK_TIMEOUT);
+                // bounded: let the copies in flight land before the buffers go unused
+                (void)mbar_wait(&bars[q], ((parity >> q) & 1u) ^ 1u);
+                if (NB == 2 && k - kRingWarps >= 0) (void)mbar_wait(&bars[q ^ 1], (parity >> (q ^ 1)) & 1u);
+                failed = true;
+            }
+        } else if (!vec) {
+            stage_chunk<SEG, SEG>(sx, xin + (size_t)9 * s0, 9 * nreal, lane, false);
+            stage_chunk<SEG, SEG>(sg, gin + (size_t)9 * s0, 9 * nreal, lane, false);
+            __syncwarp();
+        }
+        const int j0 = s0 + C * lane;
+        float o[3] = {0.f, 0.f, 0.f};  // chunk origin: its first N atom
+        float Gl[3] = {0.f, 0.f, 0.f}, Sl[3] = {0.f, 0.f, 0.f};
+        if (!failed) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) o[c] = sx[c];
+            float xb[9 * C], gb[9 * C];
+#pragma unroll
+            for (int r = 0; r < C; r++) {
+                fetch_residue<false>(xs, xb, r, r == 0);
+                fetch_residue<false>(gs, gb, r, r == 0);
+                if (j0 + r < len) {
+#pragma unroll
+                    for (int at = 0; at < 3; at++) {
+                        const float *x = xb + 9 * r + 3 * at, *g = gb + 9 * r + 3 * at;
+                        const float xr[3] = {x[0] - o[0], x[1] - o[1], x[2] - o[2]};
+                        float xg[3];
+                        cross3(xr, g, xg);
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            Gl[c] += g[c];
+                            Sl[c] += xg[c];
+                        }
+                    }
+                }
+            }
+        }
+        float G[3], S[3], tg[3], ts[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            G[i] = warp_suffix_excl(Gl[i], lane, tg[i]);
+            S[i] = warp_suffix_excl(Sl[i], lane, ts[i]);
+        }
+        // the carry from chunk k + 1, moved to this chunk's origin: S_o = S_oc + (oc - o) x Gc
+        float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, nN[3] = {0.f, 0.f, 0.f};
+        if (k + 1 < nchunk) {
+            ring_wait(k);
+            const float *cin = s_ring[k & 3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                Gc[c] = cin[c];
+                Sc[c] = cin[3 + c];
+                nN[c] = cin[6 + c];
+            }
+            const float d[3] = {nN[0] - o[0], nN[1] - o[1], nN[2] - o[2]};
+            float dx[3];
+            cross3(d, Gc, dx);
+#pragma unroll
+            for (int c = 0; c < 3; c++) Sc[c] += dx[c];
+        }
+        if (k > 0) {
+            if (lane == 0) {
+                float *cout = s_ring[(k - 1) & 3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    cout[c] = Gc[c] + tg[c];
+                    cout[3 + c] = Sc[c] + ts[c];
+                    cout[6 + c] = o[c];
+                }
+            }
+            ring_signal(k - 1);
+        }
+        if (failed) continue;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            G[i] += Gc[i];
+            S[i] += Sc[i];
+        }
+        // N after the lane's last residue: the next lane's first N, or the next chunk's
+        float nxt[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float nb = __shfl_down_sync(0xffffffffu, xs[c], 1);
+            nxt[c] = (lane == 31 ? nN[c] : nb) - o[c];
+        }
+        float gph[C], gps[C], gom[C];
+        {
+            float xb[9 * C], gb[9 * C];
+#pragma unroll
+            for (int r = C - 1; r >= 0; r--) {
+                fetch_residue<true>(xs, xb, r, r == C - 1);
+                fetch_residue<true>(gs, gb, r, r == C - 1);
+                const int j = j0 + r;
+                float xN[3], xA[3], xC[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    xN[c] = xb[9 * r + c] - o[c];
+                    xA[c] = xb[9 * r + 3 + c] - o[c];
+                    xC[c] = xb[9 * r + 6 + c] - o[c];
+                }
+                const float *gN = gb + 9 * r, *gA = gb + 9 * r + 3, *gC = gb + 9 * r + 6;
+                float u[3], tmp[3], cr[3];
+                // omega_j: axis C -> N_{j+1}, through N_{j+1}
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (nxt[c] - xC[c]) * inv_d2;
+                cross3(nxt, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gom[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                // psi_j: axis CA -> C, through C
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xC[c] - xA[c]) * inv_d1;
+                cross3(xC, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gps[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                const bool in = j < len;
+                if (in) {
+                    cross3(xC, gC, cr);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += gC[c];
+                        S[c] += cr[c];
+                    }
+                }
+                // phi_j: axis N -> CA, through CA
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[c] = (xA[c] - xN[c]) * inv_d0;
+                cross3(xA, G, cr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) tmp[c] = S[c] - cr[c];
+                gph[r] = u[0] * tmp[0] + u[1] * tmp[1] + u[2] * tmp[2];
+                if (in) {
+                    cross3(xA, gA, cr);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += gA[c];
+                        S[c] += cr[c];
+                    }
+                    cross3(xN, gN, cr);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] += gN[c];
+                        S[c] += cr[c];
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++) nxt[c] = xN[c];
+            }
+        }
+        // zeros at and past len; psi and omega of the last residue move nothing
+#pragma unroll
+        for (int r = 0; r < C; r++) {
+            const int j = j0 + r;
+            const bool ok = j < len, last = j == len - 1;
+            gph[r] = ok ? gph[r] : 0.f;
+            gps[r] = ok && !last ? gps[r] : 0.f;
+            gom[r] = ok && !last ? gom[r] : 0.f;
+        }
+        if (vec) {
+#pragma unroll
+            for (int i = 0; i < C / 4; i++) {
+                const int j = j0 + 4 * i;
+                if (j < a.L) {
+                    __stcs(reinterpret_cast<float4 *>(gout + j),
+                           make_float4(gph[4 * i], gph[4 * i + 1], gph[4 * i + 2], gph[4 * i + 3]));
+                    __stcs(reinterpret_cast<float4 *>(gout + a.L + j),
+                           make_float4(gps[4 * i], gps[4 * i + 1], gps[4 * i + 2], gps[4 * i + 3]));
+                    __stcs(reinterpret_cast<float4 *>(gout + 2 * a.L + j),
+                           make_float4(gom[4 * i], gom[4 * i + 1], gom[4 * i + 2], gom[4 * i + 3]));
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < C; r++) {
+                const int j = j0 + r;
+                if (j < a.L) {
+                    gout[j] = gph[r];
+                    gout[a.L + j] = gps[r];
+                    gout[2 * a.L + j] = gom[r];
+                }
+            }
+        }
+    }
+}
+
 // Sincos check kernel for the tests: s[i], c[i] = sincos_poly(a[i]).
 // Even elements through the paired form (the kernels' fast path), odd elements
 // through sincos_poly; |a| > 1e4 always through sincos_poly.
@@ -1039,6 +1379,14 @@ int launch_chain(K kernel, int smem, int B, const ChainArgs &a, cudaStream_t st)
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
+template <typename K>
+int launch_ring(K kernel, int smem, int B, const ChainArgs &a, cudaStream_t st) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return TPL_ERR_LAUNCH;
+    kernel<<<B, 32 * kRingWarps, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
 }  // namespace
 
 int a2b_chain_record_stride() { return kRecordStride; }
@@ -1050,9 +1398,14 @@ int a2b_forward_chain(const float *angles, const int32_t *lengths, float *coords
     a.coords = coords;
     a.vec = (L % 4 == 0) && aligned16(angles) && aligned16(coords);
     const int C = opt.residues_per_thread > 0 ? opt.residues_per_thread : 8;
+    const bool ring = opt.threads_per_cta == kRingWarps;
     switch (C) {
-        case 4: return launch_chain(a2b_fwd_chain_kernel<4>, fwd_smem<4>(), B, a, st);
-        case 8: return launch_chain(a2b_fwd_chain_kernel<8>, fwd_smem<8>(), B, a, st);
+        case 4:
+            return ring ? launch_ring(a2b_fwd_ring_kernel<4>, fwd_smem<4>(), B, a, st)
+                        : launch_chain(a2b_fwd_chain_kernel<4>, fwd_smem<4>(), B, a, st);
+        case 8:
+            return ring ? launch_ring(a2b_fwd_ring_kernel<8>, fwd_smem<8>(), B, a, st)
+                        : launch_chain(a2b_fwd_chain_kernel<8>, fwd_smem<8>(), B, a, st);
     }
     return TPL_ERR_UNSUPPORTED;
 }
@@ -1084,6 +1437,14 @@ int a2b_backward_coords(float *grad_angles, const float *grad_coords, const floa
     const int NB = opt.copy_buffers > 0 ? opt.copy_buffers : 1;
     constexpr int smem4 = kWarpsPerCta * 64 * 36 * (int)sizeof(float);
     constexpr int smem8 = kWarpsPerCta * 64 * 72 * (int)sizeof(float);
+    // automatic: four warps per chain from 384 residues (three or more 128-residue
+    // chunks), one warp per chain for shorter chains (measured on GB300)
+    if (opt.threads_per_cta == kRingWarps || (opt.threads_per_cta == 0 && L >= 384)) {
+        if (C == 4 && NB == 1) return launch_ring(a2b_bwd_coords_ring_kernel<4, 1>, smem4, B, a, st);
+        if (C == 4 && NB == 2) return launch_ring(a2b_bwd_coords_ring_kernel<4, 2>, 2 * smem4, B, a, st);
+        if (C == 8 && NB == 1) return launch_ring(a2b_bwd_coords_ring_kernel<8, 1>, smem8, B, a, st);
+        return TPL_ERR_UNSUPPORTED;
+    }
     if (C == 4 && NB == 1) return launch_chain(a2b_bwd_coords_kernel<4, 1>, smem4, B, a, st);
     if (C == 4 && NB == 2) return launch_chain(a2b_bwd_coords_kernel<4, 2>, 2 * smem4, B, a, st);
     if (C == 8 && NB == 1) return launch_chain(a2b_bwd_coords_kernel<8, 1>, smem8, B, a, st);

@@ -88,10 +88,11 @@ tpl_options resolve(const tpl_options *opt) {
 bool options_ok(const tpl_options &o) {
     const int r = o.residues_per_thread;
     if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8)) return false;
-    // 0: automatic, 1: warp tiles, 128: CTA tiles, 32: one warp per chain (4 or 8 residues per lane)
-    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 1 || o.threads_per_cta == 128 || o.threads_per_cta == 32))
-        return false;
-    if (o.threads_per_cta == 32 && !(r == 0 || r == 4 || r == 8)) return false;
+    // 0: automatic, 1: warp tiles, 128: CTA tiles, 32: one warp per chain, 4: one CTA of four warps per
+    // chain (both 4 or 8 residues per lane)
+    const int t = o.threads_per_cta;
+    if (!(t == 0 || t == 1 || t == 128 || t == 32 || t == 4)) return false;
+    if ((t == 32 || t == 4) && !(r == 0 || r == 4 || r == 8)) return false;
     if (o.max_ctas < 0) return false;
     if (o.copy_buffers < 0 || o.copy_buffers > 2) return false;
     return true;
@@ -196,6 +197,7 @@ int tpl_a2b_backward_coords_f32(float *grad_angles, const float *grad_coords, co
         return TPL_ERR_ARGUMENT;
     if (o.copy_buffers < 0 || o.copy_buffers > 2 || (o.copy_buffers == 2 && o.residues_per_thread == 8))
         return TPL_ERR_ARGUMENT;
+    if (!(o.threads_per_cta == 0 || o.threads_per_cta == 32 || o.threads_per_cta == 4)) return TPL_ERR_ARGUMENT;
     if (batch == 0 || max_len == 0) return TPL_OK;
     if (!grad_angles || !grad_coords || !coords || !lengths) return TPL_ERR_ARGUMENT;
     int s = check_ws(workspace, workspace_bytes, sizeof(WsHeader));
