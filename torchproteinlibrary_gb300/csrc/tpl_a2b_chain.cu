@@ -406,6 +406,47 @@ __device__ __forceinline__ void store_chunk(float *dst, const float *stage, int 
     }
 }
 
+// Staging layout of the forwards: lane l's 9C floats start at l SEG + GAP (l / 4).
+// With an odd number of float4s per lane (C = 4) the plain layout is already free of
+// bank conflicts; with an even number (C = 8) a 4-float gap after every four lanes
+// puts the 8 lanes of each 128-bit shared-memory phase on 8 different bank groups,
+// both for lane-local accesses and for the row-order reads of the store, at 32
+// floats of padding per warp.
+template <int C>
+struct FwdStage {
+    static constexpr int SEG = 9 * C;
+    static constexpr int GAP = ((SEG / 4) % 2 == 0) ? 4 : 0;
+    static constexpr int FLOATS = 32 * SEG + 8 * GAP;  // per warp
+    __device__ static __forceinline__ int lane_offset(int l) { return l * SEG + GAP * (l >> 2); }
+};
+
+// store_chunk for the FwdStage layout.
+template <int C>
+__device__ __forceinline__ void store_chunk_fwd(float *dst, const float *stage, int n, int lane, bool vec) {
+    using S = FwdStage<C>;
+    constexpr int SEG = S::SEG;
+    if (vec) {
+        constexpr int kStepSeg = 128 / SEG, kStepOff = 128 - kStepSeg * SEG;
+        int sl = (4 * lane) / SEG, off = 4 * lane - sl * SEG;
+#pragma unroll 2
+        for (int q = lane; 4 * q < n; q += 32) {
+            __stcs(reinterpret_cast<float4 *>(dst) + q,
+                   *reinterpret_cast<const float4 *>(stage + S::lane_offset(sl) + off));
+            sl += kStepSeg;
+            off += kStepOff;
+            if (off >= SEG) {
+                off -= SEG;
+                sl += 1;
+            }
+        }
+    } else {
+        for (int f = lane; f < n; f += 32) {
+            const int sl = f / SEG;
+            dst[f] = stage[S::lane_offset(sl) + f - sl * SEG];
+        }
+    }
+}
+
 __device__ __forceinline__ void zero_floats(float *dst, int n, int lane, bool vec) {
     if (vec) {
         for (int q = lane; 4 * q < n; q += 32) __stcs(reinterpret_cast<float4 *>(dst) + q, make_float4(0.f, 0.f, 0.f, 0.f));
@@ -428,13 +469,13 @@ constexpr int bwd_min_blocks(int C) { return C >= 8 ? 2 : 4; }
 
 template <int C>
 __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_chain_kernel(ChainArgs a) {
-    constexpr int CH = 32 * C, SEG = 9 * C, SP = SEG + 4;
+    constexpr int CH = 32 * C;
     extern __shared__ __align__(16) float s_dyn[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x * kWarpsPerCta + w;
     if (b >= a.B) return;  // warps are independent: no CTA-wide barrier follows
-    float *stage = s_dyn + w * 32 * SP;
-    float *seg = stage + lane * SP;
+    float *stage = s_dyn + w * FwdStage<C>::FLOATS;
+    float *seg = stage + FwdStage<C>::lane_offset(lane);
     const int len = checked_length(a, b, lane);
     const float *ang = a.angles + (size_t)b * 3 * a.L;
     float *out = a.coords + (size_t)b * 9 * a.L;
@@ -467,7 +508,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_
         if (a.renorm) renormalize(F);
         map_positions<C>(seg, P, j0, len);
         __syncwarp();
-        store_chunk<SEG, SP>(dst, stage, 9 * nout, lane, vec);
+        store_chunk_fwd<C>(dst, stage, 9 * nout, lane, vec);
         __syncwarp();  // the next chunk's walk rewrites the staging buffer
     }
 }
@@ -1006,6 +1047,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, coords_min_blocks(C, NB)) a
 // arrivals always match the syncs.
 
 constexpr int kRingWarps = 4;
+// 6 CTAs of 9.3 KB staging per warp (C = 8) or 7 (C = 4) fit an SM's shared memory
+constexpr int ring_fwd_min_blocks(int C) { return C >= 8 ? 6 : 7; }
 
 // Literal barrier ids, so that only barriers 1-4 are reserved for the CTA.
 __device__ __forceinline__ void ring_signal(int k) {
@@ -1028,14 +1071,14 @@ __device__ __forceinline__ void ring_wait(int k) {
 }
 
 template <int C>
-__global__ void __launch_bounds__(32 * kRingWarps, fwd_min_blocks(C)) a2b_fwd_ring_kernel(ChainArgs a) {
-    constexpr int CH = 32 * C, SEG = 9 * C, SP = SEG + 4;
+__global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_fwd_ring_kernel(ChainArgs a) {
+    constexpr int CH = 32 * C;
     extern __shared__ __align__(16) float s_dyn[];
     __shared__ __align__(16) float s_ring[kRingWarps][12];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;  // one CTA per chain: the grid is the batch
-    float *stage = s_dyn + w * 32 * SP;
-    float *seg = stage + lane * SP;
+    float *stage = s_dyn + w * FwdStage<C>::FLOATS;
+    float *seg = stage + FwdStage<C>::lane_offset(lane);
     const int len = checked_length(a, b, lane);
     const float *ang = a.angles + (size_t)b * 3 * a.L;
     float *out = a.coords + (size_t)b * 9 * a.L;
@@ -1078,7 +1121,7 @@ __global__ void __launch_bounds__(32 * kRingWarps, fwd_min_blocks(C)) a2b_fwd_ri
         if ((C * lane) % kRecordStride == 0 && j0 < len) frame_store(rec[j0 / kRecordStride].f, P);
         map_positions<C>(seg, P, j0, len);
         __syncwarp();
-        store_chunk<SEG, SP>(dst, stage, 9 * nout, lane, vec);
+        store_chunk_fwd<C>(dst, stage, 9 * nout, lane, vec);
         __syncwarp();  // the warp's next chunk rewrites the staging buffer
     }
 }
@@ -1347,11 +1390,11 @@ __global__ void sincos_poly_kernel(const float *a, float *s, float *c, int n) {
 
 template <int C>
 constexpr int fwd_smem() {
-    return kWarpsPerCta * 32 * (9 * C + 4) * (int)sizeof(float);
+    return kWarpsPerCta * FwdStage<C>::FLOATS * (int)sizeof(float);
 }
 template <int C>
-constexpr int bwd_smem() {
-    return 2 * fwd_smem<C>();
+constexpr int bwd_smem() {  // positions and dL/dx of every lane, padded lane stride 9C + 4
+    return kWarpsPerCta * 64 * (9 * C + 4) * (int)sizeof(float);
 }
 
 ChainArgs chain_args(const float *angles, const int32_t *lengths, void *ws, int B, int L, const tpl_options &opt) {
