@@ -390,9 +390,13 @@ def time_plain_fp64(rm, ang, lengths, up, dev, steps):
 def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
     """End to end through the public autograd layer: every step copies its angles,
     lengths and upstream gradient from pinned host memory, runs forward+backward,
-    and copies coordinates and dL/dangles back to pinned host memory.  Two CUDA
-    streams alternate so that one step's copies overlap the neighbouring step's
-    work (the serial figure is reported too)."""
+    and copies coordinates and dL/dangles back to pinned host memory.
+
+    Three streams form a pipeline over two buffer sets: host-to-device copies, the
+    layer, and device-to-host copies, ordered by events.  Step i+1's inputs travel
+    while step i's results come back, so both directions of the host link are busy
+    at once.  Also reported: the same copies with no kernels between them (the
+    floor the host link sets) and the steps run one at a time (serial)."""
     import torch
 
     B = ang_np.shape[0]
@@ -400,65 +404,75 @@ def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
     len_h = torch.from_numpy(len_np).pin_memory()
     up_h = torch.from_numpy(up_np).pin_memory()
     outs = [(torch.empty(B, 9 * L_RES).pin_memory(), torch.empty(ang_np.shape).pin_memory()) for _ in range(2)]
-    streams = [torch.cuda.Stream(device=dev) for _ in range(2)]
+    s_in, s_run, s_out = (torch.cuda.Stream(device=dev) for _ in range(3))
+    ins = [(torch.empty(ang_h.shape, device=dev), torch.empty(len_h.shape, dtype=len_h.dtype, device=dev),
+            torch.empty(up_h.shape, device=dev)) for _ in range(2)]
+    ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("in", "run", "out")}
+    started = [False, False]
 
-    def step(i):
-        s = streams[i % 2]
-        out_c, out_g = outs[i % 2]
-        with torch.cuda.stream(s):
-            a = ang_h.to(dev, non_blocking=True).requires_grad_()
-            ln = len_h.to(dev, non_blocking=True)
-            u = up_h.to(dev, non_blocking=True)
-            c = layer(a, ln)
-            c.backward(u)
-            out_c.copy_(c.detach(), non_blocking=True)
-            out_g.copy_(a.grad, non_blocking=True)
-
-    for i in range(2):
-        step(i)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    for i in range(steps):
-        step(i)
-    torch.cuda.synchronize(dev)
-    ms = (time.perf_counter() - t0) * 1e3 / steps
-    t0 = time.perf_counter()
-    for i in range(steps):
-        step(0)
-        torch.cuda.synchronize(dev)
-    ms_serial = (time.perf_counter() - t0) * 1e3 / steps
-    # the same copies with no work between them: the floor that the host link sets
-    dev_bufs = [(torch.empty(ang_h.shape, device=dev), torch.empty(len_h.shape, dtype=len_h.dtype, device=dev),
-                 torch.empty(up_h.shape, device=dev), torch.zeros(outs[0][0].shape, device=dev),
-                 torch.zeros(outs[0][1].shape, device=dev)) for _ in range(2)]
-
-    def copies(i):
-        a, ln, u, c, g = dev_bufs[i % 2]
-        out_c, out_g = outs[i % 2]
-        with torch.cuda.stream(streams[i % 2]):
+    def step(i, compute=True):
+        k = i % 2
+        a, ln, u = ins[k]
+        out_c, out_g = outs[k]
+        with torch.cuda.stream(s_in), torch.no_grad():
+            if started[k]:
+                s_in.wait_event(ev["run"][k])  # step i-2 has finished reading buffer set k
             a.copy_(ang_h, non_blocking=True)
             ln.copy_(len_h, non_blocking=True)
             u.copy_(up_h, non_blocking=True)
-            out_c.copy_(c, non_blocking=True)
-            out_g.copy_(g, non_blocking=True)
+            ev["in"][k].record(s_in)
+        with torch.cuda.stream(s_run):
+            s_run.wait_event(ev["in"][k])
+            if started[k]:
+                s_run.wait_event(ev["out"][k])  # step i-2's results have left buffer set k
+            if compute:
+                a.grad = None
+                a.requires_grad_()
+                c = layer(a, ln)
+                c.backward(u)
+                res = (c.detach(), a.grad)
+            else:
+                res = (a, u)  # same byte counts as the results: 9L and 3L floats per chain
+            ev["run"][k].record(s_run)
+        with torch.cuda.stream(s_out), torch.no_grad():
+            s_out.wait_event(ev["run"][k])
+            for t in res:
+                t.record_stream(s_out)
+            if compute:
+                out_c.copy_(res[0], non_blocking=True)
+                out_g.copy_(res[1], non_blocking=True)
+            else:
+                out_g.copy_(res[0], non_blocking=True)
+                out_c.copy_(res[1], non_blocking=True)
+            ev["out"][k].record(s_out)
+        started[k] = True
 
-    for i in range(2):
-        copies(i)
-    torch.cuda.synchronize(dev)
+    def timed(compute):
+        for i in range(2):
+            step(i, compute)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for i in range(steps):
+            step(i, compute)
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t0) * 1e3 / steps
+
+    ms = timed(True)
+    ms_copies = timed(False)
     t0 = time.perf_counter()
     for i in range(steps):
-        copies(i)
-    torch.cuda.synchronize(dev)
-    ms_copies = (time.perf_counter() - t0) * 1e3 / steps
+        step(i)
+        torch.cuda.synchronize(dev)
+    ms_serial = (time.perf_counter() - t0) * 1e3 / steps
     h2d = ang_np.nbytes + len_np.nbytes + up_np.nbytes
     d2h = outs[0][0].numel() * 4 + outs[0][1].numel() * 4
     return {"value": B * L_RES / (ms / 1e3), "unit": "residues/s", "ms_per_step": ms,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "serial_ms_per_step": ms_serial,
             "copies_only_ms_per_step": ms_copies,
-            "copies_only_note": "the same pinned copies on the same two streams with no kernels: the host-link floor",
+            "copies_only_note": "the same pinned copies on the same streams with no kernels: the host-link floor",
             "api": "torchproteinlibrary_gb300.ReducedModel.Angles2Backbone (autograd), pinned host buffers, "
-                   "two streams alternating"}
+                   "three-stream pipeline (copies in, layer, copies out) over two buffer sets"}
 
 
 def time_a2c(dev, steps=10, seed=1004):

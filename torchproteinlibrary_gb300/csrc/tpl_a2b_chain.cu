@@ -800,8 +800,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, coords_min_blocks(C, NB)) a
     extern __shared__ __align__(16) float s_dyn[];
     __shared__ __align__(8) uint64_t s_bar[kWarpsPerCta][NB];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int b = blockIdx.x * kWarpsPerCta + w;
-    if (b >= a.B) return;  // warps are independent
+    const int idx = blockIdx.x * kWarpsPerCta + w;
+    if (idx >= a.B) return;  // warps are independent
+    const int b = a.B - 1 - idx;  // chains last to first, as in a2b_bwd_coords_ring_kernel
     // per buffer: coordinates of a chunk (contiguous as in the row), then its dL/dx
     float *sbase = s_dyn + (size_t)w * NB * 64 * SEG;
     uint64_t *bars = s_bar[w];
@@ -1136,7 +1137,9 @@ __global__ void __launch_bounds__(32 * kRingWarps, coords_min_blocks(C, NB)) a2b
     __shared__ __align__(8) uint64_t s_bar[kRingWarps][NB];
     __shared__ __align__(16) float s_ring[kRingWarps][12];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int b = blockIdx.x;
+    // chains last to first: CTAs are dispatched in index order, so the first ones
+    // read the rows the forward wrote last, which may still be in L2
+    const int b = a.B - 1 - (int)blockIdx.x;
     float *sbase = s_dyn + (size_t)w * NB * 64 * SEG;
     uint64_t *bars = s_bar[w];
     const bool vec = a.vec != 0;
