@@ -531,22 +531,37 @@ def time_a2c(dev, steps=10, seed=1004):
         gup = torch.from_numpy(g.standard_normal((B, 3 * maxA))).to(dev, dt) if name == "f32" else \
             outs["f32"][2].to(dt)
         ga = torch.empty_like(a)
+
+        def bwd():  # what the autograd layer runs: float32 from the coordinates, float64 rebuilding the tree
+            if name == "f32":
+                fm.Angles2Coords_backward_coords(gup, ga, seq, c)
+            else:
+                fm.Angles2Coords_backward(gup, ga, seq, a)
+
         for _ in range(2):
             fm.Angles2Coords_forward(seq, a, c, rn, an)
-            fm.Angles2Coords_backward(gup, ga, seq, a)
+            bwd()
         torch.cuda.synchronize(dev)
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         n = steps if name == "f32" else max(1, steps // 4)
         e[0].record()
         for _ in range(n):
             fm.Angles2Coords_forward(seq, a, c, rn, an)
         e[1].record()
         for _ in range(n):
-            fm.Angles2Coords_backward(gup, ga, seq, a)
+            bwd()
         e[2].record()
+        if name == "f32":
+            ga_tree = torch.empty_like(a)
+            for _ in range(n):
+                fm.Angles2Coords_backward(gup, ga_tree, seq, a)
+        e[3].record()
         torch.cuda.synchronize(dev)
         fms, bms = e[0].elapsed_time(e[1]) / n, e[1].elapsed_time(e[2]) / n
         res[name] = {"residues_per_s": float(lens.sum()) / ((fms + bms) / 1e3), "fwd_ms": fms, "bwd_ms": bms}
+        if name == "f32":
+            res[name]["bwd_tree_ms"] = e[2].elapsed_time(e[3]) / n
+            res[name]["bwd"] = "from the forward's coordinates (the layer's float32 backward)"
         outs[name] = (c.double(), ga.double(), gup)
     d = (outs["f32"][0] - outs["f64"][0]).view(B, -1, 3).norm(dim=-1)
     ge = (outs["f32"][1] - outs["f64"][1]).abs().max() / outs["f64"][1].abs().max()
@@ -627,7 +642,10 @@ def time_training_step(dev, steps=10, seed=1004):
             fm.Angles2Coords_forward(seq, xd, c, e_u8, e_u8)
             rm_.Coords2RMSDGPU_forward_centering(c, target, out, na, UT, cent)
             rm_.Coords2RMSDGPU_backward(g_r, c, target, na, out, UT, cent, g_c, 1)
-            fm.Angles2Coords_backward(g_c, g_a, seq, xd)
+            if dt == torch.float32:  # the layer's float32 backward: from the forward's coordinates
+                fm.Angles2Coords_backward_coords(g_c, g_a, seq, c)
+            else:
+                fm.Angles2Coords_backward(g_c, g_a, seq, xd)
 
         st_ = torch.cuda.Stream(device=dev)
         st_.wait_stream(torch.cuda.current_stream(dev))
@@ -721,8 +739,16 @@ def main():
     ap.add_argument("--bwd-cta", type=int, default=0, help="coordinate backward: 0 = automatic, 32 = one warp per chain, 4 = one CTA of four warps per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
+    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform"],
+                    help="run one secondary leg alone and print its result (profiling); no metric line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "ours" else args.warmup
+    if args.leg:
+        import torch
+        dev = torch.device("cuda", 0)
+        fn = {"a2c": time_a2c, "training_step": time_training_step, "coords_transform": time_coords_transform}[args.leg]
+        print(json.dumps({"leg": args.leg, "result": fn(dev)}, default=float))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

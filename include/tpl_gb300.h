@@ -185,6 +185,22 @@ int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const u
                          const double *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
                          int max_atoms, const tpl_options *opt, void *stream);
 
+/* Angles2Coords backward, FP32, from the forward's output coordinates.  Also
+ * replaces Angles2Coords_backward (angles2coords_interface.cpp:76-115,
+ * cConformation.cpp:180-211), whose tree walk recomputes every joint transform.
+ * Every joint's origin is an atom of the forward's output (N, CA and C for the
+ * backbone; the first atom of each side-chain group) and every rotation axis is a
+ * bond between two such atoms, so dL/dangle = u . sum over the joint's subtree of
+ * (x - o) x g is evaluated from coords and grad_coords without rebuilding the
+ * chain.  coords must be the unmodified output of tpl_a2c_forward_f32 for the same
+ * sequences and angles.  Same outputs and zeros as tpl_a2c_backward_f32; the
+ * gradient's error against FP64 is about 1e-5 of its largest entry, since the axes
+ * come from FP32 coordinate differences.  The workspace only needs its status word
+ * (>= 64 bytes, zeroed once). */
+int tpl_a2c_backward_coords_f32(float *grad_angles, const float *grad_coords, const float *coords,
+                                const uint8_t *sequences, int seq_stride, void *workspace, size_t workspace_bytes,
+                                int batch, int max_len, int max_atoms, void *stream);
+
 /* Angles2Backbone forward, batched FP32, for callers that cannot allocate device
  * memory.  This entry point has no counterpart in the reference.
  *

@@ -28,7 +28,7 @@ def fm(built):
     return load_extension("_FullAtomModel")
 
 
-def run_gpu(fm, ang, seqs, g, dtype):
+def run_gpu(fm, ang, seqs, g, dtype, from_coords=False):
     from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
     dev = torch.device("cuda")
     a = torch.tensor(ang, dtype=dtype, device=dev)
@@ -42,7 +42,10 @@ def run_gpu(fm, ang, seqs, g, dtype):
     fm.Angles2Coords_forward(seq, a, coords, rn, an)
     gi = torch.full_like(a, float("nan"))
     gt = torch.tensor(g, dtype=dtype, device=dev) if g is not None else torch.zeros_like(coords)
-    fm.Angles2Coords_backward(gt, gi, seq, a)
+    if from_coords:
+        fm.Angles2Coords_backward_coords(gt, gi, seq, coords)
+    else:
+        fm.Angles2Coords_backward(gt, gi, seq, a)
     assert fm.workspace_status(0) == 0
     return (coords.double().cpu().numpy(), rn.cpu().numpy(), an.cpu().numpy(), np.array(na, np.int32),
             gi.double().cpu().numpy())
@@ -261,3 +264,78 @@ def test_config4_ragged_fp32_vs_fp64(fm):
         finally:
             fm.set_options(0)
         check(c32, g32, c64, g64, na, COORD_TOL_F32, GRAD_TOL_F32)
+    c32, _, _, _, g32 = run_gpu(fm, ang, seqs, g, torch.float32, from_coords=True)
+    check(c32, g32, c64, g64, na, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def coords_case(seed):
+    """Chains ending on and beside the 256-residue tiles of the coordinate backward,
+    one- and two-residue chains, an empty one, and one with all 20 residue types."""
+    rng = np.random.default_rng(seed)
+    lens = [0, 1, 2, 255, 256, 257, 300, 513]
+    seqs = ["".join(rng.choice(list(AA), n)) for n in lens] + [AA, "GP" * 10, "W" * 40]
+    L = 520
+    ang = rng.uniform(-np.pi, np.pi, (len(seqs), 8, L)).astype(np.float32).astype(np.float64)
+    ang[:, 2] = rng.normal(np.pi, 0.05, (len(seqs), L)).astype(np.float32)
+    rc, rrn, ran, na = oracle.a2c_forward(ang, seqs)
+    g = rng.standard_normal(rc.shape).astype(np.float32).astype(np.float64)
+    for b, n in enumerate(na):
+        g[b, 3 * n:] = 0
+    return seqs, ang, rc, na, g
+
+
+def test_backward_from_coordinates_matches_oracle(fm):
+    """The float32 backward from the forward's output coordinates (what the
+    float32 layer runs) against the oracle, with NaN in dL/dx past every chain's
+    atoms (ignored)."""
+    seqs, ang, rc, na, g = coords_case(61)
+    rg = oracle.a2c_backward(g, ang, seqs)
+    g_nan = g.copy()
+    for b, n in enumerate(na):
+        g_nan[b, 3 * n:] = np.nan
+    c, _, _, _, gi = run_gpu(fm, ang, seqs, g_nan, torch.float32, from_coords=True)
+    assert np.isfinite(gi).all()
+    check(c, gi, rc, rg, na, COORD_TOL_F32, GRAD_TOL_F32)
+    assert np.all(gi[0] == 0.0)
+
+
+def test_backward_from_coordinates_c_abi_and_layer(fm, built):
+    """Through the C ABI (status-word workspace only), bit-identical to the
+    extension entry; and the float32 autograd layer's gradient (from coordinates)
+    against the tree-rebuilding backward selected by backward_from_coords = False."""
+    import ctypes
+    from torchproteinlibrary_gb300 import capi
+    from torchproteinlibrary_gb300.FullAtomModel import Angles2Coords
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords.Angles2Coords import Angles2CoordsFunction
+    seqs, ang, rc, na, g = coords_case(62)
+    dev = torch.device("cuda")
+    c, _, _, _, gi = run_gpu(fm, ang, seqs, g, torch.float32, from_coords=True)
+    lib = capi.lib()
+    seq = convertStringList(seqs).to(dev)
+    B, _, L = ang.shape
+    maxA = int(max(na))
+    ct = torch.tensor(c, dtype=torch.float32, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    out = torch.full((B, 8, L), float("nan"), device=dev)
+    ws = torch.zeros(64, dtype=torch.uint8, device=dev)
+    capi.check(lib.tpl_a2c_backward_coords_f32(out.data_ptr(), gt.data_ptr(), ct.data_ptr(), seq.data_ptr(),
+                                               seq.shape[1], ws.data_ptr(), 64, B, L, maxA, capi.stream_ptr()),
+               "a2c backward from coordinates")
+    torch.cuda.synchronize()
+    assert ws[:4].view(torch.int32).item() == 0
+    np.testing.assert_array_equal(out.double().cpu().numpy(), gi)
+    layer = Angles2Coords()
+    grads = {}
+    for flag in (True, False):
+        Angles2CoordsFunction.backward_from_coords = flag
+        try:
+            x = torch.tensor(ang, dtype=torch.float32, device=dev, requires_grad=True)
+            coords = layer(x, seqs)[0]
+            coords.backward(gt)
+            grads[flag] = x.grad.double().cpu().numpy()
+        finally:
+            Angles2CoordsFunction.backward_from_coords = True
+    scale = max(1.0, np.abs(grads[False]).max())
+    assert np.abs(grads[True] - grads[False]).max() <= GRAD_TOL_F32 * scale
+    np.testing.assert_array_equal(grads[True], gi)

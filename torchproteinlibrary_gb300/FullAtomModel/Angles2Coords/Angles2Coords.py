@@ -15,6 +15,10 @@ Differences from the reference:
     so repeated calls with the same sequences skip the per-sequence Python loop.
   * Unknown residue letters raise instead of being skipped.
   * The NaN check (a host sync) runs only when TPL_CHECK_NAN=1.
+  * float32: the forward saves its output coordinates and the backward reads every
+    joint's origin and axis from them (tpl_a2c_backward_coords_f32) instead of
+    rebuilding the tree; ``Angles2CoordsFunction.backward_from_coords = False``
+    selects the rebuilding backward (the reference's entry point).
 """
 import math
 import os
@@ -60,6 +64,8 @@ def _check(t, where, device):
 class Angles2CoordsFunction(Function):
     """Protein angles -> coordinates function"""
 
+    backward_from_coords = True
+
     @staticmethod
     def forward(ctx, input_angles, sequenceTensor, num_atoms):
         input_angles = input_angles.contiguous()
@@ -72,16 +78,24 @@ class Angles2CoordsFunction(Function):
         atom_names = torch.empty(batch_size, max_num_atoms, 4, dtype=torch.uint8, device=dev)
         _FullAtomModel.Angles2Coords_forward(seq, input_angles, coords, res_names, atom_names)
         _check(coords, "forward", dev)
-        ctx.save_for_backward(input_angles, seq)
+        ctx.from_coords = Angles2CoordsFunction.backward_from_coords and input_angles.dtype == torch.float32
+        if ctx.from_coords:
+            ctx.save_for_backward(input_angles, seq, coords)
+        else:
+            ctx.save_for_backward(input_angles, seq)
         ctx.mark_non_differentiable(res_names, atom_names, num_atoms)
         return coords, res_names, atom_names, num_atoms
 
     @staticmethod
     def backward(ctx, grad_atoms, *kwargs):
-        input_angles, seq = ctx.saved_tensors
+        saved = ctx.saved_tensors
+        input_angles, seq = saved[0], saved[1]
         grad_atoms = grad_atoms.contiguous()
         grad_angles = torch.empty_like(input_angles)
-        _FullAtomModel.Angles2Coords_backward(grad_atoms, grad_angles, seq, input_angles)
+        if ctx.from_coords:
+            _FullAtomModel.Angles2Coords_backward_coords(grad_atoms, grad_angles, seq, saved[2])
+        else:
+            _FullAtomModel.Angles2Coords_backward(grad_atoms, grad_angles, seq, input_angles)
         _check(grad_angles, "backward", input_angles.device)
         return grad_angles, None, None
 

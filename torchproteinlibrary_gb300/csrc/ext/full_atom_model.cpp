@@ -136,6 +136,34 @@ void Angles2Coords_backward(torch::Tensor grad_atoms, torch::Tensor grad_angles,
     check_status(s, "Angles2Coords_backward");
 }
 
+// Backward of the float32 path from the forward's output coordinates (no tree
+// rebuild).  Not a reference entry point: the Python layer calls it with the
+// coordinates it saved; Angles2Coords_backward above keeps the reference's signature.
+void Angles2Coords_backward_coords(torch::Tensor grad_atoms, torch::Tensor grad_angles, torch::Tensor sequences,
+                                   torch::Tensor coords) {
+    TORCH_CHECK(coords.is_cuda() && grad_atoms.is_cuda() && grad_angles.is_cuda(),
+                "tensors must be CUDA tensors (this build has no CPU path)");
+    TORCH_CHECK(coords.is_contiguous() && grad_atoms.is_contiguous() && grad_angles.is_contiguous(),
+                "tensors must be contiguous");
+    TORCH_CHECK(grad_angles.dim() == 3 && grad_angles.size(1) == 8, "grad_angles must be [batch, 8, max_len]");
+    TORCH_CHECK(coords.scalar_type() == torch::kFloat && grad_atoms.scalar_type() == torch::kFloat &&
+                    grad_angles.scalar_type() == torch::kFloat,
+                "the coordinate backward is float32");
+    const int64_t B = grad_angles.size(0), L = grad_angles.size(2);
+    TORCH_CHECK(grad_atoms.dim() == 2 && grad_atoms.size(0) == B && grad_atoms.size(1) % 3 == 0 &&
+                    coords.sizes() == grad_atoms.sizes(),
+                "grad_atoms and coords must be [batch, 3 * max_atoms]");
+    const int64_t maxA = grad_atoms.size(1) / 3;
+    const at::cuda::CUDAGuard guard(coords.device());
+    auto seq = seq_on(sequences, coords.device());
+    auto ws = status_ws(coords.device());
+    const int s = tpl_a2c_backward_coords_f32(grad_angles.data_ptr<float>(), grad_atoms.data_ptr<float>(),
+                                              coords.data_ptr<float>(), seq.data_ptr<uint8_t>(), (int)seq.size(1),
+                                              ws.data_ptr(), ws.nbytes(), (int)B, (int)L, (int)maxA,
+                                              stream_of(coords));
+    check_status(s, "Angles2Coords_backward_coords");
+}
+
 int64_t getSeqNumAtoms(const std::string &sequence) {
     int n = tpl_num_atoms(sequence.c_str());
     TORCH_CHECK(n >= 0, "Unknown atom/res names in sequence '", sequence, "'");
@@ -489,6 +517,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Coords2TypedCoords_backward", &Coords2TypedCoords_backward, "Coords2TypedCoords backward (GPU)");
     m.def("Angles2Coords_forward", &Angles2Coords_forward, "Angles2Coords forward");
     m.def("Angles2Coords_backward", &Angles2Coords_backward, "Angles2Coords backward");
+    m.def("Angles2Coords_backward_coords", &Angles2Coords_backward_coords,
+          "float32 Angles2Coords backward from the forward's output coordinates");
     m.def("Angles2Coords_save", &Angles2Coords_save, "Angles2Coords save");
     m.def("getSeqNumAtoms", &getSeqNumAtoms, "Get number of atoms in a sequence");
     m.def("workspace_status", &workspace_status, "synchronise and read the first device-detected error");

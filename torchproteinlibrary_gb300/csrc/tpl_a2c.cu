@@ -600,6 +600,227 @@ __global__ void __launch_bounds__(NT) a2c_bwd_kernel(A2cArgs<T> a, int renorm, i
         for (int i = from + tid; i < a.L; i += NT) gout[(size_t)k * a.L + i] = T(0);
 }
 
+// ------------------------------------------------- backward from the coordinates
+// The forward's output holds the origin of every joint: N, CA and C for the
+// backbone, and for each side-chain joint the first atom of its group, which sits
+// at the joint's origin (every group of the table starts at its local origin).
+// Each rotation axis is a bond of known length: u = (origin - parent origin) / d,
+// with CA as the parent of the first side-chain joint (the dummy joint has no
+// length).  So dL/dalpha = u . (S - o x G) over the joint's subtree needs only the
+// coordinates and dL/dx, and this backward never rebuilds the tree.  Per tile of NT
+// residues, last to first, the CTA stages the tile's atoms and dL/dx (plus the
+// first atom after the tile), each thread sums G and S over its residue's atoms, a
+// block suffix scan adds the later residues and the carry of later tiles, and each
+// thread visits its residue's atoms last to first:
+//   omega_j  subtree: every later residue        axis C_j -> N_j+1, origin N_j+1
+//   psi_j    + O_j                                axis CA_j -> C_j,  origin C_j
+//   chi_k    side-chain groups k.. only           axis o_k-1 -> o_k, origin o_k
+//   phi_j    + side chain + C_j                   axis N_j -> CA_j,  origin CA_j
+// Positions are taken relative to the tile's first N atom to keep the sums small.
+template <int NT>
+struct A2cCoordsSmem {
+    Topology<float> topo;
+    float x[(NT * kMaxResAtoms + 1) * 3];
+    float g[(NT * kMaxResAtoms + 1) * 3];
+    signed char lut[256];
+};
+
+__device__ __forceinline__ float joint_grad(const float *o, const float *p_prev, float inv_d, const float *G,
+                                            const float *S) {
+    float cr[3];
+    cross3(o, G, cr);
+    return ((o[0] - p_prev[0]) * (S[0] - cr[0]) + (o[1] - p_prev[1]) * (S[1] - cr[1]) +
+            (o[2] - p_prev[2]) * (S[2] - cr[2])) *
+           inv_d;
+}
+
+// Sum of v over lanes above this one (exclusive suffix), and the warp total.
+__device__ __forceinline__ float suffix_excl(float v, int lane, float &total) {
+    float inc = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, inc, off);
+        if (lane + off < 32) inc += o;
+    }
+    total = __shfl_sync(0xffffffffu, inc, 0);
+    return inc - v;
+}
+
+__device__ __forceinline__ void add_atom(const float *xs, const float *gs, const float *o, float *G, float *S) {
+    const float xr[3] = {xs[0] - o[0], xs[1] - o[1], xs[2] - o[2]};
+    float xg[3];
+    cross3(xr, gs, xg);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        G[c] += gs[c];
+        S[c] += xg[c];
+    }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) a2c_bwd_coords_kernel(A2cArgs<float> a) {
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    A2cCoordsSmem<NT> &sm = *reinterpret_cast<A2cCoordsSmem<NT> *>(smem_raw);
+    __shared__ int s_len, s_bad, s_wcnt[NW];
+    __shared__ float s_wsum[NW][6];
+
+    const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    load_topology<float, NT>(sm.topo, sm.lut);
+    const Topology<float> &tp = sm.topo;
+    const unsigned char *row = a.seq + (size_t)b * a.seq_stride;
+    const int len = chain_length<NT>(row, a.seq_stride, sm.lut, &s_len, &s_bad);
+    float *gout = a.grad_angles + (size_t)b * 8 * a.L;
+    const float *xin = a.coords + (size_t)b * 3 * a.maxA;
+    const float *gin = a.grad_coords + (size_t)b * 3 * a.maxA;
+    bool ok = !s_bad && len <= a.L;
+
+    // atoms of the whole chain: the last tile ends there
+    int cnt = 0;
+    if (ok)
+        for (int j = tid; j < len; j += NT) cnt += tp.natoms[sm.lut[row[j]]];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+    if (lane == 0) s_wcnt[w] = cnt;
+    __syncthreads();
+    int total = 0;
+#pragma unroll
+    for (int q = 0; q < NW; q++) total += s_wcnt[q];
+    if (tid == 0) {
+        if (s_bad) a2c_error(a.hdr, TPL_ERR_SEQUENCE);
+        if (len > a.L) a2c_error(a.hdr, TPL_ERR_LENGTH);
+        if (ok && total > a.maxA) a2c_error(a.hdr, TPL_ERR_ATOMS);
+    }
+    if (total > a.maxA) ok = false;
+    __syncthreads();  // s_wcnt is reused below
+
+    const int ntiles = ok ? (len + NT - 1) / NT : 0;
+    const float inv_dphi = 1.f / tp.bb_d[0], inv_dpsi = 1.f / tp.bb_d[1], inv_dom = 1.f / tp.bb_d[2];
+    float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, oc[3] = {0.f, 0.f, 0.f};  // atoms after the tile
+    int abase_next = total;
+    for (int t = ntiles - 1; t >= 0; t--) {
+        const int s0 = t * NT, n = min(NT, len - s0);
+        const int j = s0 + tid;
+        const bool live = tid < n;
+        const int ty = live ? sm.lut[row[j]] : 0;
+        const int na = live ? tp.natoms[ty] : 0;
+        // the residue's first atom inside the tile: block exclusive scan of atom counts
+        int inc = na;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += v;
+        }
+        if (lane == 31) s_wcnt[w] = inc;
+        __syncthreads();
+        int wbase = 0, tcnt = 0;
+#pragma unroll
+        for (int q = 0; q < NW; q++) {
+            const int c = s_wcnt[q];
+            wbase += q < w ? c : 0;
+            tcnt += c;
+        }
+        const int aoff = wbase + inc - na;
+        const int abase = abase_next - tcnt;
+        const int nstage = 3 * (tcnt + (t + 1 < ntiles ? 1 : 0));  // + the next tile's first N
+        for (int i = tid; i < nstage; i += NT) {
+            sm.x[i] = xin[(size_t)3 * abase + i];
+            sm.g[i] = gin[(size_t)3 * abase + i];
+        }
+        __syncthreads();
+        const float o[3] = {sm.x[0], sm.x[1], sm.x[2]};
+        {  // carry to this tile's origin: S_o = S_oc + (oc - o) x G
+            const float d[3] = {oc[0] - o[0], oc[1] - o[1], oc[2] - o[2]};
+            float dx[3];
+            cross3(d, Gc, dx);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                Sc[c] += dx[c];
+                oc[c] = o[c];
+            }
+        }
+        // residue totals, then the sums over later residues
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int q = 0; q < na; q++) add_atom(sm.x + 3 * (aoff + q), sm.g + 3 * (aoff + q), o, v, v + 3);
+        float later[6], ttot[6];
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            float wt;
+            later[i] = suffix_excl(v[i], lane, wt);
+            if (lane == 0) s_wsum[w][i] = wt;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            float after = 0.f, all = 0.f;
+#pragma unroll
+            for (int q = 0; q < NW; q++) {
+                const float s = s_wsum[q][i];
+                after += q > w ? s : 0.f;
+                all += s;
+            }
+            later[i] += after + (i < 3 ? Gc[i] : Sc[i - 3]);
+            ttot[i] = all;
+        }
+        if (live) {
+            float G[3] = {later[0], later[1], later[2]}, S[3] = {later[3], later[4], later[5]};
+            const float *X = sm.x + 3 * aoff, *Gg = sm.g + 3 * aoff;
+            float xN[3], xA[3], xC[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                xN[c] = X[c] - o[c];
+                xA[c] = X[3 + c] - o[c];
+                xC[c] = X[3 * (na - 2) + c] - o[c];
+            }
+            float gr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (j + 1 < len) {  // omega_j: the next residue's N joint
+                const float xn[3] = {X[3 * na] - o[0], X[3 * na + 1] - o[1], X[3 * na + 2] - o[2]};
+                gr[2] = joint_grad(xn, xC, inv_dom, G, S);
+            }
+            add_atom(X + 3 * (na - 1), Gg + 3 * (na - 1), o, G, S);  // O
+            gr[1] = joint_grad(xC, xA, inv_dpsi, G, S);
+            add_atom(X + 3 * (na - 2), Gg + 3 * (na - 2), o, G, S);  // C
+            // side chain, groups last to first; chi subtrees hold side-chain atoms only
+            float Gs[3] = {0.f, 0.f, 0.f}, Ss[3] = {0.f, 0.f, 0.f};
+            const int nj = tp.njoints[ty];
+            if (nj == 0) {
+                for (int q = 2; q < na - 2; q++) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);  // Pro ring (none for Gly)
+            }
+            for (int k = nj - 1; k >= 0; k--) {
+                const int f0 = 2 + tp.jfirst[ty][k], f1 = f0 + tp.jna[ty][k];
+                for (int q = f1 - 1; q >= f0; q--) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);
+                const int chi = tp.jchi[ty][k];
+                if (chi >= 0) {
+                    const float *pk = X + 3 * f0;
+                    const float *pp = k == 0 ? X + 3 : X + 3 * (2 + tp.jfirst[ty][k - 1]);
+                    const float ok_[3] = {pk[0] - o[0], pk[1] - o[1], pk[2] - o[2]};
+                    const float op_[3] = {pp[0] - o[0], pp[1] - o[1], pp[2] - o[2]};
+                    gr[3 + chi] = joint_grad(ok_, op_, 1.f / tp.jd[ty][k], Gs, Ss);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                G[c] += Gs[c];
+                S[c] += Ss[c];
+            }
+            gr[0] = joint_grad(xA, xN, inv_dphi, G, S);
+#pragma unroll
+            for (int k = 0; k < 8; k++) gout[(size_t)k * a.L + j] = gr[k];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            Gc[c] += ttot[c];
+            Sc[c] += ttot[3 + c];
+        }
+        abase_next = abase;
+        __syncthreads();  // staging, s_wcnt and s_wsum are rewritten by the next tile
+    }
+    // zeros past the chain (and everywhere when the chain was rejected)
+    const int from = ok ? len : 0;
+    for (int k = 0; k < 8; k++)
+        for (int i = from + tid; i < a.L; i += NT) gout[(size_t)k * a.L + i] = 0.f;
+}
+
 // ------------------------------------------------------------------ host side
 template <typename T, int R, int NT>
 static int launch_a2c_fwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t st) {
@@ -665,6 +886,20 @@ int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const uns
         case 512: return launch_a2c_bwd<float, 1, 512>(a, B, renorm, st);
     }
     return launch_a2c_bwd<float, 1, 256>(a, B, renorm, st);
+}
+
+int a2c_backward_coords(float *grad_angles, const float *grad_coords, const float *coords, const unsigned char *seq,
+                        int seq_stride, void *ws, int B, int L, int maxA, cudaStream_t st) {
+    if (B == 0) return TPL_OK;
+    A2cArgs<float> a{seq, seq_stride, nullptr, const_cast<float *>(coords), nullptr, nullptr, grad_angles, grad_coords,
+                     (WsHeader *)ws, L, maxA};
+    constexpr int NT = 256;
+    const size_t smem = sizeof(A2cCoordsSmem<NT>);
+    auto k = a2c_bwd_coords_kernel<NT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return TPL_ERR_LAUNCH;
+    k<<<B, NT, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
 int num_atoms_host(const char *seq) {

@@ -294,6 +294,19 @@ int tpl_a2c_backward_f32(float *grad_angles, const float *grad_coords, const uin
                           workspace_bytes, batch, max_len, max_atoms, opt, stream);
 }
 
+int tpl_a2c_backward_coords_f32(float *grad_angles, const float *grad_coords, const float *coords,
+                                const uint8_t *sequences, int seq_stride, void *workspace, size_t workspace_bytes,
+                                int batch, int max_len, int max_atoms, void *stream) {
+    if (batch < 0 || max_len < 0 || max_atoms < 0 || seq_stride <= 0) return TPL_ERR_ARGUMENT;
+    if (batch == 0) return TPL_OK;
+    if (!sequences || (!grad_angles && max_len > 0) || ((!grad_coords || !coords) && max_atoms > 0))
+        return TPL_ERR_ARGUMENT;
+    int s = check_ws(workspace, workspace_bytes, sizeof(WsHeader));
+    if (s) return s;
+    return a2c_backward_coords(grad_angles, grad_coords, coords, sequences, seq_stride, workspace, batch, max_len,
+                               max_atoms, (cudaStream_t)stream);
+}
+
 int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const uint8_t *sequences, int seq_stride,
                          const double *angles, void *workspace, size_t workspace_bytes, int batch, int max_len,
                          int max_atoms, const tpl_options *opt, void *stream) {

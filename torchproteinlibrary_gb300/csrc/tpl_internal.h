@@ -81,6 +81,8 @@ bool options_ok(const tpl_options &o);
 int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *angles, void *coords,
                 uint32_t *res_names, uint32_t *atom_names, void *ws, int B, int L, int maxA,
                 const tpl_options &opt, cudaStream_t st);
+int a2c_backward_coords(float *grad_angles, const float *grad_coords, const float *coords, const unsigned char *seq,
+                        int seq_stride, void *ws, int B, int L, int maxA, cudaStream_t st);
 int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const unsigned char *seq, int seq_stride,
                  const void *angles, void *ws, int B, int L, int maxA, const tpl_options &opt, cudaStream_t st);
 int num_atoms_host(const char *seq);
