@@ -6,12 +6,12 @@
 // Python loop of .item() calls (TorchProteinLibrary/RMSD/Coords2RMSD/Coords2RMSD.py:40-62).
 //
 // Here one CTA per chain does everything in one launch: optional centring, the
-// correlation R_ab = sum x_a y_b and R2 = sum |x|^2 + |y|^2 (per-thread partial sums
-// in the coordinate type, about N / 256 atoms each, reduced across the block in
-// FP64: GB300's FP64 rate is a small fraction of its FP32 rate),
-// the 4x4 matrix T (same layout as the reference), its largest eigenpair by the
-// characteristic-polynomial method on one warp in FP64 (key_eigen_warp), U from the
-// unit quaternion, UT = U^T and
+// correlation R_ab = sum x_a y_b and R2 = sum |x|^2 + |y|^2 (sums in the coordinate
+// type per thread and per warp, in FP64 across the warps: GB300's FP64 rate is a
+// small fraction of its FP32 rate), the 4x4 matrix T (same layout as the
+// reference), its largest eigenpair by the characteristic-polynomial method on one
+// warp (key_eigen_warp: lane-parallel coefficients, FP32 Newton polished in FP64),
+// U from the unit quaternion, UT = U^T and
 // rmsd = sqrt((R2 - 2 |lambda_max| + 1e-10) / N).  The backward is one launch:
 // dL/dx_i = g (x_i - UT y_i) / (rmsd N) on the centred coordinates.
 #include <cmath>
@@ -38,15 +38,31 @@ struct RmsdArgs {
     WsHeader *hdr;
 };
 
-__device__ __forceinline__ double block_sum(double v, double *s_red) {
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+constexpr int kRmsdWarps = kRmsdThreads / 32;
+
+// Block sums of NV per-thread values: in the coordinate type within each warp, then
+// in FP64 across the warps on one lane per value, so that the FP64 work is NV x
+// warps additions rather than a shuffle tree per value on every thread (GB300's
+// FP64 rate is a small fraction of its FP32 rate).  Every thread returns with the
+// sums in s_out.
+template <typename T, int NV>
+__device__ __forceinline__ void block_sums(T (&v)[NV], double *s_red, double *s_out) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) s_red[w * NV + k] = (double)v[k];
     __syncthreads();
-    if (lane == 0) s_red[w] = v;
+    if (threadIdx.x < NV) {
+        double r = 0.0;
+#pragma unroll
+        for (int i = 0; i < kRmsdWarps; i++) r += s_red[i * NV + threadIdx.x];
+        s_out[threadIdx.x] = r;
+    }
     __syncthreads();
-    double r = 0.0;
-    for (int i = 0; i < kRmsdThreads / 32; i++) r += s_red[i];
-    return r;
 }
 
 __device__ __forceinline__ double det3(double a, double b, double c, double d, double e, double f, double g, double h,
@@ -54,38 +70,71 @@ __device__ __forceinline__ double det3(double a, double b, double c, double d, d
     return a * (e * k - f * h) - b * (d * k - f * g) + c * (d * h - e * g);
 }
 
-// Largest eigenpair of the 4x4 key matrix K (symmetric and traceless) by its
-// characteristic polynomial, as in Theobald's quaternion-characteristic-polynomial
-// method (Acta Cryst. A61, 478, 2005): det(K - l I) = l^4 + c2 l^2 + c1 l + c0 with,
-// by Newton's identities for a traceless matrix, c2 = -tr(K^2)/2, c1 = -tr(K^3)/3,
-// c0 = det K.  Newton's method from e0 >= l_max (e0 = (sum |x|^2 + |y|^2) / 2)
-// descends monotonically to the largest root.  The eigenvector is the largest row
-// of the cofactor matrix of K - l_max I (rank one for a simple root), one cofactor
-// per lane.  Executed by a full warp; every lane returns lam and the unit q (q = 1, 0,
-// 0, 0 when every cofactor vanishes).
-__device__ void key_eigen_warp(const double (&K)[4][4], double e0, double &lam, double (&q)[4]) {
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Largest eigenpair of the 4x4 key matrix K (symmetric and traceless, row-major in
+// shared memory) by its characteristic polynomial, as in Theobald's
+// quaternion-characteristic-polynomial method (Acta Cryst. A61, 478, 2005):
+// det(K - l I) = l^4 + c2 l^2 + c1 l + c0 with, by Newton's identities for a
+// traceless matrix, c2 = -tr(K^2)/2, c1 = -tr(K^3)/3, c0 = det K.
+//   * tr(K^2), tr(K^3) and det K are spread over the lanes: entry (i, j) of K^2 on
+//     lane 4 i + j, the cofactor expansion of det K along row 0 on lanes 16-19.
+//   * Newton's method from e0 >= l_max (e0 = (sum |x|^2 + |y|^2) / 2) descends
+//     monotonically to the largest root.  It runs in FP32 on s = l / e0, whose
+//     coefficients are of order one, and is then polished by three FP64 Newton
+//     steps whose quotient uses an FP32 reciprocal (each step gains about seven
+//     digits), so that only a handful of FP64 operations remain.
+//   * The eigenvector is the largest row of the cofactor matrix of K - l_max I
+//     (rank one for a simple root), one cofactor per lane.
+// Executed by a full warp; every lane returns lam and the unit q (q = 1, 0, 0, 0
+// when every cofactor vanishes).
+__device__ void key_eigen_warp(const double *sK, double e0, double &lam, double (&q)[4]) {
     const int lane = threadIdx.x & 31;
-    double t2 = 0.0, t3 = 0.0;
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) {
-            double k2 = 0.0;  // (K^2)_ij
-            for (int m = 0; m < 4; m++) k2 = fma(K[i][m], K[m][j], k2);
-            t2 = fma(K[i][j], K[i][j], t2);
-            t3 = fma(k2, K[j][i], t3);
+    double t2 = 0.0, t3 = 0.0, c0 = 0.0;
+    if (lane < 16) {
+        const int i = lane >> 2, j = lane & 3;
+        double k2 = 0.0;  // (K^2)_ij
+#pragma unroll
+        for (int m = 0; m < 4; m++) k2 = fma(sK[4 * i + m], sK[4 * m + j], k2);
+        const double kij = sK[4 * i + j];
+        t2 = kij * kij;
+        t3 = k2 * sK[4 * j + i];
+    } else if (lane < 20) {
+        const int j = lane - 16;
+        const int ca = j == 0 ? 1 : 0, cb = j <= 1 ? 2 : 1, cc = j <= 2 ? 3 : 2;
+        c0 = sK[j] * det3(sK[4 + ca], sK[4 + cb], sK[4 + cc], sK[8 + ca], sK[8 + cb], sK[8 + cc], sK[12 + ca],
+                          sK[12 + cb], sK[12 + cc]);
+        if (j & 1) c0 = -c0;
+    }
+    t2 = warp_sum_d(t2);
+    t3 = warp_sum_d(t3);
+    c0 = warp_sum_d(c0);
+    const double c2 = -0.5 * t2, c1 = t3 * (-1.0 / 3.0);
+    double l = 0.0;
+    if (e0 > 0.0) {
+        const double ie = 1.0 / e0, ie2 = ie * ie;
+        const float a2 = (float)(c2 * ie2), a1 = (float)(c1 * ie2 * ie), a0 = (float)(c0 * ie2 * ie2);
+        float s = 1.f;
+        for (int it = 0; it < 64; it++) {
+            const float P = fmaf(fmaf(fmaf(s, s, a2), s, a1), s, a0);
+            const float dP = fmaf(fmaf(4.f * s, s, 2.f * a2), s, a1);
+            if (!(dP != 0.f)) break;
+            const float d = P / dP;
+            s -= d;
+            if (fabsf(d) <= 1e-6f) break;
         }
-    const double c0 = K[0][0] * det3(K[1][1], K[1][2], K[1][3], K[2][1], K[2][2], K[2][3], K[3][1], K[3][2], K[3][3]) -
-                      K[0][1] * det3(K[1][0], K[1][2], K[1][3], K[2][0], K[2][2], K[2][3], K[3][0], K[3][2], K[3][3]) +
-                      K[0][2] * det3(K[1][0], K[1][1], K[1][3], K[2][0], K[2][1], K[2][3], K[3][0], K[3][1], K[3][3]) -
-                      K[0][3] * det3(K[1][0], K[1][1], K[1][2], K[2][0], K[2][1], K[2][2], K[3][0], K[3][1], K[3][2]);
-    const double c2 = -0.5 * t2, c1 = -t3 / 3.0;
-    double l = e0;
-    for (int it = 0; it < 64; it++) {
-        const double P = fma(fma(fma(l, l, c2), l, c1), l, c0);
-        const double dP = fma(fma(4.0 * l, l, 2.0 * c2), l, c1);
-        if (!(dP != 0.0)) break;
-        const double d = P / dP;
-        l -= d;
-        if (fabs(d) <= 1e-13 * fabs(l)) break;
+        l = (double)s * e0;
+        for (int it = 0; it < 3; it++) {
+            const double P = fma(fma(fma(l, l, c2), l, c1), l, c0);
+            const double dP = fma(fma(4.0 * l, l, 2.0 * c2), l, c1);
+            const float dPf = (float)dP;
+            if (!(dPf != 0.f) || !isfinite(dPf)) break;
+            l -= P * (double)(1.f / dPf);
+        }
     }
     lam = l;
     // cofactor (i, j) of M = K - l I on lane 4 i + j
@@ -94,10 +143,12 @@ __device__ void key_eigen_warp(const double (&K)[4][4], double e0, double &lam, 
         const int i = lane >> 2, j = lane & 3;
         double m[9];
         int t = 0;
+#pragma unroll
         for (int r = 0; r < 4; r++)
             if (r != i)
+#pragma unroll
                 for (int c = 0; c < 4; c++)
-                    if (c != j) m[t++] = K[r][c] - (r == c ? l : 0.0);
+                    if (c != j) m[t++] = sK[4 * r + c] - (r == c ? l : 0.0);
         cof = det3(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
         if ((i + j) & 1) cof = -cof;
     }
@@ -124,8 +175,9 @@ __device__ void key_eigen_warp(const double (&K)[4][4], double e0, double &lam, 
 
 template <typename T>
 __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
-    __shared__ double s_red[kRmsdThreads / 32];
-    __shared__ double s_c[6];
+    __shared__ double s_red[kRmsdWarps * 10];
+    __shared__ double s_out[10];
+    __shared__ double s_K[16];
     const int b = blockIdx.x, tid = threadIdx.x;
     int n = a.num_atoms[b];
     if (n < 0 || n > a.atoms_stride) {
@@ -142,12 +194,8 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
                 sx[k] += x[3 * i + k];
                 sx[3 + k] += y[3 * i + k];
             }
-        for (int k = 0; k < 6; k++) {
-            const double s = block_sum((double)sx[k], s_red);
-            if (tid == 0) s_c[k] = n > 0 ? s / n : 0.0;
-        }
-        __syncthreads();
-        for (int k = 0; k < 6; k++) c[k] = s_c[k];
+        block_sums<T, 6>(sx, s_red, s_out);
+        for (int k = 0; k < 6; k++) c[k] = n > 0 ? s_out[k] / n : 0.0;
     }
     T ct[6];
     for (int k = 0; k < 6; k++) ct[k] = (T)c[k];
@@ -162,18 +210,22 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
             for (int q = 0; q < 3; q++) acc[3 * p + q] = fma(xi[p], yi[q], acc[3 * p + q]);
         acc[9] += xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2] + yi[0] * yi[0] + yi[1] * yi[1] + yi[2] * yi[2];
     }
-    double tot[10];
-    for (int k = 0; k < 10; k++) tot[k] = block_sum((double)acc[k], s_red);
+    block_sums<T, 10>(acc, s_red, s_out);
     if (tid < 32) {
-        const double *R = tot;
-        // quaternion matrix, same layout as the reference (coords2rmsd_interface.cpp:146-149)
-        const double F[4][4] = {
-            {R[0] + R[4] + R[8], R[5] - R[7], R[6] - R[2], R[1] - R[3]},
-            {R[5] - R[7], R[0] - R[4] - R[8], R[1] + R[3], R[2] + R[6]},
-            {R[6] - R[2], R[1] + R[3], -R[0] + R[4] - R[8], R[5] + R[7]},
-            {R[1] - R[3], R[2] + R[6], R[5] + R[7], -R[0] - R[4] + R[8]}};
+        const double *R = s_out;
+        double tot[10];
+        for (int k = 0; k < 10; k++) tot[k] = s_out[k];
+        if (tid == 0) {
+            // quaternion matrix, same layout as the reference (coords2rmsd_interface.cpp:146-149)
+            const double F[16] = {R[0] + R[4] + R[8], R[5] - R[7], R[6] - R[2], R[1] - R[3],
+                                  R[5] - R[7], R[0] - R[4] - R[8], R[1] + R[3], R[2] + R[6],
+                                  R[6] - R[2], R[1] + R[3], -R[0] + R[4] - R[8], R[5] + R[7],
+                                  R[1] - R[3], R[2] + R[6], R[5] + R[7], -R[0] - R[4] + R[8]};
+            for (int k = 0; k < 16; k++) s_K[k] = F[k];
+        }
+        __syncwarp();
         double lam, q[4];
-        key_eigen_warp(F, 0.5 * tot[9], lam, q);
+        key_eigen_warp(s_K, 0.5 * tot[9], lam, q);
         if (tid != 0) return;
         // rotation from the unit quaternion (coords2rmsd_interface.cpp:36-46)
         double U[9];
