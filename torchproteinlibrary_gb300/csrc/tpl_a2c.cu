@@ -24,6 +24,7 @@
 
 #include "tpl_common.cuh"
 #include "tpl_internal.h"
+#include "tpl_sincos.cuh"
 #include "tpl_topology.cuh"
 
 namespace tpl {
@@ -58,6 +59,10 @@ __device__ __forceinline__ void a2c_error(WsHeader *h, int code) {
 
 template <typename T>
 __device__ __forceinline__ void sc(T a, T *s, T *c) { sincos_t(a, s, c); }
+// float angles: the register polynomial of the Angles2Backbone kernels (about one
+// ulp, no special-function unit; sincosf beyond |a| = 1e4)
+template <>
+__device__ __forceinline__ void sc<float>(float a, float *s, float *c) { sincos_poly(a, s, c); }
 
 template <typename T>
 __device__ __forceinline__ void renorm_if(Frame<T> &f, bool on) {
