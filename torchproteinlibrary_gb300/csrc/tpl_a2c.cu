@@ -79,6 +79,15 @@ struct A2cSmem {
     signed char lut[256];
 };
 
+// The forward also stages the tile's residue and atom names, so that they leave
+// with the coordinates' coalesced store instead of per-residue scattered writes.
+template <typename T, int TILE>
+struct A2cSmemFwd {
+    A2cSmem<T, TILE> f;
+    uint32_t res_name[TILE * kMaxResAtoms];
+    uint32_t atom_name[TILE * kMaxResAtoms];
+};
+
 template <typename T, int TILE>
 struct A2cSmemBwd {
     A2cSmem<T, TILE> f;
@@ -248,7 +257,8 @@ template <typename T, int R, int NT>
 __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
     constexpr int TILE = R * NT, NW = NT / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    A2cSmem<T, TILE> &sm = *reinterpret_cast<A2cSmem<T, TILE> *>(smem_raw);
+    A2cSmemFwd<T, TILE> &smf = *reinterpret_cast<A2cSmemFwd<T, TILE> *>(smem_raw);
+    A2cSmem<T, TILE> &sm = smf.f;
     __shared__ Frame<T> s_wtot[NW], s_wpre[NW];
     __shared__ int s_wcnt[NW], s_wcpre[NW];
     __shared__ Frame<T> s_carry;
@@ -308,7 +318,6 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
             if (j < n) {
                 const int ty = sm.type[j];
                 T *dst = sm.xyz + 3 * aoff;
-                const int gatom = abase + aoff;
                 residue_atoms<T>(sm.topo, ty, P, ts.cs[r], ts.sn[r], &sm.ang[3][j], TILE,
                                  [&](int slot, const T *x) {
                                      dst[3 * slot] = x[0];
@@ -317,9 +326,9 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
                                  });
                 if (rn && an) {
                     const int na = sm.topo.natoms[ty];
-                    for (int k = 0; k < na && gatom + k < a.maxA; k++) {
-                        rn[gatom + k] = sm.topo.res_name[ty];
-                        an[gatom + k] = sm.topo.atom_name[ty][k];
+                    for (int k = 0; k < na; k++) {
+                        smf.res_name[aoff + k] = sm.topo.res_name[ty];
+                        smf.atom_name[aoff + k] = sm.topo.atom_name[ty][k];
                     }
                 }
                 aoff += sm.topo.natoms[ty];
@@ -330,6 +339,11 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
         const int nstore = max(0, min(tcnt, a.maxA - abase));
         const T org[3] = {s_org[0], s_org[1], s_org[2]};
         store_tile_atoms<T, NT>(out + (size_t)3 * abase, sm.xyz, org, nstore);
+        if (rn && an)
+            for (int i = tid; i < nstore; i += NT) {
+                rn[abase + i] = smf.res_name[i];
+                an[abase + i] = smf.atom_name[i];
+            }
         __syncthreads();
         if (tid == 0) s_abase = abase + tcnt;
         __syncthreads();
@@ -830,7 +844,7 @@ __global__ void __launch_bounds__(NT) a2c_bwd_coords_kernel(A2cArgs<float> a) {
 template <typename T, int R, int NT>
 static int launch_a2c_fwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t st) {
     constexpr int TILE = R * NT;
-    const size_t smem = sizeof(A2cSmem<T, TILE>);
+    const size_t smem = sizeof(A2cSmemFwd<T, TILE>);
     auto k = a2c_fwd_kernel<T, R, NT>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return TPL_ERR_LAUNCH;
