@@ -12,7 +12,8 @@
 // reference), its largest eigenpair by the characteristic-polynomial method on one
 // warp (key_eigen_warp: lane-parallel coefficients, FP32 Newton polished in FP64),
 // U from the unit quaternion, UT = U^T and
-// rmsd = sqrt((R2 - 2 |lambda_max| + 1e-10) / N).  The backward is one launch:
+// rmsd = sqrt((R2 - 2 |lambda_max| + 1e-10) / N).  The backward is one launch with
+// one thread per atom (chains on x, blocks of atoms on y):
 // dL/dx_i = g (x_i - UT y_i) / (rmsd N) on the centred coordinates.
 #include <cmath>
 
@@ -178,6 +179,8 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
     __shared__ double s_red[kRmsdWarps * 10];
     __shared__ double s_out[10];
     __shared__ double s_K[16];
+    __shared__ double s_c[6];  // centroids (src, dst)
+    __shared__ T s_ct[6];
     const int b = blockIdx.x, tid = threadIdx.x;
     int n = a.num_atoms[b];
     if (n < 0 || n > a.atoms_stride) {
@@ -186,20 +189,29 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
     }
     const T *x = a.src + (size_t)b * 3 * a.atoms_stride;
     const T *y = a.dst + (size_t)b * 3 * a.atoms_stride;
-    double c[6] = {0, 0, 0, 0, 0, 0};
     if (a.center) {
         T sx[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 4
         for (int i = tid; i < n; i += kRmsdThreads)
             for (int k = 0; k < 3; k++) {
                 sx[k] += x[3 * i + k];
                 sx[3 + k] += y[3 * i + k];
             }
         block_sums<T, 6>(sx, s_red, s_out);
-        for (int k = 0; k < 6; k++) c[k] = n > 0 ? s_out[k] / n : 0.0;
+        if (tid < 6) {  // one division per value, on six lanes (FP64 is slow on GB300)
+            const double v = n > 0 ? s_out[tid] / n : 0.0;
+            s_c[tid] = v;
+            s_ct[tid] = (T)v;
+        }
+    } else if (tid < 6) {
+        s_c[tid] = 0.0;
+        s_ct[tid] = T(0);
     }
+    __syncthreads();
     T ct[6];
-    for (int k = 0; k < 6; k++) ct[k] = (T)c[k];
+    for (int k = 0; k < 6; k++) ct[k] = s_ct[k];
     T acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // R (row-major) and R2
+#pragma unroll 4
     for (int i = tid; i < n; i += kRmsdThreads) {
         T xi[3], yi[3];
         for (int k = 0; k < 3; k++) {
@@ -244,7 +256,7 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
         const double msd = n > 0 ? (tot[9] - 2.0 * fabs(lam) + 1e-10) / (double)n : 0.0;
         a.rmsd[b] = (T)sqrt(msd > 0.0 ? msd : 0.0);
         if (a.centroids)
-            for (int k = 0; k < 6; k++) a.centroids[6 * b + k] = c[k];
+            for (int k = 0; k < 6; k++) a.centroids[6 * b + k] = s_c[k];
     }
 }
 
@@ -255,15 +267,23 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_bwd_kernel(RmsdArgs<T> a) {
     const T *x = a.src + (size_t)b * 3 * a.atoms_stride;
     const T *y = a.dst + (size_t)b * 3 * a.atoms_stride;
     T *gx = a.grad_src + (size_t)b * 3 * a.atoms_stride;
-    T c[6] = {0, 0, 0, 0, 0, 0};
-    if (a.center && a.centroids)
-        for (int k = 0; k < 6; k++) c[k] = (T)a.centroids[6 * b + k];
-    const T *ut = a.ut + (size_t)9 * b;
-    T U[9];
-    for (int k = 0; k < 9; k++) U[k] = ut[k];
-    const T r = a.rmsd[b];
-    const T scale = (n > 0 && r > T(0)) ? a.grad_rmsd[b] / (r * (T)n) : T(0);
-    for (int i = tid; i < a.atoms_stride; i += kRmsdThreads) {
+    // per-chain constants once per block: converting the FP64 centroids on every
+    // thread would keep GB300's slow FP64 pipe busy
+    __shared__ T s_c[6], s_U[9], s_scale;
+    if (tid < 6) s_c[tid] = (a.center && a.centroids) ? (T)a.centroids[6 * b + tid] : T(0);
+    if (tid < 9) s_U[tid] = a.ut[(size_t)9 * b + tid];
+    if (tid == 0) {
+        const T r = a.rmsd[b];
+        s_scale = (n > 0 && r > T(0)) ? a.grad_rmsd[b] / (r * (T)n) : T(0);
+    }
+    __syncthreads();
+    T c[6], U[9];
+    for (int k = 0; k < 6; k++) c[k] = s_c[k];
+    for (int k = 0; k < 9; k++) U[k] = s_U[k];
+    const T scale = s_scale;
+    // one atom per thread: chains on x, blocks of atoms on y
+    const int i = blockIdx.y * kRmsdThreads + tid;
+    if (i < a.atoms_stride) {
         if (i < n) {
             T xi[3], yi[3];
             for (int k = 0; k < 3; k++) {
@@ -294,7 +314,9 @@ static int rmsd_bwd_launch(const T *grad_rmsd, const T *src, const T *dst, const
     if (B == 0) return TPL_OK;
     RmsdArgs<T> a{src, dst, num_atoms, stride, center, const_cast<T *>(rmsd), const_cast<T *>(ut),
                   const_cast<double *>(centroids), grad_rmsd, grad_src, nullptr};
-    rmsd_bwd_kernel<T><<<B, kRmsdThreads, 0, st>>>(a);
+    const int ablocks = (max(stride, 1) + kRmsdThreads - 1) / kRmsdThreads;
+    if (ablocks > 65535) return TPL_ERR_UNSUPPORTED;
+    rmsd_bwd_kernel<T><<<dim3((unsigned)B, (unsigned)ablocks), kRmsdThreads, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
