@@ -680,8 +680,8 @@ def time_training_step(dev, steps=10, seed=1004):
 def time_coords_transform(dev, steps=20):
     """CoordsTransform's elementwise passes on a batch larger than L2: 2048 rows of
     4000 atoms (98 MB of float32 coordinates per tensor).  Translate and rotate read
-    and write 12 B per atom each; reported as achieved bandwidth against the
-    measured HBM peak."""
+    and write 12 B per atom each, centre reads 12 B per atom; reported as achieved
+    bandwidth against the measured HBM peak."""
     import torch
     from torchproteinlibrary_gb300 import load_extension
 
@@ -695,8 +695,10 @@ def time_coords_transform(dev, steps=20):
     R = torch.linalg.qr(torch.randn(B, 3, 3, device=dev, generator=g))[0].contiguous()
     peak, _ = peaks()
     res = {"workload": f"{B} rows x {S} atoms, float32", "bytes_per_call": 2 * x.numel() * 4}
-    for name, fn in (("translate", lambda: fm.CoordsTranslateGPU_forward(x, out, T, na)),
-                     ("rotate", lambda: fm.CoordsRotateGPU_forward(x, out, R, na))):
+    cen = torch.empty(B, 3, device=dev)
+    for name, fn, nbytes in (("translate", lambda: fm.CoordsTranslateGPU_forward(x, out, T, na), 2 * x.numel() * 4),
+                             ("rotate", lambda: fm.CoordsRotateGPU_forward(x, out, R, na), 2 * x.numel() * 4),
+                             ("center", lambda: fm.Coords2CenterGPU_forward(x, cen, na), x.numel() * 4)):
         for _ in range(3):
             fn()
         torch.cuda.synchronize(dev)
@@ -707,7 +709,7 @@ def time_coords_transform(dev, steps=20):
         e1.record()
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / steps
-        gbs = res["bytes_per_call"] / (ms / 1e3) / 1e9
+        gbs = nbytes / (ms / 1e3) / 1e9
         res[name] = {"ms": ms, "GB/s": gbs, "frac_of_hbm_peak": gbs / peak}
     return res
 

@@ -169,20 +169,36 @@ __device__ __forceinline__ R block_reduce(R v, Op op, R *s_warp) {
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) center_kernel(const T *in, T *center, const int *num_atoms,
                                                                 int stride) {
-    __shared__ double s_warp[kReduceThreads / 32];
-    const int b = blockIdx.x;
+    constexpr int NW = kReduceThreads / 32;
+    __shared__ double s_warp[NW][3];
+    const int b = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int n = min(num_atoms[b], stride);  // a count past the row is clamped to it
     const T *x = in + (size_t)b * 3 * stride;
-    double s[3] = {0.0, 0.0, 0.0};
+    // offsets from the chain's first atom, summed in the coordinate type per thread and
+    // per warp and in FP64 across the warps: the offsets stay of the chain's own extent
+    // wherever the chain sits, and GB300's FP64 rate is a small fraction of its FP32 rate
+    const T p0 = n > 0 ? x[0] : T(0), p1 = n > 0 ? x[1] : T(0), p2 = n > 0 ? x[2] : T(0);
+    T s[3] = {T(0), T(0), T(0)};
     for (int i = threadIdx.x; i < n; i += kReduceThreads) {
-        s[0] += (double)x[3 * i];
-        s[1] += (double)x[3 * i + 1];
-        s[2] += (double)x[3 * i + 2];
+        s[0] += x[3 * i] - p0;
+        s[1] += x[3 * i + 1] - p1;
+        s[2] += x[3 * i + 2] - p2;
     }
-    auto add = [](double p, double q) { return p + q; };
-    for (int c = 0; c < 3; c++) {
-        const double t = block_reduce<double>(s[c], add, s_warp);
-        if (threadIdx.x == 0) center[3 * b + c] = n > 0 ? (T)(t / n) : T(0);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; c++) s[c] += __shfl_xor_sync(0xffffffffu, s[c], off);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 3; c++) s_warp[w][c] = (double)s[c];
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int c = threadIdx.x;
+        double t = 0.0;
+#pragma unroll
+        for (int q = 0; q < NW; q++) t += s_warp[q][c];
+        const double pc = c == 0 ? (double)p0 : (c == 1 ? (double)p1 : (double)p2);
+        center[3 * b + c] = n > 0 ? (T)(pc + t / n) : T(0);
     }
 }
 
