@@ -281,7 +281,7 @@ def run_ours(args):
     value = residues / (ms / 1e3)
 
     if args.no_extras:
-        check = plain = e2e = a2c = train = transform = None
+        check = plain = e2e = a2c = train = transform = ragged = None
     else:
         # correctness of this very run against the FP64 plain form on a slice
         check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
@@ -291,6 +291,7 @@ def run_ours(args):
         e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
         a2c = time_a2c(dev)
         train = time_training_step(dev)
+        ragged = time_ragged(dev)
         transform = time_coords_transform(dev)
 
     peak, peak_kind = peaks()
@@ -334,6 +335,7 @@ def run_ours(args):
         "plain_fp64": plain,
         "angles2coords": a2c,
         "training_step": train,
+        "ragged_batch": ragged,
         "coords_transform": transform,
         "accuracy_vs_fp64": check,
     }
@@ -677,6 +679,79 @@ def time_training_step(dev, steps=10, seed=1004):
     return res
 
 
+def time_ragged(dev, steps=20, seed=1003):
+    """The ragged Angles2Backbone batch: 1024 chains of U{20..700} residues (padded to
+    700), phi, psi ~ U[-pi, pi), omega ~ N(pi, 0.05), FP32; one forward and the float32
+    layer's backward (from the coordinates) with the automatic scheme, captured once
+    in a CUDA graph and replayed; residues/s counts real residues.  Accuracy against
+    the plain FP64 form on the same float32 angles."""
+    import torch
+    from torchproteinlibrary_gb300 import load_extension
+
+    rm = load_extension("_ReducedModel")
+    g = np.random.default_rng(seed)
+    B, L = 1024, 700
+    lens = g.integers(20, L + 1, B).astype(np.int32)
+    ang = g.uniform(-np.pi, np.pi, (B, 3, L)).astype(np.float32)
+    ang[:, 2] = g.normal(np.pi, 0.05, (B, L)).astype(np.float32)
+    for b, n in enumerate(lens):
+        ang[b, :, n:] = 0.0
+    up = g.standard_normal((B, 9 * L)).astype(np.float32)
+    a = torch.from_numpy(ang).to(dev)
+    ln = torch.from_numpy(lens).to(dev)
+    u = torch.from_numpy(up).to(dev)
+    saved_f, saved_b = rm.get_options(), rm.get_backward_options()
+    rm.set_options(0, 0, 0, 0, 0)
+    rm.set_backward_options(0, 0, 0)
+    try:
+        ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+        c = torch.empty(B, 9 * L, device=dev)
+        gi = torch.empty(B, 3, L, device=dev)
+
+        def step():
+            rm.Angles2BackboneGPU_forward(a, c, ln, ws)
+            rm.Angles2BackboneGPU_backward_coords(gi, u, c, ln, ws)
+
+        st = torch.cuda.Stream(device=dev)
+        st.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(st):
+            for _ in range(3):
+                step()
+        torch.cuda.current_stream(dev).wait_stream(st)
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step()
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        assert rm.workspace_status(ws) == 0
+        # accuracy on the 64 longest chains
+        idx = torch.from_numpy(np.argsort(lens)[-64:].copy()).to(dev)
+        a64 = a[idx].double().contiguous()
+        l64 = ln[idx].contiguous()
+        c64 = torch.empty(64, 9 * L, dtype=torch.float64, device=dev)
+        g64 = torch.empty(64, 3, L, dtype=torch.float64, device=dev)
+        ws64 = torch.zeros(rm.workspace_bytes(64, L), dtype=torch.uint8, device=dev)
+        rm.Angles2BackboneGPU_forward(a64, c64, l64, ws64)
+        rm.Angles2BackboneGPU_backward(g64, u[idx].double().contiguous(), a64, l64, ws64, torch.empty(0, device=dev))
+        d = (c[idx].double() - c64).view(64, -1, 3).norm(dim=-1)
+        ge = (gi[idx].double() - g64).abs().max() / g64.abs().max()
+    finally:
+        rm.set_options(*saved_f)
+        rm.set_backward_options(*saved_b)
+    return {"workload": "1024 chains x U{20..700} residues (padded to 700), FP32, omega ~ N(pi, 0.05)",
+            "residues": int(lens.sum()), "graph_ms_per_step": ms,
+            "residues_per_s": float(lens.sum()) / (ms / 1e3), "coord_max_A": float(d.max()),
+            "grad_max_rel": float(ge), "launch": "forward + backward from the coordinates, one CUDA graph"}
+
+
 def time_coords_transform(dev, steps=20):
     """CoordsTransform's elementwise passes on a batch larger than L2: 2048 rows of
     4000 atoms (98 MB of float32 coordinates per tensor).  Translate and rotate read
@@ -742,14 +817,15 @@ def main():
     ap.add_argument("--bwd-cta", type=int, default=0, help="coordinate backward: 0 = automatic, 32 = one warp per chain, 4 = one CTA of four warps per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
-    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform"],
+    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform", "ragged_batch"],
                     help="run one secondary leg alone and print its result (profiling); no metric line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "ours" else args.warmup
     if args.leg:
         import torch
         dev = torch.device("cuda", 0)
-        fn = {"a2c": time_a2c, "training_step": time_training_step, "coords_transform": time_coords_transform}[args.leg]
+        fn = {"a2c": time_a2c, "training_step": time_training_step, "coords_transform": time_coords_transform,
+              "ragged_batch": time_ragged}[args.leg]
         print(json.dumps({"leg": args.leg, "result": fn(dev)}, default=float))
         return
     if args.impl == "reference":
