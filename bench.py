@@ -324,6 +324,15 @@ def run_ours(args):
                      "bytes_moved_per_launch": B * L * (BWD_COORDS_MOVED_PER_RES if dom == "backward"
                                                         else FWD_BYTES_PER_RES)},
         "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
+        "roofline_by_kernel": {
+            "forward": {"achieved": B * L * FWD_BYTES_PER_RES / (fwd_ms / 1e3) / 1e9,
+                        "frac": B * L * FWD_BYTES_PER_RES / (fwd_ms / 1e3) / 1e9 / peak,
+                        "algorithmic_bytes_per_residue": FWD_BYTES_PER_RES},
+            "backward": {"achieved": B * L * BWD_BYTES_PER_RES / (bwd_ms / 1e3) / 1e9,
+                         "frac": B * L * BWD_BYTES_PER_RES / (bwd_ms / 1e3) / 1e9 / peak,
+                         "algorithmic_bytes_per_residue": BWD_BYTES_PER_RES,
+                         "moved_frac": B * L * BWD_COORDS_MOVED_PER_RES / (bwd_ms / 1e3) / 1e9 / peak},
+            "unit": "GB/s of algorithmic bytes", "peak": peak},
         "tuned": tuned,
         "tile_sweep": [{k: (round(v, 5) if isinstance(v, float) else v) for k, v in r.items()}
                        for r in getattr(autotune.tune, "last_sweep", [])],
@@ -411,6 +420,10 @@ def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
             torch.empty(up_h.shape, device=dev)) for _ in range(2)]
     ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("in", "run", "out")}
     started = [False, False]
+    # each buffer set keeps its step's results alive until the layer stream has waited
+    # for their copies out; they are then released before the next allocation on that
+    # same stream, so the allocator reuses them in stream order (no record_stream)
+    keep = [None, None]
 
     def step(i, compute=True):
         k = i % 2
@@ -427,6 +440,7 @@ def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
             s_run.wait_event(ev["in"][k])
             if started[k]:
                 s_run.wait_event(ev["out"][k])  # step i-2's results have left buffer set k
+            keep[k] = None
             if compute:
                 a.grad = None
                 a.requires_grad_()
@@ -436,10 +450,9 @@ def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
             else:
                 res = (a, u)  # same byte counts as the results: 9L and 3L floats per chain
             ev["run"][k].record(s_run)
+            keep[k] = res
         with torch.cuda.stream(s_out), torch.no_grad():
             s_out.wait_event(ev["run"][k])
-            for t in res:
-                t.record_stream(s_out)
             if compute:
                 out_c.copy_(res[0], non_blocking=True)
                 out_g.copy_(res[1], non_blocking=True)
@@ -817,15 +830,20 @@ def main():
     ap.add_argument("--bwd-cta", type=int, default=0, help="coordinate backward: 0 = automatic, 32 = one warp per chain, 4 = one CTA of four warps per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
-    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform", "ragged_batch"],
+    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform", "ragged_batch", "e2e"],
                     help="run one secondary leg alone and print its result (profiling); no metric line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "ours" else args.warmup
     if args.leg:
         import torch
         dev = torch.device("cuda", 0)
+        def e2e_leg(dev):
+            from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+            ang_np, len_np, up_np = make_inputs()
+            return time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10)
+
         fn = {"a2c": time_a2c, "training_step": time_training_step, "coords_transform": time_coords_transform,
-              "ragged_batch": time_ragged}[args.leg]
+              "ragged_batch": time_ragged, "e2e": e2e_leg}[args.leg]
         print(json.dumps({"leg": args.leg, "result": fn(dev)}, default=float))
         return
     if args.impl == "reference":
