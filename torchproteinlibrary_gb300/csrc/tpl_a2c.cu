@@ -247,10 +247,10 @@ __device__ __forceinline__ void residue_atoms(const Topology<T> &tp, int ty, Fra
     apply_joint(P, tp.bb_cb[2], tp.bb_sb[2], tp.bb_d[2], cs[2], sn[2]);
 }
 
+// Copy n staged values (world coordinates, xyz interleaved) to dst, coalesced.
 template <typename T, int NT>
-__device__ __forceinline__ void store_tile_atoms(T *dst, const T *src, const T org[3], int n_atoms) {
-    // dst: global coords of the tile's first atom (3 * n_atoms values, xyz interleaved)
-    for (int i = threadIdx.x; i < 3 * n_atoms; i += NT) dst[i] = src[i] + org[i % 3];
+__device__ __forceinline__ void store_tile_atoms(T *dst, const T *src, int n) {
+    for (int i = threadIdx.x; i < n; i += NT) dst[i] = src[i];
 }
 
 template <typename T, int R, int NT>
@@ -312,6 +312,9 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
         renorm_if(P, renorm);
         int aoff = s_wcpre[w] + ts.cnt_exc;  // first atom of this thread inside the tile
         const int abase = s_abase;
+        // positions are built relative to the tile origin and moved to it as they are
+        // staged (the same FP32 addition as at store time, without a per-value modulo)
+        const T org[3] = {s_org[0], s_org[1], s_org[2]};
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const int j = tid * R + r;
@@ -320,9 +323,9 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
                 T *dst = sm.xyz + 3 * aoff;
                 residue_atoms<T>(sm.topo, ty, P, ts.cs[r], ts.sn[r], &sm.ang[3][j], TILE,
                                  [&](int slot, const T *x) {
-                                     dst[3 * slot] = x[0];
-                                     dst[3 * slot + 1] = x[1];
-                                     dst[3 * slot + 2] = x[2];
+                                     dst[3 * slot] = x[0] + org[0];
+                                     dst[3 * slot + 1] = x[1] + org[1];
+                                     dst[3 * slot + 2] = x[2] + org[2];
                                  });
                 if (rn && an) {
                     const int na = sm.topo.natoms[ty];
@@ -337,8 +340,7 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
         __syncthreads();
         const int tcnt = s_tcnt;
         const int nstore = max(0, min(tcnt, a.maxA - abase));
-        const T org[3] = {s_org[0], s_org[1], s_org[2]};
-        store_tile_atoms<T, NT>(out + (size_t)3 * abase, sm.xyz, org, nstore);
+        store_tile_atoms<T, NT>(out + (size_t)3 * abase, sm.xyz, 3 * nstore);
         if (rn && an)
             for (int i = tid; i < nstore; i += NT) {
                 rn[abase + i] = smf.res_name[i];
@@ -814,7 +816,10 @@ __global__ void __launch_bounds__(NT) a2c_bwd_coords_kernel(A2cArgs<float> a) {
                     const float *pp = k == 0 ? X + 3 : X + 3 * (2 + tp.jfirst[ty][k - 1]);
                     const float ok_[3] = {pk[0] - o[0], pk[1] - o[1], pk[2] - o[2]};
                     const float op_[3] = {pp[0] - o[0], pp[1] - o[1], pp[2] - o[2]};
-                    gr[3 + chi] = joint_grad(ok_, op_, 1.f / tp.jd[ty][k], Gs, Ss);
+                    const float gk = joint_grad(ok_, op_, 1.f / tp.jd[ty][k], Gs, Ss);
+#pragma unroll
+                    for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
+                        if (chi == q) gr[3 + q] = gk;
                 }
             }
 #pragma unroll
