@@ -281,7 +281,7 @@ def run_ours(args):
     value = residues / (ms / 1e3)
 
     if args.no_extras:
-        check = plain = e2e = a2c = train = transform = ragged = None
+        check = plain = e2e = a2c = train = transform = ragged = typed = None
     else:
         # correctness of this very run against the FP64 plain form on a slice
         check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
@@ -293,6 +293,7 @@ def run_ours(args):
         train = time_training_step(dev)
         ragged = time_ragged(dev)
         transform = time_coords_transform(dev)
+        typed = time_typed_coords(dev)
 
     peak, peak_kind = peaks()
     fwd_ms, bwd_ms = statistics.mean(t_f), statistics.mean(t_b)
@@ -345,6 +346,7 @@ def run_ours(args):
         "angles2coords": a2c,
         "training_step": train,
         "ragged_batch": ragged,
+        "typed_coords": typed,
         "coords_transform": transform,
         "accuracy_vs_fp64": check,
     }
@@ -765,6 +767,60 @@ def time_ragged(dev, steps=20, seed=1003):
             "grad_max_rel": float(ge), "launch": "forward + backward from the coordinates, one CUDA graph"}
 
 
+def time_typed_coords(dev, steps=20, seed=1006):
+    """Coords2TypedCoords (the 11-type regrouping) on Angles2Coords output: 4096 chains
+    of U{50..500} random residues (about 190 MB of coordinates and names, more than
+    L2).  Forward reads coordinates and names and writes typed coordinates and atom
+    indexes (36 B per atom); backward reads the typed gradient and the indexes and
+    writes the flat gradient (28 B per atom)."""
+    import torch
+    from torchproteinlibrary_gb300 import load_extension
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+
+    fm = load_extension("_FullAtomModel")
+    g = np.random.default_rng(seed)
+    B = 4096
+    lens = g.integers(50, 501, B)
+    aa = np.array(list("ACDEFGHIKLMNPQRSTVWY"))
+    seqs = ["".join(g.choice(aa, n)) for n in lens]
+    L = int(lens.max())
+    ang = torch.from_numpy(g.uniform(-np.pi, np.pi, (B, 8, L)).astype(np.float32)).to(dev)
+    seq = convertStringList(seqs).to(dev)
+    na_list = [fm.getSeqNumAtoms(x) for x in seqs]
+    maxA = max(na_list)
+    x = torch.empty(B, 3 * maxA, device=dev)
+    rn = torch.empty(B, maxA, 4, dtype=torch.uint8, device=dev)
+    an = torch.empty(B, maxA, 4, dtype=torch.uint8, device=dev)
+    fm.Angles2Coords_forward(seq, ang, x, rn, an)
+    na = torch.tensor(na_list, dtype=torch.int32, device=dev)
+    out = torch.empty_like(x)
+    n_of_type = torch.empty(B, 11, dtype=torch.int32, device=dev)
+    offsets = torch.empty(B, 11, dtype=torch.int32, device=dev)
+    idx = torch.empty(B, maxA, dtype=torch.int32, device=dev)
+    gt = torch.randn_like(x)
+    gf = torch.empty_like(x)
+    fwd = lambda: fm.Coords2TypedCoords_forward(x, rn, an, na, out, n_of_type, offsets, idx)
+    bwd = lambda: fm.Coords2TypedCoords_backward(gt, gf, n_of_type, offsets, idx)
+    atoms = float(sum(na_list))
+    peak, _ = peaks()
+    res = {"workload": f"{B} chains x U{{50..500}} residues ({int(atoms)} atoms), float32, Angles2Coords output"}
+    for name, fn, per_atom in (("forward", fwd, 36), ("backward", bwd, 28)):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        gbs = atoms * per_atom / (ms / 1e3) / 1e9
+        res[name] = {"ms": ms, "GB/s": gbs, "frac_of_hbm_peak": gbs / peak, "bytes_per_atom": per_atom}
+    assert fm.workspace_status(0) == 0
+    return res
+
+
 def time_coords_transform(dev, steps=20):
     """CoordsTransform's elementwise passes on a batch larger than L2: 2048 rows of
     4000 atoms (98 MB of float32 coordinates per tensor).  Translate and rotate read
@@ -830,7 +886,7 @@ def main():
     ap.add_argument("--bwd-cta", type=int, default=0, help="coordinate backward: 0 = automatic, 32 = one warp per chain, 4 = one CTA of four warps per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
-    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform", "ragged_batch", "e2e"],
+    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform", "ragged_batch", "e2e", "typed_coords"],
                     help="run one secondary leg alone and print its result (profiling); no metric line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "ours" else args.warmup
@@ -843,7 +899,7 @@ def main():
             return time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10)
 
         fn = {"a2c": time_a2c, "training_step": time_training_step, "coords_transform": time_coords_transform,
-              "ragged_batch": time_ragged, "e2e": e2e_leg}[args.leg]
+              "ragged_batch": time_ragged, "e2e": e2e_leg, "typed_coords": time_typed_coords}[args.leg]
         print(json.dumps({"leg": args.leg, "result": fn(dev)}, default=float))
         return
     if args.impl == "reference":

@@ -32,7 +32,7 @@ struct TypedName {
 
 // Residue-specific types (0-based, as get11AtomType returns them); the
 // residue-agnostic backbone names are handled first in atom_type().
-__device__ const TypedName kTypedNames[] = {
+constexpr TypedName kTypedNames[] = {
     // 0: sulfur / selenium
     {nm("CYS"), nm("SG"), 0}, {nm("MET"), nm("SD"), 0}, {nm("MSE"), nm("SE"), 0},
     // 1: amide N
@@ -76,6 +76,32 @@ __device__ const TypedName kTypedNames[] = {
 };
 constexpr int kTypedNameCount = sizeof(kTypedNames) / sizeof(TypedName);
 
+// The table as an open-addressing hash of 256 slots (filled at compile time; load
+// factor about 0.4), so that a lookup takes one or two probes instead of a walk
+// over every entry.  A residue word of 0 marks an empty slot.
+constexpr int kHashSlots = 256;
+struct TypedHash {
+    uint32_t res[kHashSlots], atom[kHashSlots];
+    int type[kHashSlots];
+};
+constexpr uint32_t typed_hash(uint32_t res, uint32_t atom) {
+    return ((res * 0x9E3779B1u) ^ (atom * 0x85EBCA77u)) >> 24;  // top 8 bits
+}
+constexpr TypedHash build_typed_hash() {
+    TypedHash h{};
+    for (int i = 0; i < kHashSlots; i++) h.type[i] = -1;
+    for (int i = 0; i < kTypedNameCount; i++) {
+        uint32_t k = typed_hash(kTypedNames[i].res, kTypedNames[i].atom);
+        while (h.res[k] != 0) k = (k + 1) & (kHashSlots - 1);
+        h.res[k] = kTypedNames[i].res;
+        h.atom[k] = kTypedNames[i].atom;
+        h.type[k] = kTypedNames[i].type;
+    }
+    return h;
+}
+static_assert(kTypedNameCount < kHashSlots / 2, "hash load factor");
+__device__ const TypedHash g_typed_hash = build_typed_hash();
+
 // Drop the space bytes of a name word (the reference erases whitespace from the
 // atom name before comparing) and stop at the first NUL.
 __device__ __forceinline__ uint32_t squeeze(uint32_t w) {
@@ -99,8 +125,13 @@ __device__ __forceinline__ int atom_type(uint32_t res, uint32_t atom) {
     if (atom == nm("N")) return 1;
     if (atom == nm("C")) return 8;
     if (atom == nm("CA")) return 10;
-    for (int i = 0; i < kTypedNameCount; i++)
-        if (kTypedNames[i].res == res && kTypedNames[i].atom == atom) return kTypedNames[i].type;
+    uint32_t k = typed_hash(res, atom);
+    for (int probe = 0; probe < kHashSlots; probe++) {
+        const uint32_t r = g_typed_hash.res[k];
+        if (r == 0u) return -1;
+        if (r == res && g_typed_hash.atom[k] == atom) return g_typed_hash.type[k];
+        k = (k + 1) & (kHashSlots - 1);
+    }
     return -1;
 }
 
