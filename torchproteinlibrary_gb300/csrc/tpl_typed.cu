@@ -234,6 +234,37 @@ __global__ void __launch_bounds__(kTypedThreads) typed_bwd_kernel(const T *grad_
     }
 }
 
+// The same with every flat row written once, in order: the slot of each atom is
+// first inverted into shared memory (in_stride ints), then grad_flat[j] is gathered
+// from grad_typed[slot(j)] with coalesced stores (zero for atoms without a slot).
+template <typename T>
+__global__ void __launch_bounds__(kTypedThreads) typed_bwd_gather_kernel(const T *grad_typed, T *grad_flat,
+                                                                         const int *n_of_type, const int *atom_index,
+                                                                         int in_stride, int out_stride) {
+    extern __shared__ int s_slot[];
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const size_t row = (size_t)b * in_stride, orow = (size_t)b * out_stride;
+    int ntyped = 0;
+    for (int k = 0; k < kTypes; k++) ntyped += n_of_type[(size_t)b * kTypes + k];
+    ntyped = max(0, min(ntyped, out_stride));
+    for (int j = tid; j < in_stride; j += kTypedThreads) s_slot[j] = -1;
+    __syncthreads();
+    for (int s = tid; s < ntyped; s += kTypedThreads) {
+        const int j = atom_index[orow + s];
+        if (j >= 0 && j < in_stride) s_slot[j] = s;
+    }
+    __syncthreads();
+    const T *src = grad_typed + 3 * orow;
+    T *dst = grad_flat + 3 * row;
+    for (int e = tid; e < 3 * in_stride; e += kTypedThreads) {
+        const int j = e / 3, c = e - 3 * j;
+        const int s = s_slot[j];
+        dst[e] = s >= 0 ? src[3 * s + c] : T(0);
+    }
+}
+
+constexpr int kGatherMaxAtoms = 16384;  // 64 KB of slots per CTA
+
 }  // namespace
 
 int typed_forward(bool f64, const void *coords, const uint32_t *res_names, const uint32_t *atom_names,
@@ -257,6 +288,23 @@ int typed_forward(bool f64, const void *coords, const uint32_t *res_names, const
 int typed_backward(bool f64, const void *grad_typed, void *grad_flat, const int *n_of_type, const int *atom_index,
                    int B, int in_stride, int out_stride, cudaStream_t st) {
     if (B == 0) return TPL_OK;
+    if (in_stride <= kGatherMaxAtoms) {
+        const int smem = in_stride * (int)sizeof(int);
+        if (f64) {
+            auto k = typed_bwd_gather_kernel<double>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+                return TPL_ERR_LAUNCH;
+            k<<<B, kTypedThreads, smem, st>>>(static_cast<const double *>(grad_typed), static_cast<double *>(grad_flat),
+                                              n_of_type, atom_index, in_stride, out_stride);
+        } else {
+            auto k = typed_bwd_gather_kernel<float>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+                return TPL_ERR_LAUNCH;
+            k<<<B, kTypedThreads, smem, st>>>(static_cast<const float *>(grad_typed), static_cast<float *>(grad_flat),
+                                              n_of_type, atom_index, in_stride, out_stride);
+        }
+        return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+    }
     if (f64)
         typed_bwd_kernel<double><<<B, kTypedThreads, 0, st>>>(static_cast<const double *>(grad_typed),
                                                              static_cast<double *>(grad_flat), n_of_type, atom_index,
