@@ -137,13 +137,16 @@ __device__ __forceinline__ int atom_type(uint32_t res, uint32_t atom) {
 
 // Input rows hold in_stride atoms (coordinates and names); typed rows and atom
 // indexes hold out_stride slots.
-template <typename T>
+// CACHE: each atom's type from the counting pass is kept in shared memory (in_stride
+// bytes of dynamic shared memory) for the scatter pass, instead of looked up again.
+template <typename T, bool CACHE>
 __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coords, const uint32_t *res_names,
                                                                   const uint32_t *atom_names, const int *num_atoms,
                                                                   int in_stride, int out_stride, T *out,
                                                                   int *n_of_type, int *offsets, int *atom_index,
                                                                   WsHeader *hdr) {
     constexpr int NW = kTypedThreads / 32;
+    extern __shared__ signed char s_ty[];
     __shared__ int s_count[kTypes], s_off[kTypes], s_base[kTypes];
     __shared__ int s_wc[kTypes][NW];
     const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -156,6 +159,7 @@ __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coord
     __syncthreads();
     for (int j = tid; j < n; j += kTypedThreads) {
         const int t = atom_type(res_names[row + j], atom_names[row + j]);
+        if (CACHE) s_ty[j] = (signed char)t;
         if (t >= 0) atomicAdd(&s_count[t], 1);
         else atomicCAS(&hdr->status, 0u, (unsigned)TPL_ERR_ATOM_TYPE);
     }
@@ -176,7 +180,7 @@ __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coord
     // stable scatter, one tile of kTypedThreads atoms at a time
     for (int j0 = 0; j0 < n; j0 += kTypedThreads) {
         const int j = j0 + tid;
-        const int t = j < n ? atom_type(res_names[row + j], atom_names[row + j]) : -1;
+        const int t = j < n ? (CACHE ? (int)s_ty[j] : atom_type(res_names[row + j], atom_names[row + j])) : -1;
         int rank = 0;
         const unsigned below = (1u << lane) - 1u;
 #pragma unroll
@@ -264,6 +268,7 @@ __global__ void __launch_bounds__(kTypedThreads) typed_bwd_gather_kernel(const T
 }
 
 constexpr int kGatherMaxAtoms = 16384;  // 64 KB of slots per CTA
+constexpr int kTypeCacheMax = 32768;    // forward type cache: one byte per input atom
 
 }  // namespace
 
@@ -272,17 +277,23 @@ int typed_forward(bool f64, const void *coords, const uint32_t *res_names, const
                   int *atom_index, void *ws, cudaStream_t st) {
     if (B == 0) return TPL_OK;
     WsHeader *hdr = reinterpret_cast<WsHeader *>(ws);
-    if (f64)
-        typed_fwd_kernel<double><<<B, kTypedThreads, 0, st>>>(static_cast<const double *>(coords), res_names,
-                                                             atom_names, num_atoms, in_stride, out_stride,
-                                                             static_cast<double *>(out), n_of_type, offsets,
-                                                             atom_index, hdr);
-    else
-        typed_fwd_kernel<float><<<B, kTypedThreads, 0, st>>>(static_cast<const float *>(coords), res_names, atom_names,
-                                                            num_atoms, in_stride, out_stride,
-                                                            static_cast<float *>(out), n_of_type, offsets, atom_index,
-                                                            hdr);
-    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+    const bool cache = in_stride <= kTypeCacheMax;
+    const size_t smem = cache ? (size_t)in_stride : 0;
+    auto launch = [&](auto kernel, auto *out_t, auto *coords_t) -> int {
+        if (smem > 48 * 1024 && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return TPL_ERR_LAUNCH;
+        kernel<<<B, kTypedThreads, smem, st>>>(coords_t, res_names, atom_names, num_atoms, in_stride, out_stride,
+                                               out_t, n_of_type, offsets, atom_index, hdr);
+        return cudaGetLastError() == cudaSuccess ? (int)TPL_OK : (int)TPL_ERR_LAUNCH;
+    };
+    if (f64) {
+        auto *o = static_cast<double *>(out);
+        auto *c = static_cast<const double *>(coords);
+        return cache ? launch(typed_fwd_kernel<double, true>, o, c) : launch(typed_fwd_kernel<double, false>, o, c);
+    }
+    auto *o = static_cast<float *>(out);
+    auto *c = static_cast<const float *>(coords);
+    return cache ? launch(typed_fwd_kernel<float, true>, o, c) : launch(typed_fwd_kernel<float, false>, o, c);
 }
 
 int typed_backward(bool f64, const void *grad_typed, void *grad_flat, const int *n_of_type, const int *atom_index,
