@@ -281,14 +281,19 @@ def run_ours(args):
     value = residues / (ms / 1e3)
 
     if args.no_extras:
-        check = plain = e2e = a2c = train = transform = ragged = typed = None
+        check = plain = e2e = e2e_io = a2c = train = transform = ragged = typed = None
     else:
         # correctness of this very run against the FP64 plain form on a slice
         check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
         # plain FP64 form on the same workload (the drop-in denominator)
         plain = time_plain_fp64(rm, ang, lengths, up, dev, steps=max(1, min(3, args.steps)))
         # e2e: public autograd layer, host (pinned) inputs in, results back to the host
-        e2e = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
+        e2e = time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
+        e2e["eager"] = {k: v for k, v in time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev,
+                                                         steps=max(4, min(10, args.steps)), graph=False).items()
+                        if k in ("value", "ms_per_step", "host_issue_ms_per_step")}
+        # the layer's full I/O through the host link as well: upstream gradient in, coordinates out
+        e2e_io = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
         a2c = time_a2c(dev)
         train = time_training_step(dev)
         ragged = time_ragged(dev)
@@ -342,6 +347,7 @@ def run_ours(args):
         "fp64_carry_sweep": sweep_rows,
         "gpu_launches": 2 * args.steps,
         "e2e": e2e,
+        "e2e_layer_io": e2e_io,
         "plain_fp64": plain,
         "angles2coords": a2c,
         "training_step": train,
@@ -490,6 +496,126 @@ def time_e2e(layer, ang_np, len_np, up_np, dev, steps):
             "copies_only_note": "the same pinned copies on the same streams with no kernels: the host-link floor",
             "api": "torchproteinlibrary_gb300.ReducedModel.Angles2Backbone (autograd), pinned host buffers, "
                    "three-stream pipeline (copies in, layer, copies out) over two buffer sets"}
+
+
+def time_e2e_train(layer, ang_np, len_np, up_np, dev, steps, graph=True):
+    """End to end as a training step through the public autograd layer: every step
+    copies its angles and lengths from pinned host memory, runs the forward, the loss
+    L = sum(coords * w) with a fixed weight tensor w resident on the device (the
+    synthetic upstream gradient of the device-timed step: dL/dcoords = w), the
+    backward, and copies the loss and dL/dangles back to pinned host memory (what a
+    host-side optimiser needs).  Copies in, the step and copies out form a
+    three-stream pipeline over two buffer sets.  graph=True: the step (layer
+    forward, loss, backward) is captured once per buffer set with torch.cuda.graph and
+    replayed, as a training loop would; graph=False issues it eagerly, which on this
+    host's cores takes longer than the step's copies."""
+    import torch
+
+    B = ang_np.shape[0]
+    ang_h = torch.from_numpy(ang_np).pin_memory()
+    len_h = torch.from_numpy(len_np).pin_memory()
+    w = torch.from_numpy(up_np).to(dev)
+    wf = w.view(-1)
+    outs = [(torch.empty(ang_np.shape).pin_memory(), torch.empty(1).pin_memory()) for _ in range(2)]
+    s_in, s_run, s_out = (torch.cuda.Stream(device=dev) for _ in range(3))
+    ins = [(torch.empty(ang_h.shape, device=dev), torch.empty(len_h.shape, dtype=len_h.dtype, device=dev))
+           for _ in range(2)]
+    for a, ln in ins:
+        a.copy_(ang_h)
+        ln.copy_(len_h)
+        a.requires_grad_()
+    ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("in", "run", "out")}
+    started = [False, False]
+    keep = [None, None]
+
+    def compute(a, ln):
+        c = layer(a, ln)
+        c.backward(w)  # dL/dcoords of L = sum(coords * w)
+        return a.grad, torch.dot(c.detach().view(-1), wf).view(1)
+
+    graphs, static = [None, None], [None, None]
+    if graph:
+        for k in range(2):
+            a, ln = ins[k]
+            side = torch.cuda.Stream(device=dev)
+            side.wait_stream(torch.cuda.current_stream(dev))
+            with torch.cuda.stream(side):
+                for _ in range(3):
+                    a.grad = None
+                    compute(a, ln)
+            torch.cuda.current_stream(dev).wait_stream(side)
+            torch.cuda.synchronize(dev)
+            a.grad = None
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                static[k] = compute(a, ln)
+            graphs[k] = g
+
+    def step(i):
+        k = i % 2
+        a, ln = ins[k]
+        out_g, out_l = outs[k]
+        with torch.cuda.stream(s_in), torch.no_grad():
+            if started[k]:
+                s_in.wait_event(ev["run"][k])
+            a.copy_(ang_h, non_blocking=True)
+            ln.copy_(len_h, non_blocking=True)
+            ev["in"][k].record(s_in)
+        with torch.cuda.stream(s_run):
+            s_run.wait_event(ev["in"][k])
+            if started[k]:
+                s_run.wait_event(ev["out"][k])
+            if graph:
+                graphs[k].replay()
+                res = static[k]
+            else:
+                keep[k] = None
+                a.grad = None
+                res = compute(a, ln)
+                keep[k] = res
+            ev["run"][k].record(s_run)
+        with torch.cuda.stream(s_out), torch.no_grad():
+            s_out.wait_event(ev["run"][k])
+            out_g.copy_(res[0], non_blocking=True)
+            out_l.copy_(res[1], non_blocking=True)
+            ev["out"][k].record(s_out)
+        started[k] = True
+
+    for i in range(2):
+        step(i)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        step(i)
+    t_issue = time.perf_counter()
+    torch.cuda.synchronize(dev)
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    ms_issue = (t_issue - t0) * 1e3 / steps  # host time to issue one step (the GPU may still be running)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        step(i)
+        torch.cuda.synchronize(dev)
+    ms_serial = (time.perf_counter() - t0) * 1e3 / steps
+    # the last step's copied-out gradient and loss against the eager layer on the same inputs
+    k_last = (steps - 1) % 2
+    a_ref = torch.from_numpy(ang_np).to(dev).requires_grad_()
+    c_ref = layer(a_ref, torch.from_numpy(len_np).to(dev))
+    c_ref.backward(w)
+    loss_ref = float(torch.dot(c_ref.detach().view(-1), wf))
+    torch.cuda.synchronize(dev)
+    g_ref = a_ref.grad.cpu()
+    check = {"grad_max_rel": float((outs[k_last][0] - g_ref).abs().max() / g_ref.abs().max()),
+             "loss_rel": abs(float(outs[k_last][1][0]) - loss_ref) / max(1.0, abs(loss_ref))}
+    h2d = ang_np.nbytes + len_np.nbytes
+    d2h = outs[0][0].numel() * 4 + 4
+    return {"value": B * L_RES / (ms / 1e3), "unit": "residues/s", "ms_per_step": ms,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "serial_ms_per_step": ms_serial,
+            "host_issue_ms_per_step": ms_issue, "graph": graph, "check_vs_eager_layer": check,
+            "api": "torchproteinlibrary_gb300.ReducedModel.Angles2Backbone (autograd) as a training step: angles and "
+                   "lengths in from pinned host memory, loss sum(coords * w) with w resident, loss and dL/dangles "
+                   "out to pinned host memory; three-stream pipeline over two buffer sets"
+                   + ("; forward, loss and backward captured once per buffer set in a CUDA graph" if graph else
+                      "; eager")}
 
 
 def time_a2c(dev, steps=10, seed=1004):
@@ -896,7 +1022,9 @@ def main():
         def e2e_leg(dev):
             from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
             ang_np, len_np, up_np = make_inputs()
-            return time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10)
+            return {"e2e": time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10),
+                    "e2e_eager": time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10, graph=False),
+                    "e2e_layer_io": time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10)}
 
         fn = {"a2c": time_a2c, "training_step": time_training_step, "coords_transform": time_coords_transform,
               "ragged_batch": time_ragged, "e2e": e2e_leg, "typed_coords": time_typed_coords}[args.leg]
