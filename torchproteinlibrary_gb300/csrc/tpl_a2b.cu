@@ -1401,7 +1401,7 @@ template <int R>
 static int launch_fwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
     auto k = a2b_fwd_f32_kernel<R, 128>;
     const int smem = 12 * R * 128 * (int)sizeof(float);
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), smem))
         return TPL_ERR_LAUNCH;
     int grid = persistent_grid(k, 128, a.total, max_ctas, smem);
     k<<<grid, 128, smem, st>>>(a);
@@ -1411,7 +1411,7 @@ template <int R, int NT>
 static int launch_bwd(A2bArgs &a, int max_ctas, cudaStream_t st) {
     auto k = a2b_bwd_f32_kernel<R, NT>;
     const int smem = 21 * R * NT * (int)sizeof(float);
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), smem))
         return TPL_ERR_LAUNCH;
     int grid = persistent_grid(k, NT, a.total, max_ctas, smem);
     k<<<grid, NT, smem, st>>>(a);

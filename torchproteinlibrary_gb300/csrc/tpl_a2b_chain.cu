@@ -1341,7 +1341,7 @@ bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 template <typename K>
 int launch_chain(K kernel, int smem, int B, const ChainArgs &a, cudaStream_t st) {
-    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(kernel), smem))
         return TPL_ERR_LAUNCH;
     const int grid = (B + kWarpsPerCta - 1) / kWarpsPerCta;
     kernel<<<grid, 32 * kWarpsPerCta, smem, st>>>(a);
@@ -1350,7 +1350,7 @@ int launch_chain(K kernel, int smem, int B, const ChainArgs &a, cudaStream_t st)
 
 template <typename K>
 int launch_ring(K kernel, int smem, int B, const ChainArgs &a, cudaStream_t st) {
-    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(kernel), smem))
         return TPL_ERR_LAUNCH;
     kernel<<<B, 32 * kRingWarps, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;

@@ -851,7 +851,7 @@ static int launch_a2c_fwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t s
     constexpr int TILE = R * NT;
     const size_t smem = sizeof(A2cSmemFwd<T, TILE>);
     auto k = a2c_fwd_kernel<T, R, NT>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), (int)smem))
         return TPL_ERR_LAUNCH;
     k<<<B, NT, smem, st>>>(a, renorm);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
@@ -867,7 +867,7 @@ static int launch_a2c_bwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t s
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if ((int)smem > optin) return TPL_ERR_UNSUPPORTED;
     auto k = a2c_bwd_kernel<T, R, NT>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), (int)smem))
         return TPL_ERR_LAUNCH;
     k<<<B, NT, smem, st>>>(a, renorm, max_tiles);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
@@ -920,7 +920,7 @@ int a2c_backward_coords(float *grad_angles, const float *grad_coords, const floa
     constexpr int NT = 256;
     const size_t smem = sizeof(A2cCoordsSmem<NT>);
     auto k = a2c_bwd_coords_kernel<NT>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), (int)smem))
         return TPL_ERR_LAUNCH;
     k<<<B, NT, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;

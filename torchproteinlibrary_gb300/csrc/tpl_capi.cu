@@ -2,6 +2,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "tpl_internal.h"
 
@@ -77,6 +79,23 @@ const BondConsts &bond_constants() {
         return c;
     }();
     return bc;
+}
+
+bool set_max_dynamic_smem(const void *func, int bytes) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> done;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = done.find({func, dev});
+        if (it != done.end() && it->second >= bytes) return true;
+    }
+    if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return false;
+    std::lock_guard<std::mutex> lk(mu);
+    int &v = done[{func, dev}];
+    v = v > bytes ? v : bytes;
+    return true;
 }
 
 tpl_options resolve(const tpl_options *opt) {

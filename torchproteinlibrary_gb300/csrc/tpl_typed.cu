@@ -280,7 +280,7 @@ int typed_forward(bool f64, const void *coords, const uint32_t *res_names, const
     const bool cache = in_stride <= kTypeCacheMax;
     const size_t smem = cache ? (size_t)in_stride : 0;
     auto launch = [&](auto kernel, auto *out_t, auto *coords_t) -> int {
-        if (smem > 48 * 1024 && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        if (smem > 48 * 1024 && !set_max_dynamic_smem(reinterpret_cast<const void *>(kernel), (int)smem))
             return TPL_ERR_LAUNCH;
         kernel<<<B, kTypedThreads, smem, st>>>(coords_t, res_names, atom_names, num_atoms, in_stride, out_stride,
                                                out_t, n_of_type, offsets, atom_index, hdr);
@@ -303,13 +303,13 @@ int typed_backward(bool f64, const void *grad_typed, void *grad_flat, const int 
         const int smem = in_stride * (int)sizeof(int);
         if (f64) {
             auto k = typed_bwd_gather_kernel<double>;
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+            if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), smem))
                 return TPL_ERR_LAUNCH;
             k<<<B, kTypedThreads, smem, st>>>(static_cast<const double *>(grad_typed), static_cast<double *>(grad_flat),
                                               n_of_type, atom_index, in_stride, out_stride);
         } else {
             auto k = typed_bwd_gather_kernel<float>;
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+            if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), smem))
                 return TPL_ERR_LAUNCH;
             k<<<B, kTypedThreads, smem, st>>>(static_cast<const float *>(grad_typed), static_cast<float *>(grad_flat),
                                               n_of_type, atom_index, in_stride, out_stride);
