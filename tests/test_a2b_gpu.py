@@ -501,3 +501,61 @@ def test_backward_from_coordinates_c_abi_and_layer(built):
     assert (gi - grads[1]).abs().max().item() <= GRAD_TOL_F32 * scale
     assert lib.tpl_a2b_backward_coords_f32(gi.data_ptr(), gt.data_ptr(), coords.data_ptr(), ln.data_ptr(),
                                            ws.data_ptr(), 16, B, L, None, capi.stream_ptr()) == -2
+
+
+def _bond_angle(p, q, r):
+    """Angle at q between q->p and q->r (float64 tensors [..., 3])."""
+    u, v = p - q, r - q
+    c = (u * v).sum(-1) / (u.norm(dim=-1) * v.norm(dim=-1))
+    return torch.acos(c.clamp(-1.0, 1.0))
+
+
+def test_full_size_geometry_and_fp64_slice(rm):
+    """The measured workload, 4096 chains x 1000 residues in FP32 with the default
+    (automatic) scheme and the float32 layer's backward: every bond length and
+    bond angle of every residue equals the joint geometry (size-independent
+    invariants; the reference values are read off the FP64 oracle), and 32 chains
+    match the FP64 form within the FP32 tolerances."""
+    dev = torch.device("cuda")
+    B, L = 4096, 1000
+    rng = np.random.default_rng(1005)
+    ang = rng.uniform(-np.pi, np.pi, (B, 3, L)).astype(np.float32)
+    ang[:, 2] = np.float32(np.pi)
+    lengths = np.full(B, L, np.int32)
+    up = rng.standard_normal((B, 9 * L)).astype(np.float32)
+    a = torch.tensor(ang, device=dev)
+    ln = torch.tensor(lengths, device=dev)
+    u = torch.tensor(up, device=dev)
+    ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+    coords = torch.empty(B, 9 * L, device=dev)
+    gi = torch.empty(B, 3, L, device=dev)
+    rm.Angles2BackboneGPU_forward(a, coords, ln, ws)
+    rm.Angles2BackboneGPU_backward_coords(gi, u, coords, ln, ws)
+    assert rm.workspace_status(ws) == 0
+    x = coords.double().view(B, L, 3, 3)
+    N, CA, C = x[:, :, 0], x[:, :, 1], x[:, :, 2]
+    # reference geometry from the FP64 oracle on a short chain
+    rc, _ = oracle.a2b_forward(ang[:1, :, :8].astype(np.float64), np.array([8], np.int32))
+    r = torch.tensor(rc, dtype=torch.float64).view(8, 3, 3)
+    rN, rCA, rC = r[:, 0], r[:, 1], r[:, 2]
+    bonds = [((CA - N).norm(dim=-1), (rCA - rN).norm(dim=-1)[0]),
+             ((C - CA).norm(dim=-1), (rC - rCA).norm(dim=-1)[0]),
+             ((N[:, 1:] - C[:, :-1]).norm(dim=-1), (rN[1] - rC[0]).norm())]
+    for got, want in bonds:
+        assert (got - float(want)).abs().max().item() <= 1e-4
+    angles = [(_bond_angle(N, CA, C), _bond_angle(rN, rCA, rC)[0]),
+              (_bond_angle(CA[:, :-1], C[:, :-1], N[:, 1:]), _bond_angle(rCA[0], rC[0], rN[1])),
+              (_bond_angle(C[:, :-1], N[:, 1:], CA[:, 1:]), _bond_angle(rC[0], rN[1], rCA[1]))]
+    for got, want in angles:
+        assert (got - float(want)).abs().max().item() <= 1e-4
+    # 32 chains against the FP64 form on the same float32 angles
+    n = 32
+    a64 = a[:n].double().contiguous()
+    c64 = torch.empty(n, 9 * L, dtype=torch.float64, device=dev)
+    g64 = torch.empty(n, 3, L, dtype=torch.float64, device=dev)
+    ws64 = torch.zeros(rm.workspace_bytes(n, L), dtype=torch.uint8, device=dev)
+    rm.Angles2BackboneGPU_forward(a64, c64, ln[:n].contiguous(), ws64)
+    rm.Angles2BackboneGPU_backward(g64, u[:n].double().contiguous(), a64, ln[:n].contiguous(), ws64,
+                                   torch.empty(0, device=dev))
+    check(coords[:n].double().cpu().numpy(), gi[:n].double().cpu().numpy(), c64.cpu().numpy(),
+          g64.cpu().numpy(), lengths[:n], L, COORD_TOL_F32, GRAD_TOL_F32)
