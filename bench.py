@@ -962,7 +962,13 @@ def time_coords_transform(dev, steps=20):
     out = torch.empty_like(x)
     na = torch.full((B,), S, dtype=torch.int32, device=dev)
     T = torch.randn(B, 3, device=dev, generator=g)
-    R = torch.linalg.qr(torch.randn(B, 3, 3, device=dev, generator=g))[0].contiguous()
+    q = torch.randn(B, 4, device=dev, generator=g)
+    q = q / q.norm(dim=1, keepdim=True)  # random unit quaternions -> rotation matrices
+    qa, qb, qc, qd = q.unbind(1)
+    R = torch.stack([qa * qa + qb * qb - qc * qc - qd * qd, 2 * (qb * qc - qa * qd), 2 * (qb * qd + qa * qc),
+                     2 * (qb * qc + qa * qd), qa * qa - qb * qb + qc * qc - qd * qd, 2 * (qc * qd - qa * qb),
+                     2 * (qb * qd - qa * qc), 2 * (qc * qd + qa * qb), qa * qa - qb * qb - qc * qc + qd * qd],
+                    dim=1).view(B, 3, 3).contiguous()
     peak, _ = peaks()
     res = {"workload": f"{B} rows x {S} atoms, float32", "bytes_per_call": 2 * x.numel() * 4}
     cen = torch.empty(B, 3, device=dev)
