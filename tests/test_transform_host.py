@@ -33,3 +33,30 @@ def test_random_rotation_and_translation_ranges(ct):
     d = torch.clamp(20.0 - (b - a) / 2.0, min=0.0) * 0.5
     assert T.shape == a.shape and bool((T.abs() <= d + 1e-6).all())
     assert float(T[1, 0]) == 0.0  # a box wider than the volume leaves no room
+
+
+def test_extension_pose_helpers_match_the_layer_module(ct):
+    """The reference-signature entry points of _FullAtomModel fill caller tensors
+    (coordsTransform_interface.cpp:201-259) with the same formulas."""
+    from torchproteinlibrary_gb300 import load_extension
+    ext = load_extension("_FullAtomModel")
+    u = torch.tensor(np.random.default_rng(4).uniform(0, 1, (8, 3)))
+    R = torch.zeros(8, 3, 3, dtype=torch.float64)
+    ext.getRotation(R, u)
+    assert torch.allclose(R, ct.getRotation(u), atol=1e-14)
+    R32 = torch.zeros(8, 3, 3, dtype=torch.float32)
+    ext.getRandomRotation(R32)
+    eye = torch.eye(3).expand(8, 3, 3)
+    assert torch.allclose(R32 @ R32.transpose(1, 2), eye, atol=1e-5)
+    torch.manual_seed(11)
+    ext.getRandomRotation(R)
+    torch.manual_seed(11)
+    assert torch.allclose(R, ct.getRotation(torch.rand(8, 3, dtype=torch.float64)), atol=1e-14)
+    a = torch.tensor([[0.0, -5.0, 2.0], [10.0, 10.0, 10.0]], dtype=torch.float64)
+    b = torch.tensor([[4.0, 5.0, 2.0], [90.0, 12.0, 10.0]], dtype=torch.float64)
+    T = torch.full((2, 3), 99.0, dtype=torch.float64)
+    ext.getRandomTranslation(T, a, b, 40.0)
+    d = torch.clamp(20.0 - (b - a) / 2.0, min=0.0) * 0.5
+    assert bool((T.abs() <= d + 1e-12).all()) and float(T[1, 0]) == 0.0
+    with pytest.raises(RuntimeError):
+        ext.getRotation(torch.zeros(2, 3), u)

@@ -12,8 +12,11 @@ Mirrors TorchProteinLibrary/FullAtomModel/PDB2Coords/PDB2Coords.py:
 Differences from the reference: ``pdb2sequence`` / ``get_sequence`` read the residue
 names with the native reader instead of Biopython (absent here): one letter per
 (chain, residue number) in file order, standard amino acids and MSE; anything else
-raises, as Biopython's three_to_one does.  ``PDB2CoordsOrdered`` is not provided:
-its C++ body is commented out in the reference and its Python wrapper cannot run.
+raises, as Biopython's three_to_one does.  ``PDB2CoordsOrdered`` exists by name only
+and raises when called: its C++ body is commented out in the reference
+(Layers/FullAtomModel/PDB2Coords/pdb2coords_interface.cpp:7, not bound in
+Layers/FullAtomModel/main.cpp) and its Python wrapper reads an attribute it never
+sets, so it has no behaviour to reproduce.
 """
 import os
 
@@ -24,7 +27,7 @@ from ... import load_extension
 
 _FullAtomModel = load_extension("_FullAtomModel")
 
-__all__ = ["PDB2CoordsUnordered", "writePDB", "pdb2sequence", "get_sequence", "convertStringList",
+__all__ = ["PDB2CoordsOrdered", "PDB2CoordsUnordered", "writePDB", "pdb2sequence", "get_sequence", "convertStringList",
            "string2tensor", "tensor2string"]
 
 _THREE_TO_ONE = {"ALA": "A", "ARG": "R", "ASN": "N", "ASP": "D", "CYS": "C", "GLN": "Q", "GLU": "E", "GLY": "G",
@@ -48,6 +51,15 @@ def string2tensor(string):
 
 def tensor2string(tensor):
     return bytes(tensor.cpu().numpy().tobytes()).split(b"\x00")[0].decode("utf-8", "strict")
+
+
+class PDB2CoordsOrdered:
+    """Name kept from the reference (PDB2Coords.py:54-70), whose native body is
+    commented out; calling it raises.  ``PDB2CoordsUnordered`` reads the same files."""
+
+    def __call__(self, filenames):
+        raise NotImplementedError("PDB2CoordsOrdered has no implementation in the reference either; "
+                                  "use PDB2CoordsUnordered")
 
 
 class PDB2CoordsUnordered:

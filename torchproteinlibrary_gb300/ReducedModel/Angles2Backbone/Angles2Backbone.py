@@ -80,6 +80,22 @@ class Angles2BackboneGPUFunction(Function):
         return gradInput, None
 
 
+class Angles2BackboneCPUFunction(Function):
+    """The reference's float64 CPU function, kept under its name so that code
+    importing it still loads.  This build has no CPU path: calling it raises, as
+    ``_ReducedModel.Angles2BackboneCPU_forward`` does.  Run float64 angles on a
+    CUDA device through ``Angles2BackboneGPUFunction`` instead."""
+
+    @staticmethod
+    def forward(ctx, input, angles_length):
+        raise RuntimeError("Angles2BackboneCPUFunction: this build has no CPU path; "
+                           "move the tensors to a CUDA device")
+
+    @staticmethod
+    def backward(ctx, gradOutput):  # pragma: no cover - forward never succeeds
+        raise RuntimeError("Angles2BackboneCPUFunction: this build has no CPU path")
+
+
 class Angles2Backbone(Module):
     def __init__(self):
         super(Angles2Backbone, self).__init__()

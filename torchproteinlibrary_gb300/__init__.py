@@ -38,13 +38,29 @@ def load_extension(name: str):
             f"or `python -m torchproteinlibrary_gb300._build`") from e
 
 
-def install_alias() -> None:
-    """Make ``import TorchProteinLibrary`` (and its ReducedModel / FullAtomModel
-    sub-packages) resolve to this package."""
-    from . import RMSD, FullAtomModel, ReducedModel  # noqa: F401
+_ALIAS = "TorchProteinLibrary"
+_ALIASED_PACKAGES = ("ReducedModel", "FullAtomModel", "RMSD")
 
-    sys.modules.setdefault("TorchProteinLibrary", sys.modules[__name__])
-    for sub in ("ReducedModel", "FullAtomModel", "RMSD"):
-        sys.modules.setdefault(f"TorchProteinLibrary.{sub}", sys.modules[f"{__name__}.{sub}"])
+
+def install_alias() -> None:
+    """Make ``import TorchProteinLibrary`` and every module below its ReducedModel,
+    FullAtomModel and RMSD packages (``TorchProteinLibrary.FullAtomModel.CoordsTransform``
+    and so on), as well as the bare extension names ``_ReducedModel``,
+    ``_FullAtomModel`` and ``_RMSD``, resolve to this package's modules.
+
+    Each alias is the same module object as the original, so classes compare
+    identical whichever name imported them.  Names already present in
+    ``sys.modules`` (an installed reference, say) are left alone."""
+    import pkgutil
+
+    sys.modules.setdefault(_ALIAS, sys.modules[__name__])
+    for sub in _ALIASED_PACKAGES:
+        pkg = importlib.import_module(f"{__name__}.{sub}")
+        for info in pkgutil.walk_packages(pkg.__path__, prefix=f"{pkg.__name__}."):
+            importlib.import_module(info.name)
+    prefix = f"{__name__}."
+    for name, module in list(sys.modules.items()):
+        if name.startswith(prefix) and name[len(prefix):].split(".")[0] in _ALIASED_PACKAGES:
+            sys.modules.setdefault(_ALIAS + name[len(__name__):], module)
     for ext in ("_ReducedModel", "_FullAtomModel", "_RMSD"):
         sys.modules.setdefault(ext, load_extension(ext))

@@ -360,6 +360,50 @@ void getBBox(torch::Tensor input_coords, torch::Tensor a, torch::Tensor b, torch
     check_status(s, "getBBox");
 }
 
+// ------------------------------------------------------------ random poses
+// Host helpers of the reference (coordsTransform_interface.cpp:201-259 over
+// Math/nUtil.cpp:60-100), which fill small [B, 3, 3] / [B, 3] tensors for a
+// training loop's data augmentation.  They are tensor arithmetic here, so they
+// accept tensors on any device; the draws come from torch.rand (torch.manual_seed
+// applies, as it does for the reference's draws).
+
+// Rotation from u in [0, 1)^3 through the unit quaternion
+// q = (sqrt(1-u1) sin 2 pi u2, sqrt(1-u1) cos 2 pi u2, sqrt(u1) sin 2 pi u3, sqrt(u1) cos 2 pi u3).
+torch::Tensor rotation_from_uniform(const torch::Tensor &u) {
+    const torch::Tensor ud = u.to(torch::kDouble);
+    const double two_pi = 6.283185307179586;
+    const torch::Tensor u1 = ud.select(1, 0), w2 = ud.select(1, 1) * two_pi, w3 = ud.select(1, 2) * two_pi;
+    const torch::Tensor s1 = torch::sqrt(1.0 - u1), s2 = torch::sqrt(u1);
+    const torch::Tensor q0 = s1 * torch::sin(w2), q1 = s1 * torch::cos(w2), q2 = s2 * torch::sin(w3),
+                        q3 = s2 * torch::cos(w3);
+    return torch::stack({q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3, 2.0 * (q1 * q2 - q0 * q3), 2.0 * (q1 * q3 + q0 * q2),
+                         2.0 * (q1 * q2 + q0 * q3), q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3, 2.0 * (q2 * q3 - q0 * q1),
+                         2.0 * (q1 * q3 - q0 * q2), 2.0 * (q2 * q3 + q0 * q1), q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3},
+                        1)
+        .view({-1, 3, 3});
+}
+
+void getRotation(torch::Tensor R, torch::Tensor u) {
+    TORCH_CHECK(R.dim() == 3 && R.size(1) == 3 && R.size(2) == 3, "getRotation: R must be [batch, 3, 3]");
+    TORCH_CHECK(u.dim() == 2 && u.size(0) == R.size(0) && u.size(1) >= 3, "getRotation: u must be [batch, 3]");
+    R.copy_(rotation_from_uniform(u.to(R.device())));
+}
+
+void getRandomRotation(torch::Tensor R) {
+    TORCH_CHECK(R.dim() == 3 && R.size(1) == 3 && R.size(2) == 3, "getRandomRotation: R must be [batch, 3, 3]");
+    R.copy_(rotation_from_uniform(torch::rand({R.size(0), 3}, R.options().dtype(torch::kDouble))));
+}
+
+// T_k ~ U[-d_k, d_k], d_k = max(0, volume_size / 2 - (b_k - a_k) / 2) / 2: the box [a, b]
+// stays inside a cube of side volume_size centred on the origin.
+void getRandomTranslation(torch::Tensor T, torch::Tensor a, torch::Tensor b, double volume_size) {
+    TORCH_CHECK(T.dim() == 2 && T.size(1) == 3, "getRandomTranslation: T must be [batch, 3]");
+    TORCH_CHECK(a.sizes() == T.sizes() && b.sizes() == T.sizes(), "getRandomTranslation: a and b must be [batch, 3]");
+    const torch::Tensor ad = a.to(T.device(), torch::kDouble), bd = b.to(T.device(), torch::kDouble);
+    const torch::Tensor d = torch::clamp_min(volume_size / 2.0 - (bd - ad) / 2.0, 0.0) * 0.5;
+    T.copy_(torch::rand(T.sizes(), T.options().dtype(torch::kDouble)) * (2.0 * d) - d);
+}
+
 // ---------------------------------------------------------- Coords2TypedCoords
 // Reference entry points (Layers/FullAtomModel/Coords2TypedCoords/
 // coords2typedcoords_interface.cpp), on CUDA tensors.  Typed rows hold
@@ -501,6 +545,9 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Coords2Center_forward", &no_cpu_center, "not available: no CPU path");
     m.def("Coords2Center_backward", &no_cpu_center, "not available: no CPU path");
     m.def("getBBox", &getBBox, "per-chain bounding box (GPU)");
+    m.def("getRotation", &getRotation, "rotation matrices from uniform parameters");
+    m.def("getRandomRotation", &getRandomRotation, "uniformly random rotations");
+    m.def("getRandomTranslation", &getRandomTranslation, "random translation keeping a box inside a cube");
     m.def("PDB2CoordsUnordered", &PDB2CoordsUnordered, "Convert PDB to coordinates in the PDB order");
     m.def(
         "set_options",
