@@ -139,6 +139,98 @@ __device__ __forceinline__ void from_pair(const PairFrame &g, Frame<float> &f) {
     f.p[2] = g.p2;
 }
 
+__device__ __forceinline__ PairFrame pair_identity() {
+    PairFrame g;
+    g.c[0] = make_float2(1.f, 0.f);
+    g.c[1] = make_float2(0.f, 1.f);
+    g.c[2] = make_float2(0.f, 0.f);
+    g.r2[0] = 0.f;
+    g.r2[1] = 0.f;
+    g.r2[2] = 1.f;
+    g.p = make_float2(0.f, 0.f);
+    g.p2 = 0.f;
+    return g;
+}
+
+// compose (tpl_common.cuh) on PairFrames, c = a o b: 12 paired and 12 scalar
+// operations, with the same rounding as the scalar form (each output is the same
+// chain of fused multiply-adds).
+__device__ __forceinline__ PairFrame compose_pair(const PairFrame &a, const PairFrame &b) {
+    PairFrame c;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const float b0 = b.c[j].x, b1 = b.c[j].y, b2 = b.r2[j];  // column j of b's rotation
+        c.c[j] = __ffma2_rn(a.c[0], f2(b0), __ffma2_rn(a.c[1], f2(b1), __fmul2_rn(a.c[2], f2(b2))));
+        c.r2[j] = fmaf(a.r2[0], b0, fmaf(a.r2[1], b1, a.r2[2] * b2));
+    }
+    c.p = __ffma2_rn(a.c[0], f2(b.p.x), __ffma2_rn(a.c[1], f2(b.p.y), __ffma2_rn(a.c[2], f2(b.p2), a.p)));
+    c.p2 = fmaf(a.r2[0], b.p.x, fmaf(a.r2[1], b.p.y, fmaf(a.r2[2], b.p2, a.p2)));
+    return c;
+}
+
+__device__ __forceinline__ PairFrame shfl_up_pair(const PairFrame &f, int delta) {
+    PairFrame o;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        o.c[j].x = __shfl_up_sync(0xffffffffu, f.c[j].x, delta);
+        o.c[j].y = __shfl_up_sync(0xffffffffu, f.c[j].y, delta);
+        o.r2[j] = __shfl_up_sync(0xffffffffu, f.r2[j], delta);
+    }
+    o.p.x = __shfl_up_sync(0xffffffffu, f.p.x, delta);
+    o.p.y = __shfl_up_sync(0xffffffffu, f.p.y, delta);
+    o.p2 = __shfl_up_sync(0xffffffffu, f.p2, delta);
+    return o;
+}
+
+__device__ __forceinline__ PairFrame shfl_idx_pair(const PairFrame &f, int src) {
+    PairFrame o;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        o.c[j].x = __shfl_sync(0xffffffffu, f.c[j].x, src);
+        o.c[j].y = __shfl_sync(0xffffffffu, f.c[j].y, src);
+        o.r2[j] = __shfl_sync(0xffffffffu, f.r2[j], src);
+    }
+    o.p.x = __shfl_sync(0xffffffffu, f.p.x, src);
+    o.p.y = __shfl_sync(0xffffffffu, f.p.y, src);
+    o.p2 = __shfl_sync(0xffffffffu, f.p2, src);
+    return o;
+}
+
+__device__ __forceinline__ void renormalize_pair(PairFrame &g) {
+    Frame<float> f;
+    from_pair(g, f);
+    renormalize(f);
+    g = to_pair(f);
+}
+
+// warp_exclusive_total on PairFrames: the exclusive prefix of the lane transforms in
+// lane order (Kogge-Stone over shuffles), and the warp total.
+__device__ __forceinline__ PairFrame warp_exclusive_total_pair(PairFrame t, int lane, bool renorm,
+                                                               PairFrame &total) {
+    if (renorm) renormalize_pair(t);
+#pragma unroll
+    for (int off = 1; off < kWarp; off <<= 1) {
+        const PairFrame o = shfl_up_pair(t, off);
+        if (lane >= off) t = compose_pair(o, t);
+    }
+    total = shfl_idx_pair(t, 31);
+    PairFrame exc = shfl_up_pair(t, 1);
+    if (lane == 0) exc = pair_identity();
+    return exc;
+}
+
+__device__ __forceinline__ void pair_store(float *dst, const PairFrame &g) {
+    Frame<float> f;
+    from_pair(g, f);
+    frame_store(dst, f);
+}
+
+__device__ __forceinline__ PairFrame pair_load(const float *src) {
+    Frame<float> f;
+    frame_load(f, src);
+    return to_pair(f);
+}
+
 // apply_joint (tpl_common.cuh) on a PairFrame: 9 paired and 9 scalar operations.
 __device__ __forceinline__ void apply_joint_pair(PairFrame &f, float cb, float sb, float d, float ca, float sa) {
     const float2 c0 = f.c[0], c1 = f.c[1], c2 = f.c[2];
@@ -164,7 +256,7 @@ template <bool FAST>
 __device__ __forceinline__ void walk4(const BondConsts &bc, Frame<float> &f, const float (&a0)[4],
                                       const float (&a1)[4], const float (&a2)[4], float *seg) {
     float buf[36];
-    if (FAST) {
+    if constexpr (FAST) {
         float so[4], co[4];  // omega pairs (residues 0-1, 2-3)
         sincos_fast2(a2[0], a2[1], &so[0], &co[0], &so[1], &co[1]);
         sincos_fast2(a2[2], a2[3], &so[2], &co[2], &so[3], &co[3]);
@@ -186,27 +278,25 @@ __device__ __forceinline__ void walk4(const BondConsts &bc, Frame<float> &f, con
                         make_float4(buf[4 * q], buf[4 * q + 1], buf[4 * q + 2], buf[4 * q + 3]);
         }
         from_pair(g, f);
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        float s0, c0, s1, c1, s2, c2;
-        {
+        for (int r = 0; r < 4; r++) {
+            float s0, c0, s1, c1, s2, c2;
             sincos_poly(a0[r], &s0, &c0);
             sincos_poly(a1[r], &s1, &c1);
             sincos_poly(a2[r], &s2, &c2);
-        }
-        buf[9 * r] = f.p[0]; buf[9 * r + 1] = f.p[1]; buf[9 * r + 2] = f.p[2];
-        apply_joint(f, bc.cb[0], bc.sb[0], bc.d[0], c0, s0);
-        buf[9 * r + 3] = f.p[0]; buf[9 * r + 4] = f.p[1]; buf[9 * r + 5] = f.p[2];
-        apply_joint(f, bc.cb[1], bc.sb[1], bc.d[1], c1, s1);
-        buf[9 * r + 6] = f.p[0]; buf[9 * r + 7] = f.p[1]; buf[9 * r + 8] = f.p[2];
-        apply_joint(f, bc.cb[2], bc.sb[2], bc.d[2], c2, s2);
+            buf[9 * r] = f.p[0]; buf[9 * r + 1] = f.p[1]; buf[9 * r + 2] = f.p[2];
+            apply_joint(f, bc.cb[0], bc.sb[0], bc.d[0], c0, s0);
+            buf[9 * r + 3] = f.p[0]; buf[9 * r + 4] = f.p[1]; buf[9 * r + 5] = f.p[2];
+            apply_joint(f, bc.cb[1], bc.sb[1], bc.d[1], c1, s1);
+            buf[9 * r + 6] = f.p[0]; buf[9 * r + 7] = f.p[1]; buf[9 * r + 8] = f.p[2];
+            apply_joint(f, bc.cb[2], bc.sb[2], bc.d[2], c2, s2);
 #pragma unroll
-        for (int q = 0; q < 9; q++)  // flush the float4s this residue completed
-            if (4 * q + 3 <= 9 * r + 8 && 4 * q + 3 > 9 * r - 1)
-                *reinterpret_cast<float4 *>(seg + 4 * q) =
-                    make_float4(buf[4 * q], buf[4 * q + 1], buf[4 * q + 2], buf[4 * q + 3]);
+            for (int q = 0; q < 9; q++)  // flush the float4s this residue completed
+                if (4 * q + 3 <= 9 * r + 8 && 4 * q + 3 > 9 * r - 1)
+                    *reinterpret_cast<float4 *>(seg + 4 * q) =
+                        make_float4(buf[4 * q], buf[4 * q + 1], buf[4 * q + 2], buf[4 * q + 3]);
+        }
     }
 }
 
@@ -278,6 +368,14 @@ __device__ __forceinline__ void map_positions(float *seg, const Frame<float> &P,
     else map_points<C, true>(seg, P, len - j0);
 }
 
+// The map stays scalar: paired arithmetic there makes the forwards spill registers.
+template <int C>
+__device__ __forceinline__ void map_positions(float *seg, const PairFrame &P, int j0, int len) {
+    Frame<float> Pf;
+    from_pair(P, Pf);
+    map_positions<C>(seg, Pf, j0, len);
+}
+
 // Stage floats [0, 32 SEG) of a chunk: src[f] for f < nvalid, 0 after.  Lane l's
 // segment (floats l SEG .. l SEG + SEG - 1) lands at stage + l SP.
 template <int SEG, int SP>
@@ -343,25 +441,17 @@ struct FwdStage {
     __device__ static __forceinline__ int lane_offset(int l) { return l * SEG + GAP * (l >> 2); }
 };
 
-// store_chunk for the FwdStage layout.
+// store_chunk for the FwdStage layout: float4 q of the chunk (floats 4q..4q+3, in lane
+// segment floor(4q / SEG)) is staged at float 4q + GAP floor(q / SEG).
 template <int C>
 __device__ __forceinline__ void store_chunk_fwd(float *dst, const float *stage, int n, int lane, bool vec) {
     using S = FwdStage<C>;
     constexpr int SEG = S::SEG;
     if (vec) {
-        constexpr int kStepSeg = 128 / SEG, kStepOff = 128 - kStepSeg * SEG;
-        int sl = (4 * lane) / SEG, off = 4 * lane - sl * SEG;
 #pragma unroll 2
-        for (int q = lane; 4 * q < n; q += 32) {
+        for (int q = lane; 4 * q < n; q += 32)
             __stcs(reinterpret_cast<float4 *>(dst) + q,
-                   *reinterpret_cast<const float4 *>(stage + S::lane_offset(sl) + off));
-            sl += kStepSeg;
-            off += kStepOff;
-            if (off >= SEG) {
-                off -= SEG;
-                sl += 1;
-            }
-        }
+                   *reinterpret_cast<const float4 *>(stage + 4 * q + S::GAP * (q / SEG)));
     } else {
         for (int f = lane; f < n; f += 32) {
             const int sl = f / SEG;
@@ -405,8 +495,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_
     ChainRecord *rec = a.rec + (size_t)b * a.nrec;
     const bool vec = a.vec != 0;
 
-    Frame<float> F;  // chain frame at the chunk start (world)
-    frame_identity(F);
+    PairFrame F = pair_identity();  // chain frame at the chunk start (world)
     for (int s0 = 0; s0 < a.L; s0 += CH) {
         const int nout = min(CH, a.L - s0);
         float *dst = out + (size_t)9 * s0;
@@ -415,20 +504,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_
             continue;
         }
         const int j0 = s0 + C * lane;
-        const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg);
-        Frame<float> tot;
-        const Frame<float> E = warp_exclusive_total(t, lane, a.renorm, tot);
+        PairFrame tot;
+        const PairFrame E = warp_exclusive_total_pair(to_pair(walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg)),
+                                                      lane, a.renorm, tot);
         // E composes at most 31 renormalised lane transforms: P needs no renormalisation
-        const Frame<float> P = compose(F, E);
-        if ((C * lane) % kRecordStride == 0 && j0 < len) {
-            float *r = rec[j0 / kRecordStride].f;
-#pragma unroll
-            for (int i = 0; i < 9; i++) r[i] = P.r[i];
-#pragma unroll
-            for (int i = 0; i < 3; i++) r[9 + i] = P.p[i];
-        }
-        F = compose(F, tot);
-        if (a.renorm) renormalize(F);
+        const PairFrame P = compose_pair(F, E);
+        if ((C * lane) % kRecordStride == 0 && j0 < len) pair_store(rec[j0 / kRecordStride].f, P);
+        F = compose_pair(F, tot);
+        if (a.renorm) renormalize_pair(F);
         map_positions<C>(seg, P, j0, len);
         __syncwarp();
         store_chunk_fwd<C>(dst, stage, 9 * nout, lane, vec);
@@ -1016,24 +1099,18 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
         const int nout = min(CH, a.L - s0);
         const bool live = s0 < len;
         const int j0 = s0 + C * lane;
-        Frame<float> E, tot;
-        frame_identity(E);
-        frame_identity(tot);
-        if (live) {
-            const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg);
-            E = warp_exclusive_total(t, lane, a.renorm, tot);
-        }
-        Frame<float> F;  // chain frame at the chunk start
-        if (k == 0) {
-            frame_identity(F);
-        } else {
+        PairFrame E = pair_identity(), tot = pair_identity();
+        if (live) E = warp_exclusive_total_pair(to_pair(walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg)), lane,
+                                                a.renorm, tot);
+        PairFrame F = pair_identity();  // chain frame at the chunk start
+        if (k > 0) {
             ring_wait(k);
-            frame_load(F, s_ring[k & 3]);
+            F = pair_load(s_ring[k & 3]);
         }
         if (k + 1 < nchunk) {
-            Frame<float> Fn = compose(F, tot);
-            if (a.renorm) renormalize(Fn);
-            if (lane == 0) frame_store(s_ring[(k + 1) & 3], Fn);
+            PairFrame Fn = compose_pair(F, tot);
+            if (a.renorm) renormalize_pair(Fn);
+            if (lane == 0) pair_store(s_ring[(k + 1) & 3], Fn);
             ring_signal(k + 1);
         }
         float *dst = out + (size_t)9 * s0;
@@ -1041,8 +1118,8 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
             zero_floats(dst, 9 * nout, lane, vec);
             continue;
         }
-        const Frame<float> P = compose(F, E);
-        if ((C * lane) % kRecordStride == 0 && j0 < len) frame_store(rec[j0 / kRecordStride].f, P);
+        const PairFrame P = compose_pair(F, E);
+        if ((C * lane) % kRecordStride == 0 && j0 < len) pair_store(rec[j0 / kRecordStride].f, P);
         map_positions<C>(seg, P, j0, len);
         __syncwarp();
         store_chunk_fwd<C>(dst, stage, 9 * nout, lane, vec);

@@ -44,14 +44,15 @@ __device__ __forceinline__ void sincos_fast(float a, float *s, float *c) {
 // are k mod 4, so no float-to-integer conversion is needed.  Valid for |a| <= 1e4.
 __device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 
+// sin and cos of a = r + q pi/2 (mod 2 pi) from sin r, cos r and the low bits of q: odd q
+// swaps them; bit 1 of q is the sign of sin, bit 1 of q + 1 the sign of cos.
 __device__ __forceinline__ void quadrant(float sr, float cr, int t_bits, float *s, float *c) {
-    const int q = t_bits & 3;  // a = r + q pi/2 (mod 2 pi)
-    float ss = (q & 1) ? cr : sr;
-    float cc = (q & 1) ? sr : cr;
-    ss = __int_as_float(__float_as_int(ss) ^ ((q & 2) << 30));
-    cc = __int_as_float(__float_as_int(cc) ^ (((q + 1) & 2) << 30));
-    *s = ss;
-    *c = cc;
+    const unsigned u = (unsigned)t_bits;
+    const bool odd = (u & 1u) != 0u;
+    const unsigned ssign = (u << 30) & 0x80000000u;
+    const unsigned csign = ((u + 1u) << 30) & 0x80000000u;
+    *s = __uint_as_float(__float_as_uint(odd ? cr : sr) ^ ssign);
+    *c = __uint_as_float(__float_as_uint(odd ? sr : cr) ^ csign);
 }
 
 __device__ __forceinline__ void sincos_fast2(float a0, float a1, float *s0, float *c0, float *s1, float *c1) {
