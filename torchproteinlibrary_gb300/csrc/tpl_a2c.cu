@@ -20,10 +20,12 @@
 // over tiles, threads and residues; side-chain joints use prefix sums over the
 // side-chain path of their residue.  Complexity O(atoms) per chain instead of
 // the reference's O(nodes x subtree).
+#include <cstddef>
 #include <cstdio>
 
 #include "tpl_common.cuh"
 #include "tpl_internal.h"
+#include "tpl_pair.cuh"
 #include "tpl_sincos.cuh"
 #include "tpl_topology.cuh"
 
@@ -201,11 +203,12 @@ __device__ __forceinline__ void a2c_tile_prefix(const Frame<T> &carry, const Fra
     tile_cnt = cr;
 }
 
-// All atoms of residue j (type ty) from the frame P at its N atom.  emit(slot, xyz)
-// receives positions in P's coordinates; returns the frame at the next N.
-template <typename T, typename Emit>
+// All atoms of residue j (type ty) from the frame P at its N atom.  chi_angle(q)
+// returns the residue's chi_(q+1); emit(slot, xyz) receives positions in P's
+// coordinates; returns the frame at the next N.
+template <typename T, typename Chi, typename Emit>
 __device__ __forceinline__ void residue_atoms(const Topology<T> &tp, int ty, Frame<T> &P, const T cs[3],
-                                              const T sn[3], const T *chi_ang, int chi_stride, Emit emit) {
+                                              const T sn[3], Chi chi_angle, Emit emit) {
     emit(0, P.p);
     Frame<T> F = P;
     apply_joint(F, tp.bb_cb[0], tp.bb_sb[0], tp.bb_d[0], cs[0], sn[0]);
@@ -225,7 +228,7 @@ __device__ __forceinline__ void residue_atoms(const Topology<T> &tp, int ty, Fra
         for (int k = 0; k < nj; k++) {
             const int chi = tp.jchi[ty][k];
             T c = T(1), s = T(0);
-            if (chi >= 0) sc(chi_ang[(size_t)chi * chi_stride], &s, &c);
+            if (chi >= 0) sc(chi_angle(chi), &s, &c);
             apply_joint(S, tp.jcb[ty][k], tp.jsb[ty][k], tp.jd[ty][k], c, s);
             const int f0 = tp.jfirst[ty][k];
             for (int a = 0; a < tp.jna[ty][k]; a++) {
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
             if (j < n) {
                 const int ty = sm.type[j];
                 T *dst = sm.xyz + 3 * aoff;
-                residue_atoms<T>(sm.topo, ty, P, ts.cs[r], ts.sn[r], &sm.ang[3][j], TILE,
+                residue_atoms<T>(sm.topo, ty, P, ts.cs[r], ts.sn[r], [&](int q) { return sm.ang[3 + q][j]; },
                                  [&](int slot, const T *x) {
                                      dst[3 * slot] = x[0] + org[0];
                                      dst[3 * slot + 1] = x[1] + org[1];
@@ -359,6 +362,156 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
     if (rn && an)
         for (int i = total + tid; i < a.maxA; i += NT) rn[i] = an[i] = 0u;
     (void)lane;
+}
+
+// --------------------------------------------- forward, four warps per chain
+// One CTA of four warps per chain and chunks of 32 residues, one per lane; chunk k
+// belongs to warp k % 4.  Per chunk a warp loads its residues' backbone angles,
+// composes each residue's three backbone joints (N -> CA -> C -> next N), scans the
+// lane transforms and the atom counts over the warp, and places every atom of its
+// residue from the lane's frame at N into a per-warp staging buffer, from which the
+// chunk's contiguous atom range leaves with coalesced stores.  Only the chain frame
+// at the chunk start and the chunk's first atom index pass between warps, through
+// the named-barrier handoff of tpl_pair.cuh, so the chunk loop has no CTA-wide
+// barrier.  Positions are built relative to the chunk's first N atom and moved to
+// it as they are staged.
+constexpr int kA2cRingWarps = 4;
+constexpr int kA2cChunk = 32;
+constexpr int kA2cStageAtoms = kA2cChunk * kMaxResAtoms;
+
+struct A2cRingSmem {
+    Topology<float> topo;
+    signed char lut[256];
+    float xyz[kA2cRingWarps][kA2cStageAtoms * 3];
+    uint32_t res_name[kA2cRingWarps][kA2cStageAtoms];  // present when names are written
+    uint32_t atom_name[kA2cRingWarps][kA2cStageAtoms];
+};
+constexpr size_t kA2cRingSmemNoNames = offsetof(A2cRingSmem, res_name);
+
+template <bool NAMES>
+__global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_fwd_ring_kernel(A2cArgs<float> a, int renorm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    A2cRingSmem &sm = *reinterpret_cast<A2cRingSmem *>(smem_raw);
+    __shared__ __align__(16) float s_ring[kA2cRingWarps][16];  // chain frame (12) and first atom index
+    __shared__ int s_len, s_bad, s_total;
+
+    const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    if (tid == 0) s_total = 0;  // ordered before every chunk by the barriers of chain_length
+    load_topology<float, 32 * kA2cRingWarps>(sm.topo, sm.lut);
+    const Topology<float> &tp = sm.topo;
+    const unsigned char *row = a.seq + (size_t)b * a.seq_stride;
+    const int len = chain_length<32 * kA2cRingWarps>(row, a.seq_stride, sm.lut, &s_len, &s_bad);
+    const bool ok = !s_bad && len <= a.L;
+    if (tid == 0) {
+        if (s_bad) a2c_error(a.hdr, TPL_ERR_SEQUENCE);
+        if (len > a.L) a2c_error(a.hdr, TPL_ERR_LENGTH);
+    }
+    float *out = a.coords + (size_t)b * 3 * a.maxA;
+    uint32_t *rn = NAMES ? a.res_names + (size_t)b * a.maxA : nullptr;
+    uint32_t *an = NAMES ? a.atom_names + (size_t)b * a.maxA : nullptr;
+    const float *ang = a.angles + (size_t)b * 8 * a.L;
+    float *stage = sm.xyz[w];
+    const int nchunk = ok ? (len + kA2cChunk - 1) / kA2cChunk : 0;
+
+#pragma unroll 1
+    for (int k = w; k < nchunk; k += kA2cRingWarps) {
+        const int j = k * kA2cChunk + lane;
+        const bool live = j < len;
+        const int ty = live ? sm.lut[row[j]] : 0;
+        const int na = live ? tp.natoms[ty] : 0;
+        // backbone angles; omega of the chain's last residue moves no atom
+        float cs[3] = {1.f, 1.f, 1.f}, sn[3] = {0.f, 0.f, 0.f};
+        float chi[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // loaded with the backbone angles: one latency per chunk
+        PairFrame t = pair_identity();
+        if (live) {
+            const float phi = ang[j], psi = ang[a.L + j];
+            const float om = j + 1 < len ? ang[2 * a.L + j] : 0.f;
+#pragma unroll
+            for (int q = 0; q < 5; q++) chi[q] = ang[(size_t)(3 + q) * a.L + j];
+            if (fmaxf(fabsf(phi), fmaxf(fabsf(psi), fabsf(om))) <= 1.0e4f) {
+                sincos_fast2(phi, psi, &sn[0], &cs[0], &sn[1], &cs[1]);
+                sincos_fast(om, &sn[2], &cs[2]);
+            } else {
+                sincos_poly(phi, &sn[0], &cs[0]);
+                sincos_poly(psi, &sn[1], &cs[1]);
+                sincos_poly(om, &sn[2], &cs[2]);
+            }
+#pragma unroll
+            for (int q = 0; q < 3; q++) apply_joint_pair(t, tp.bb_cb[q], tp.bb_sb[q], tp.bb_d[q], cs[q], sn[q]);
+        }
+        PairFrame tot;
+        const PairFrame E = warp_exclusive_total_pair(t, lane, renorm != 0, tot);
+        int ci = na;  // atoms of the lanes up to this one
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, ci, off);
+            if (lane >= off) ci += o;
+        }
+        const int cnt = __shfl_sync(0xffffffffu, ci, 31), aoff = ci - na;
+
+        PairFrame F = pair_identity();  // chain frame at the chunk start
+        int abase = 0;                  // first atom of the chunk
+        if (k > 0) {
+            ring_wait(k);
+            F = pair_load(s_ring[k & 3]);
+            abase = __float_as_int(s_ring[k & 3][12]);
+        }
+        if (k + 1 < nchunk) {
+            PairFrame Fn = compose_pair(F, tot);
+            if (renorm) renormalize_pair(Fn);
+            if (lane == 0) {
+                pair_store(s_ring[(k + 1) & 3], Fn);
+                s_ring[(k + 1) & 3][12] = __int_as_float(abase + cnt);
+            }
+            ring_signal(k + 1);
+        } else if (lane == 0) {
+            s_total = abase + cnt;
+        }
+
+        const float org[3] = {F.p.x, F.p.y, F.p2};
+        PairFrame Fr = F;  // rotation only: positions relative to the chunk origin
+        Fr.p = make_float2(0.f, 0.f);
+        Fr.p2 = 0.f;
+        if (live) {
+            Frame<float> P;
+            from_pair(compose_pair(Fr, E), P);
+            float *dst = stage + 3 * aoff;
+            const auto chi_angle = [&](int q) {  // register selects: a dynamic index would go to local memory
+                float v = chi[0];
+#pragma unroll
+                for (int i = 1; i < 5; i++) v = q == i ? chi[i] : v;
+                return v;
+            };
+            residue_atoms<float>(tp, ty, P, cs, sn, chi_angle, [&](int slot, const float *x) {
+                dst[3 * slot] = x[0] + org[0];
+                dst[3 * slot + 1] = x[1] + org[1];
+                dst[3 * slot + 2] = x[2] + org[2];
+            });
+            if (NAMES)
+                for (int q = 0; q < na; q++) {
+                    sm.res_name[w][aoff + q] = tp.res_name[ty];
+                    sm.atom_name[w][aoff + q] = tp.atom_name[ty][q];
+                }
+        }
+        __syncwarp();
+        const int nstore = max(0, min(cnt, a.maxA - abase));
+        for (int i = lane; i < 3 * nstore; i += 32) out[(size_t)3 * abase + i] = stage[i];
+        if (NAMES)
+            for (int i = lane; i < nstore; i += 32) {
+                rn[abase + i] = sm.res_name[w][i];
+                an[abase + i] = sm.atom_name[w][i];
+            }
+        __syncwarp();  // the warp's next chunk rewrites the staging buffers
+    }
+    __syncthreads();
+    int total = s_total;
+    if (total > a.maxA) {
+        if (tid == 0) a2c_error(a.hdr, TPL_ERR_ATOMS);
+        total = a.maxA;
+    }
+    for (int i = 3 * total + tid; i < 3 * a.maxA; i += 32 * kA2cRingWarps) out[i] = 0.f;
+    if (NAMES)
+        for (int i = total + tid; i < a.maxA; i += 32 * kA2cRingWarps) rn[i] = an[i] = 0u;
 }
 
 // ------------------------------------------------------------------ backward
@@ -461,7 +614,8 @@ __global__ void __launch_bounds__(NT) a2c_bwd_kernel(A2cArgs<T> a, int renorm, i
                 const int ty = sm.f.type[j];
                 T *dst = sm.f.xyz + 3 * aoff;
                 const T *gg = sm.g + 3 * aoff;
-                residue_atoms<T>(tp, ty, P, ts.cs[r], ts.sn[r], &sm.f.ang[3][j], TILE, [&](int slot, const T *x) {
+                residue_atoms<T>(tp, ty, P, ts.cs[r], ts.sn[r], [&](int q) { return sm.f.ang[3 + q][j]; },
+                                 [&](int slot, const T *x) {
                     dst[3 * slot] = x[0];
                     dst[3 * slot + 1] = x[1];
                     dst[3 * slot + 2] = x[2];
@@ -845,6 +999,199 @@ __global__ void __launch_bounds__(NT) a2c_bwd_coords_kernel(A2cArgs<float> a) {
         for (int i = from + tid; i < a.L; i += NT) gout[(size_t)k * a.L + i] = 0.f;
 }
 
+// Backward from the coordinates, four warps per chain: a2c_bwd_coords_kernel's
+// per-residue evaluation on chunks of 32 residues (one per lane), chunk k on warp
+// (nchunk - 1 - k) % 4, last chunk first.  The chunks' first atom indices come from
+// one pass over the sequence at the start; per chunk a warp stages the chunk's atom
+// range of coordinates and dL/dx with coalesced loads, sums G and S over each
+// lane's residue about the chunk's first N atom, suffix-scans them over the warp
+// and takes the sums over later chunks from the warp of chunk k + 1 (G, S and that
+// chunk's first N atom, through the named-barrier handoff of tpl_pair.cuh).
+__device__ __forceinline__ void cp_async4(float *dst_smem, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst_smem)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
+struct A2cBwdRingSmem {
+    Topology<float> topo;
+    signed char lut[256];
+    float x[kA2cRingWarps][kA2cStageAtoms * 3];
+    float g[kA2cRingWarps][kA2cStageAtoms * 3];
+    int base[1];  // first atom of each chunk, nchunk + 1 entries (dynamic)
+};
+
+__global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_bwd_coords_ring_kernel(A2cArgs<float> a) {
+    constexpr int NT = 32 * kA2cRingWarps;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    A2cBwdRingSmem &sm = *reinterpret_cast<A2cBwdRingSmem *>(smem_raw);
+    __shared__ __align__(16) float s_ring[kA2cRingWarps][12];
+    __shared__ int s_len, s_bad;
+
+    // chains last to first: the first CTAs read the rows the forward wrote last, which may still be in L2
+    const int b = (int)gridDim.x - 1 - (int)blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    load_topology<float, NT>(sm.topo, sm.lut);
+    const Topology<float> &tp = sm.topo;
+    const unsigned char *row = a.seq + (size_t)b * a.seq_stride;
+    const int len = chain_length<NT>(row, a.seq_stride, sm.lut, &s_len, &s_bad);
+    float *gout = a.grad_angles + (size_t)b * 8 * a.L;
+    const float *xin = a.coords + (size_t)b * 3 * a.maxA;
+    const float *gin = a.grad_coords + (size_t)b * 3 * a.maxA;
+    bool ok = !s_bad && len <= a.L;
+    const int nchunk = ok ? (len + kA2cChunk - 1) / kA2cChunk : 0;
+
+    // atoms per chunk (warp w counts chunks w, w + 4, ...), then their exclusive prefix
+    for (int c = w; c < nchunk; c += kA2cRingWarps) {
+        const int j = c * kA2cChunk + lane;
+        int n = j < len ? tp.natoms[sm.lut[row[j]]] : 0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
+        if (lane == 0) sm.base[c + 1] = n;
+    }
+    __syncthreads();
+    if (w == 0) {
+        int run = 0;
+        for (int c0 = 0; c0 < nchunk; c0 += 32) {
+            const int c = c0 + lane;
+            int v = c < nchunk ? sm.base[c + 1] : 0;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int o = __shfl_up_sync(0xffffffffu, v, off);
+                if (lane >= off) v += o;
+            }
+            if (c < nchunk) sm.base[c + 1] = run + v;
+            run += __shfl_sync(0xffffffffu, v, 31);
+        }
+        if (lane == 0) sm.base[0] = 0;
+    }
+    __syncthreads();
+    const int total = nchunk > 0 ? sm.base[nchunk] : 0;
+    if (tid == 0) {
+        if (s_bad) a2c_error(a.hdr, TPL_ERR_SEQUENCE);
+        if (len > a.L) a2c_error(a.hdr, TPL_ERR_LENGTH);
+        if (ok && total > a.maxA) a2c_error(a.hdr, TPL_ERR_ATOMS);
+    }
+    const int nrun = total > a.maxA ? 0 : nchunk;  // a chain whose atoms overflow the rows gets zeros
+    const float inv_dphi = 1.f / tp.bb_d[0], inv_dpsi = 1.f / tp.bb_d[1], inv_dom = 1.f / tp.bb_d[2];
+    float *sx = sm.x[w], *sg = sm.g[w];
+
+#pragma unroll 1
+    for (int k = nrun - 1 - w; k >= 0; k -= kA2cRingWarps) {
+        const int j = k * kA2cChunk + lane;
+        const bool live = j < len;
+        const int ty = live ? sm.lut[row[j]] : 0;
+        const int na = live ? tp.natoms[ty] : 0;
+        int inc = na;  // the residue's first atom inside the chunk: warp exclusive scan
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += v;
+        }
+        const int aoff = inc - na;
+        const int abase = sm.base[k], n3 = 3 * (sm.base[k + 1] - abase);
+        __syncwarp();  // the previous chunk's reads of the staging buffers are done
+        // asynchronous 4-byte copies: every copy of the chunk is in flight before the one wait
+        for (int i = lane; i < n3; i += 32) {
+            cp_async4(sx + i, xin + (size_t)3 * abase + i);
+            cp_async4(sg + i, gin + (size_t)3 * abase + i);
+        }
+        cp_async_wait_all();
+        __syncwarp();
+        const float o[3] = {sx[0], sx[1], sx[2]};  // chunk origin: its first N atom
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int q = 0; q < na; q++) add_atom(sx + 3 * (aoff + q), sg + 3 * (aoff + q), o, v, v + 3);
+        float later[6], ctot[6];
+#pragma unroll
+        for (int i = 0; i < 6; i++) later[i] = suffix_excl(v[i], lane, ctot[i]);
+        // the sums over later chunks, moved to this chunk's origin: S_o = S_on + (on - o) x G
+        float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, nN[3] = {0.f, 0.f, 0.f};
+        if (k + 1 < nrun) {
+            ring_wait(k);
+            const float *cin = s_ring[k & 3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                Gc[c] = cin[c];
+                Sc[c] = cin[3 + c];
+                nN[c] = cin[6 + c];
+            }
+            const float d[3] = {nN[0] - o[0], nN[1] - o[1], nN[2] - o[2]};
+            float dx[3];
+            cross3(d, Gc, dx);
+#pragma unroll
+            for (int c = 0; c < 3; c++) Sc[c] += dx[c];
+        }
+        if (k > 0) {
+            if (lane == 0) {
+                float *cout = s_ring[(k - 1) & 3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    cout[c] = Gc[c] + ctot[c];
+                    cout[3 + c] = Sc[c] + ctot[3 + c];
+                    cout[6 + c] = o[c];
+                }
+            }
+            ring_signal(k - 1);
+        }
+        if (live) {
+            float G[3] = {later[0] + Gc[0], later[1] + Gc[1], later[2] + Gc[2]};
+            float S[3] = {later[3] + Sc[0], later[4] + Sc[1], later[5] + Sc[2]};
+            const float *X = sx + 3 * aoff, *Gg = sg + 3 * aoff;
+            float xN[3], xA[3], xC[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                xN[c] = X[c] - o[c];
+                xA[c] = X[3 + c] - o[c];
+                xC[c] = X[3 * (na - 2) + c] - o[c];
+            }
+            float gr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (j + 1 < len) {  // omega_j: the next residue's N joint (the next chunk's first N after lane 31)
+                float xn[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) xn[c] = (lane == 31 ? nN[c] : X[3 * na + c]) - o[c];
+                gr[2] = joint_grad(xn, xC, inv_dom, G, S);
+            }
+            add_atom(X + 3 * (na - 1), Gg + 3 * (na - 1), o, G, S);  // O
+            gr[1] = joint_grad(xC, xA, inv_dpsi, G, S);
+            add_atom(X + 3 * (na - 2), Gg + 3 * (na - 2), o, G, S);  // C
+            // side chain, groups last to first; chi subtrees hold side-chain atoms only
+            float Gs[3] = {0.f, 0.f, 0.f}, Ss[3] = {0.f, 0.f, 0.f};
+            const int nj = tp.njoints[ty];
+            if (nj == 0)
+                for (int q = 2; q < na - 2; q++) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);  // Pro ring (none for Gly)
+            for (int kk = nj - 1; kk >= 0; kk--) {
+                const int f0 = 2 + tp.jfirst[ty][kk], f1 = f0 + tp.jna[ty][kk];
+                for (int q = f1 - 1; q >= f0; q--) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);
+                const int chi = tp.jchi[ty][kk];
+                if (chi >= 0) {
+                    const float *pk = X + 3 * f0;
+                    const float *pp = kk == 0 ? X + 3 : X + 3 * (2 + tp.jfirst[ty][kk - 1]);
+                    const float ok_[3] = {pk[0] - o[0], pk[1] - o[1], pk[2] - o[2]};
+                    const float op_[3] = {pp[0] - o[0], pp[1] - o[1], pp[2] - o[2]};
+                    const float gk = joint_grad(ok_, op_, 1.f / tp.jd[ty][kk], Gs, Ss);
+#pragma unroll
+                    for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
+                        if (chi == q) gr[3 + q] = gk;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                G[c] += Gs[c];
+                S[c] += Ss[c];
+            }
+            gr[0] = joint_grad(xA, xN, inv_dphi, G, S);
+#pragma unroll
+            for (int q = 0; q < 8; q++) gout[(size_t)q * a.L + j] = gr[q];
+        }
+    }
+    // zeros past the chain (and everywhere when the chain was rejected)
+    const int from = nrun > 0 ? len : 0;
+    for (int q = 0; q < 8; q++)
+        for (int i = from + tid; i < a.L; i += NT) gout[(size_t)q * a.L + i] = 0.f;
+}
+
 // ------------------------------------------------------------------ host side
 template <typename T, int R, int NT>
 static int launch_a2c_fwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t st) {
@@ -873,6 +1220,26 @@ static int launch_a2c_bwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t s
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
+// Four warps per chain once the batch gives every SM two chains or more; below that
+// the CTA-per-chain kernels keep more warps busy (GB300, 500-residue chains: 256
+// chains 0.023 against 0.027 ms forward, 4096 chains 0.28 against 0.17 ms).
+static bool a2c_use_ring(int B) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    return B >= 2 * sms;
+}
+
+static int launch_a2c_fwd_ring(const A2cArgs<float> &a, int B, int renorm, cudaStream_t st) {
+    const bool names = a.res_names && a.atom_names;
+    const size_t smem = names ? sizeof(A2cRingSmem) : kA2cRingSmemNoNames;
+    auto k = names ? a2c_fwd_ring_kernel<true> : a2c_fwd_ring_kernel<false>;
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), (int)smem))
+        return TPL_ERR_LAUNCH;
+    k<<<B, 32 * kA2cRingWarps, smem, st>>>(a, renorm);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
 int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *angles, void *coords,
                 uint32_t *res_names, uint32_t *atom_names, void *ws, int B, int L, int maxA,
                 const tpl_options &opt, cudaStream_t st) {
@@ -888,10 +1255,12 @@ int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *
     // threads_per_cta: 128 = 128 threads x 2 residues; 0 / 256 (default) or 512 = one
     // residue per thread
     switch (opt.threads_per_cta) {
+        case 4: return launch_a2c_fwd_ring(a, B, renorm, st);
         case 128: return launch_a2c_fwd<float, 2, 128>(a, B, renorm, st);
+        case 256: return launch_a2c_fwd<float, 1, 256>(a, B, renorm, st);
         case 512: return launch_a2c_fwd<float, 1, 512>(a, B, renorm, st);
     }
-    return launch_a2c_fwd<float, 1, 256>(a, B, renorm, st);
+    return a2c_use_ring(B) ? launch_a2c_fwd_ring(a, B, renorm, st) : launch_a2c_fwd<float, 1, 256>(a, B, renorm, st);
 }
 
 int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const unsigned char *seq, int seq_stride,
@@ -917,6 +1286,13 @@ int a2c_backward_coords(float *grad_angles, const float *grad_coords, const floa
     if (B == 0) return TPL_OK;
     A2cArgs<float> a{seq, seq_stride, nullptr, const_cast<float *>(coords), nullptr, nullptr, grad_angles, grad_coords,
                      (WsHeader *)ws, L, maxA};
+    if (a2c_use_ring(B)) {
+        const size_t smem = offsetof(A2cBwdRingSmem, base) + sizeof(int) * (size_t)((L + kA2cChunk - 1) / kA2cChunk + 1);
+        if (!set_max_dynamic_smem(reinterpret_cast<const void *>(a2c_bwd_coords_ring_kernel), (int)smem))
+            return TPL_ERR_LAUNCH;
+        a2c_bwd_coords_ring_kernel<<<B, 32 * kA2cRingWarps, smem, st>>>(a);
+        return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+    }
     constexpr int NT = 256;
     const size_t smem = sizeof(A2cCoordsSmem<NT>);
     auto k = a2c_bwd_coords_kernel<NT>;

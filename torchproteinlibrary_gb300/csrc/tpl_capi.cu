@@ -256,9 +256,10 @@ size_t tpl_a2c_workspace_bytes(int batch, int max_len, int max_atoms, const tpl_
     return sizeof(WsHeader);
 }
 
-// Angles2Coords reads only threads_per_cta (0 / 128, 256 or 512) and renormalize.
+// Angles2Coords reads only threads_per_cta (0 / 4, 128, 256 or 512) and renormalize.
 static bool a2c_options_ok(const tpl_options &o) {
-    return o.threads_per_cta == 0 || o.threads_per_cta == 128 || o.threads_per_cta == 256 || o.threads_per_cta == 512;
+    return o.threads_per_cta == 0 || o.threads_per_cta == 4 || o.threads_per_cta == 128 ||
+           o.threads_per_cta == 256 || o.threads_per_cta == 512;
 }
 
 static int a2c_fwd_common(bool f64, const uint8_t *sequences, int seq_stride, const void *angles, void *coords,
