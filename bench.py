@@ -641,7 +641,7 @@ def time_a2c(dev, steps=10, seed=1004):
     outs = {}
     # threads per chain of the float32 kernels: time each, keep the fastest
     sweep = []
-    for nt in (4, 128, 256, 512):
+    for nt in (4, 8, 128, 256, 512):
         fm.set_options(nt)
         a = ang.contiguous()
         c = torch.empty(B, 3 * maxA, device=dev)

@@ -164,10 +164,11 @@ size_t tpl_a2c_workspace_bytes(int batch, int max_len, int max_atoms, const tpl_
  *              to skip them (they depend on the sequences only)
  * Unknown letters, chains longer than max_len or with more than max_atoms atoms are
  * reported through the workspace status; such chains are zeroed.  One CTA walks a
- * chain (float32): opt->threads_per_cta 4 = four warps on chunks of 32 residues, one
- * per lane; 256 or 512 threads with one residue each; 128 threads with two residues
- * each; 0 (the default) = four warps from 2 x (number of SMs) chains up, else 256.
- * float64 always uses 128 threads with one residue each. */
+ * chain (float32): opt->threads_per_cta 4 or 8 = four or eight warps on chunks of 32
+ * residues, one per lane; 256 or 512 threads with one residue each; 128 threads with
+ * two residues each; 0 (the default) = eight warps below 8 x (number of SMs) chains
+ * (4 x with names), four from there.  float64 always uses 128 threads with one
+ * residue each. */
 int tpl_a2c_forward_f32(const uint8_t *sequences, int seq_stride, const float *angles, float *coords,
                         uint8_t *res_names, uint8_t *atom_names, void *workspace, size_t workspace_bytes, int batch,
                         int max_len, int max_atoms, const tpl_options *opt, void *stream);
@@ -198,8 +199,8 @@ int tpl_a2c_backward_f64(double *grad_angles, const double *grad_coords, const u
  * sequences and angles.  Same outputs and zeros as tpl_a2c_backward_f32; the
  * gradient's error against FP64 is about 1e-5 of its largest entry, since the axes
  * come from FP32 coordinate differences.  The workspace only needs its status word
- * (>= 64 bytes, zeroed once).  From 2 x (number of SMs) chains up, four warps share a
- * chain on chunks of 32 residues; below, one CTA of 256 threads walks it. */
+ * (>= 64 bytes, zeroed once).  Eight warps share a chain on chunks of 32 residues
+ * below 4 x (number of SMs) chains, four from there. */
 int tpl_a2c_backward_coords_f32(float *grad_angles, const float *grad_coords, const float *coords,
                                 const uint8_t *sequences, int seq_stride, void *workspace, size_t workspace_bytes,
                                 int batch, int max_len, int max_atoms, void *stream);

@@ -72,8 +72,9 @@ def test_golden_fp64(fm):
     check(c, gi, d["coords"], d["grad_angles"], na, COORD_TOL_F64, GRAD_TOL_F64)
 
 
-@pytest.mark.parametrize("dtype,threads", [(torch.float32, 0), (torch.float32, 4), (torch.float32, 128),
-                                           (torch.float32, 512), (torch.float64, 0)])
+@pytest.mark.parametrize("dtype,threads", [(torch.float32, 0), (torch.float32, 4), (torch.float32, 8),
+                                           (torch.float32, 128), (torch.float32, 256), (torch.float32, 512),
+                                           (torch.float64, 0)])
 def test_random_batch_matches_oracle(fm, dtype, threads):
     rng = np.random.default_rng(31)
     seqs = ["".join(rng.choice(list(AA), rng.integers(1, 300))) for _ in range(7)] + ["G", "P", "W", AA]
@@ -257,7 +258,7 @@ def test_config4_ragged_fp32_vs_fp64(fm):
     c64, _, _, na, _ = run_gpu(fm, ang, seqs, None, torch.float64)
     g = rng.standard_normal(c64.shape).astype(np.float32).astype(np.float64)
     c64, _, _, _, g64 = run_gpu(fm, ang, seqs, g, torch.float64)
-    for threads in (0, 4, 128, 512):
+    for threads in (0, 4, 8, 128, 512):
         fm.set_options(threads)
         try:
             c32, _, _, _, g32 = run_gpu(fm, ang, seqs, g, torch.float32)
@@ -268,17 +269,19 @@ def test_config4_ragged_fp32_vs_fp64(fm):
     check(c32, g32, c64, g64, na, COORD_TOL_F32, GRAD_TOL_F32)
 
 
-def test_four_warp_forward_chunk_edges(fm):
-    """Forward with four warps per chain (threads_per_cta = 4): chains ending on and
-    beside the 32-residue chunks and the four-warp rounds (128 residues), an empty
-    chain, with names, against the oracle; padding past each chain is zero."""
+@pytest.mark.parametrize("warps", [4, 8])
+def test_four_warp_forward_chunk_edges(fm, warps):
+    """Forward with four or eight warps per chain (threads_per_cta = 4 or 8): chains
+    ending on and beside the 32-residue chunks and the rounds of 128 and 256
+    residues, an empty chain, with names, against the oracle; padding past each
+    chain is zero."""
     rng = np.random.default_rng(44)
-    lens = [0, 1, 2, 31, 32, 33, 64, 65, 127, 128, 129, 160, 161, 257, 300]
+    lens = [0, 1, 2, 31, 32, 33, 64, 65, 127, 128, 129, 160, 161, 255, 256, 257, 300]
     seqs = ["".join(rng.choice(list(AA), n)) for n in lens]
     L = max(lens)
     ang = rng.uniform(-np.pi, np.pi, (len(seqs), 8, L)).astype(np.float32).astype(np.float64)
     rc, rrn, ran, na = oracle.a2c_forward(ang, seqs)
-    fm.set_options(4)
+    fm.set_options(warps)
     try:
         c, rn, an, na2, _ = run_gpu(fm, ang, seqs, None, torch.float32)
     finally:
@@ -324,12 +327,14 @@ def test_backward_from_coordinates_matches_oracle(fm):
 
 
 def test_four_warp_kernels_at_batch_size(fm):
-    """From 2 x (number of SMs) chains up the automatic choice runs the forward and
-    the backward from the coordinates with four warps per chain: the chains of
-    coords_case, repeated to that batch size, against the oracle in every replica."""
+    """Below 4 x (number of SMs) chains the automatic choice runs the forward with
+    names and the backward from the coordinates with eight warps per chain, from
+    there with four: the chains of coords_case, repeated to that batch size, against
+    the oracle in every replica (the other tests of this file run the eight-warp
+    kernels)."""
     seqs, ang, rc, na, g = coords_case(63)
     rg = oracle.a2c_backward(g, ang, seqs)
-    reps = -(-2 * torch.cuda.get_device_properties(0).multi_processor_count // len(seqs))
+    reps = -(-4 * torch.cuda.get_device_properties(0).multi_processor_count // len(seqs))
     c, _, _, na2, gi = run_gpu(fm, np.tile(ang, (reps, 1, 1)), seqs * reps, np.tile(g, (reps, 1)), torch.float32,
                                from_coords=True)
     n = len(seqs)

@@ -1,10 +1,12 @@
-"""Handoff schedule of the four-warps-per-chain kernels (a2b_fwd_ring_kernel,
-a2b_bwd_coords_ring_kernel), checked on the CPU before any GPU runs it.
+"""Handoff schedule of the kernels that share a chain between the W warps of a CTA
+(a2b_fwd_ring_kernel, a2b_bwd_coords_ring_kernel with W = 4; a2c_fwd_ring_kernel,
+a2c_bwd_coords_ring_kernel with W = 4 or 8), checked on the CPU before any GPU runs
+it.
 
 Each warp of the CTA owns the chunks the kernels give it (forward: chunk k on warp
-k % 4, visited in ascending order; backward: chunk k on warp (nchunk - 1 - k) % 4,
+k % W, visited in ascending order; backward: chunk k on warp (nchunk - 1 - k) % W,
 visited in descending order).  The carry into chunk k passes under named barrier
-1 + k % 4 with 64 threads: the producer warp arrives (bar.arrive), the consumer warp
+1 + k % W with 64 threads: the producer warp arrives (bar.arrive), the consumer warp
 syncs (bar.sync).  The model below replays every warp's sequence of barrier
 operations under random interleavings, with the hardware rule that a barrier phase
 completes once 64 threads (two warps) have arrived.  It checks that no schedule
@@ -15,10 +17,7 @@ import random
 
 import pytest
 
-WARPS = 4
-
-
-def warp_programs(nchunk, forward):
+def warp_programs(nchunk, forward, WARPS):
     progs = {w: [] for w in range(WARPS)}
     for w in range(WARPS):
         if forward:
@@ -39,7 +38,7 @@ def warp_programs(nchunk, forward):
     return progs
 
 
-def replay(progs, rng):
+def replay(progs, rng, WARPS):
     pc = {w: 0 for w in progs}
     blocked = set()
     phase = {}
@@ -50,7 +49,7 @@ def replay(progs, rng):
         w = rng.choice(ready)
         op, k = progs[w][pc[w]]
         pc[w] += 1
-        bid = 1 + (k & 3)
+        bid = 1 + k % WARPS
         members = phase.setdefault(bid, [])
         members.append((w, op, k))
         if op == "sync":
@@ -64,13 +63,14 @@ def replay(progs, rng):
             phase[bid] = []
 
 
+@pytest.mark.parametrize("warps", [4, 8])
 @pytest.mark.parametrize("forward", [True, False])
-def test_ring_handoffs_never_deadlock_or_mix(forward):
+def test_ring_handoffs_never_deadlock_or_mix(forward, warps):
     for nchunk in range(0, 40):
-        progs = warp_programs(nchunk, forward)
+        progs = warp_programs(nchunk, forward, warps)
         n_sync = sum(op == "sync" for p in progs.values() for op, _ in p)
         n_arrive = sum(op == "arrive" for p in progs.values() for op, _ in p)
         assert n_sync == n_arrive == max(0, nchunk - 1)
         for seed in range(200):
-            result, info = replay(progs, random.Random(seed))
+            result, info = replay(progs, random.Random(seed), warps)
             assert result == "ok", (nchunk, seed, result, info)

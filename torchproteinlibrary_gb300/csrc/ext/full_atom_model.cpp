@@ -552,13 +552,13 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def(
         "set_options",
         [](int64_t threads_per_cta) {
-            TORCH_CHECK(threads_per_cta == 0 || threads_per_cta == 4 || threads_per_cta == 128 ||
-                            threads_per_cta == 256 || threads_per_cta == 512,
-                        "threads_per_cta of Angles2Coords must be 0, 4, 128, 256 or 512");
+            TORCH_CHECK(threads_per_cta == 0 || threads_per_cta == 4 || threads_per_cta == 8 ||
+                            threads_per_cta == 128 || threads_per_cta == 256 || threads_per_cta == 512,
+                        "threads_per_cta of Angles2Coords must be 0, 4, 8, 128, 256 or 512");
             g_a2c_opt.threads_per_cta = (int)threads_per_cta;
         },
         "Angles2Coords float32 forward: threads per chain (0 = 256; 256 or 512 = 1 residue each; 128 = 2 each; "
-        "4 = four warps per chain, chunks of 32 residues)",
+        "4 or 8 = four or eight warps per chain, chunks of 32 residues)",
         py::arg("threads_per_cta") = 0);
     m.def("get_options", []() { return (int64_t)g_a2c_opt.threads_per_cta; }, "Angles2Coords threads per chain");
     m.def("Coords2TypedCoords_forward", &Coords2TypedCoords_forward, "Coords2TypedCoords forward (GPU)");

@@ -364,9 +364,9 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
     (void)lane;
 }
 
-// --------------------------------------------- forward, four warps per chain
-// One CTA of four warps per chain and chunks of 32 residues, one per lane; chunk k
-// belongs to warp k % 4.  Per chunk a warp loads its residues' backbone angles,
+// ------------------------------------------ forward, four or eight warps per chain
+// One CTA of NW = 4 or 8 warps per chain and chunks of 32 residues, one per lane;
+// chunk k belongs to warp k % NW.  Per chunk a warp loads its residues' angles,
 // composes each residue's three backbone joints (N -> CA -> C -> next N), scans the
 // lane transforms and the atom counts over the warp, and places every atom of its
 // residue from the lane's frame at N into a per-warp staging buffer, from which the
@@ -375,32 +375,34 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
 // the named-barrier handoff of tpl_pair.cuh, so the chunk loop has no CTA-wide
 // barrier.  Positions are built relative to the chunk's first N atom and moved to
 // it as they are staged.
-constexpr int kA2cRingWarps = 4;
 constexpr int kA2cChunk = 32;
 constexpr int kA2cStageAtoms = kA2cChunk * kMaxResAtoms;
 
+template <int NW>
 struct A2cRingSmem {
     Topology<float> topo;
     signed char lut[256];
-    float xyz[kA2cRingWarps][kA2cStageAtoms * 3];
-    uint32_t res_name[kA2cRingWarps][kA2cStageAtoms];  // present when names are written
-    uint32_t atom_name[kA2cRingWarps][kA2cStageAtoms];
+    float xyz[NW][kA2cStageAtoms * 3];
+    uint32_t res_name[NW][kA2cStageAtoms];  // present when names are written
+    uint32_t atom_name[NW][kA2cStageAtoms];
 };
-constexpr size_t kA2cRingSmemNoNames = offsetof(A2cRingSmem, res_name);
+template <int NW>
+constexpr size_t a2c_ring_smem_no_names() { return offsetof(A2cRingSmem<NW>, res_name); }
 
-template <bool NAMES>
-__global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_fwd_ring_kernel(A2cArgs<float> a, int renorm) {
+template <int NW, bool NAMES>
+__global__ void __launch_bounds__(32 * NW) a2c_fwd_ring_kernel(A2cArgs<float> a, int renorm) {
+    constexpr int NT = 32 * NW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    A2cRingSmem &sm = *reinterpret_cast<A2cRingSmem *>(smem_raw);
-    __shared__ __align__(16) float s_ring[kA2cRingWarps][16];  // chain frame (12) and first atom index
+    A2cRingSmem<NW> &sm = *reinterpret_cast<A2cRingSmem<NW> *>(smem_raw);
+    __shared__ __align__(16) float s_ring[NW][16];  // chain frame (12) and first atom index
     __shared__ int s_len, s_bad, s_total;
 
     const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     if (tid == 0) s_total = 0;  // ordered before every chunk by the barriers of chain_length
-    load_topology<float, 32 * kA2cRingWarps>(sm.topo, sm.lut);
+    load_topology<float, NT>(sm.topo, sm.lut);
     const Topology<float> &tp = sm.topo;
     const unsigned char *row = a.seq + (size_t)b * a.seq_stride;
-    const int len = chain_length<32 * kA2cRingWarps>(row, a.seq_stride, sm.lut, &s_len, &s_bad);
+    const int len = chain_length<NT>(row, a.seq_stride, sm.lut, &s_len, &s_bad);
     const bool ok = !s_bad && len <= a.L;
     if (tid == 0) {
         if (s_bad) a2c_error(a.hdr, TPL_ERR_SEQUENCE);
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_fwd_ring_kernel(A2cArg
     const int nchunk = ok ? (len + kA2cChunk - 1) / kA2cChunk : 0;
 
 #pragma unroll 1
-    for (int k = w; k < nchunk; k += kA2cRingWarps) {
+    for (int k = w; k < nchunk; k += NW) {
         const int j = k * kA2cChunk + lane;
         const bool live = j < len;
         const int ty = live ? sm.lut[row[j]] : 0;
@@ -452,18 +454,18 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_fwd_ring_kernel(A2cArg
         PairFrame F = pair_identity();  // chain frame at the chunk start
         int abase = 0;                  // first atom of the chunk
         if (k > 0) {
-            ring_wait(k);
-            F = pair_load(s_ring[k & 3]);
-            abase = __float_as_int(s_ring[k & 3][12]);
+            ring_wait<NW>(k);
+            F = pair_load(s_ring[k % NW]);
+            abase = __float_as_int(s_ring[k % NW][12]);
         }
         if (k + 1 < nchunk) {
             PairFrame Fn = compose_pair(F, tot);
             if (renorm) renormalize_pair(Fn);
             if (lane == 0) {
-                pair_store(s_ring[(k + 1) & 3], Fn);
-                s_ring[(k + 1) & 3][12] = __int_as_float(abase + cnt);
+                pair_store(s_ring[(k + 1) % NW], Fn);
+                s_ring[(k + 1) % NW][12] = __int_as_float(abase + cnt);
             }
-            ring_signal(k + 1);
+            ring_signal<NW>(k + 1);
         } else if (lane == 0) {
             s_total = abase + cnt;
         }
@@ -509,9 +511,9 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_fwd_ring_kernel(A2cArg
         if (tid == 0) a2c_error(a.hdr, TPL_ERR_ATOMS);
         total = a.maxA;
     }
-    for (int i = 3 * total + tid; i < 3 * a.maxA; i += 32 * kA2cRingWarps) out[i] = 0.f;
+    for (int i = 3 * total + tid; i < 3 * a.maxA; i += NT) out[i] = 0.f;
     if (NAMES)
-        for (int i = total + tid; i < a.maxA; i += 32 * kA2cRingWarps) rn[i] = an[i] = 0u;
+        for (int i = total + tid; i < a.maxA; i += NT) rn[i] = an[i] = 0u;
 }
 
 // ------------------------------------------------------------------ backward
@@ -782,24 +784,15 @@ __global__ void __launch_bounds__(NT) a2c_bwd_kernel(A2cArgs<T> a, int renorm, i
 // Each rotation axis is a bond of known length: u = (origin - parent origin) / d,
 // with CA as the parent of the first side-chain joint (the dummy joint has no
 // length).  So dL/dalpha = u . (S - o x G) over the joint's subtree needs only the
-// coordinates and dL/dx, and this backward never rebuilds the tree.  Per tile of NT
-// residues, last to first, the CTA stages the tile's atoms and dL/dx (plus the
-// first atom after the tile), each thread sums G and S over its residue's atoms, a
-// block suffix scan adds the later residues and the carry of later tiles, and each
-// thread visits its residue's atoms last to first:
+// coordinates and dL/dx, and this backward never rebuilds the tree.  Each lane owns
+// one residue: it sums G and S over the residue's atoms, a warp suffix scan adds the
+// later residues of its chunk and a carry the later chunks, and the lane visits its
+// residue's atoms last to first:
 //   omega_j  subtree: every later residue        axis C_j -> N_j+1, origin N_j+1
 //   psi_j    + O_j                                axis CA_j -> C_j,  origin C_j
 //   chi_k    side-chain groups k.. only           axis o_k-1 -> o_k, origin o_k
 //   phi_j    + side chain + C_j                   axis N_j -> CA_j,  origin CA_j
-// Positions are taken relative to the tile's first N atom to keep the sums small.
-template <int NT>
-struct A2cCoordsSmem {
-    Topology<float> topo;
-    float x[(NT * kMaxResAtoms + 1) * 3];
-    float g[(NT * kMaxResAtoms + 1) * 3];
-    signed char lut[256];
-};
-
+// Positions are taken relative to the chunk's first N atom to keep the sums small.
 __device__ __forceinline__ float joint_grad(const float *o, const float *p_prev, float inv_d, const float *G,
                                             const float *S) {
     float cr[3];
@@ -832,176 +825,8 @@ __device__ __forceinline__ void add_atom(const float *xs, const float *gs, const
     }
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT) a2c_bwd_coords_kernel(A2cArgs<float> a) {
-    constexpr int NW = NT / 32;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    A2cCoordsSmem<NT> &sm = *reinterpret_cast<A2cCoordsSmem<NT> *>(smem_raw);
-    __shared__ int s_len, s_bad, s_wcnt[NW];
-    __shared__ float s_wsum[NW][6];
-
-    const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    load_topology<float, NT>(sm.topo, sm.lut);
-    const Topology<float> &tp = sm.topo;
-    const unsigned char *row = a.seq + (size_t)b * a.seq_stride;
-    const int len = chain_length<NT>(row, a.seq_stride, sm.lut, &s_len, &s_bad);
-    float *gout = a.grad_angles + (size_t)b * 8 * a.L;
-    const float *xin = a.coords + (size_t)b * 3 * a.maxA;
-    const float *gin = a.grad_coords + (size_t)b * 3 * a.maxA;
-    bool ok = !s_bad && len <= a.L;
-
-    // atoms of the whole chain: the last tile ends there
-    int cnt = 0;
-    if (ok)
-        for (int j = tid; j < len; j += NT) cnt += tp.natoms[sm.lut[row[j]]];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
-    if (lane == 0) s_wcnt[w] = cnt;
-    __syncthreads();
-    int total = 0;
-#pragma unroll
-    for (int q = 0; q < NW; q++) total += s_wcnt[q];
-    if (tid == 0) {
-        if (s_bad) a2c_error(a.hdr, TPL_ERR_SEQUENCE);
-        if (len > a.L) a2c_error(a.hdr, TPL_ERR_LENGTH);
-        if (ok && total > a.maxA) a2c_error(a.hdr, TPL_ERR_ATOMS);
-    }
-    if (total > a.maxA) ok = false;
-    __syncthreads();  // s_wcnt is reused below
-
-    const int ntiles = ok ? (len + NT - 1) / NT : 0;
-    const float inv_dphi = 1.f / tp.bb_d[0], inv_dpsi = 1.f / tp.bb_d[1], inv_dom = 1.f / tp.bb_d[2];
-    float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, oc[3] = {0.f, 0.f, 0.f};  // atoms after the tile
-    int abase_next = total;
-    for (int t = ntiles - 1; t >= 0; t--) {
-        const int s0 = t * NT, n = min(NT, len - s0);
-        const int j = s0 + tid;
-        const bool live = tid < n;
-        const int ty = live ? sm.lut[row[j]] : 0;
-        const int na = live ? tp.natoms[ty] : 0;
-        // the residue's first atom inside the tile: block exclusive scan of atom counts
-        int inc = na;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, inc, off);
-            if (lane >= off) inc += v;
-        }
-        if (lane == 31) s_wcnt[w] = inc;
-        __syncthreads();
-        int wbase = 0, tcnt = 0;
-#pragma unroll
-        for (int q = 0; q < NW; q++) {
-            const int c = s_wcnt[q];
-            wbase += q < w ? c : 0;
-            tcnt += c;
-        }
-        const int aoff = wbase + inc - na;
-        const int abase = abase_next - tcnt;
-        const int nstage = 3 * (tcnt + (t + 1 < ntiles ? 1 : 0));  // + the next tile's first N
-        for (int i = tid; i < nstage; i += NT) {
-            sm.x[i] = xin[(size_t)3 * abase + i];
-            sm.g[i] = gin[(size_t)3 * abase + i];
-        }
-        __syncthreads();
-        const float o[3] = {sm.x[0], sm.x[1], sm.x[2]};
-        {  // carry to this tile's origin: S_o = S_oc + (oc - o) x G
-            const float d[3] = {oc[0] - o[0], oc[1] - o[1], oc[2] - o[2]};
-            float dx[3];
-            cross3(d, Gc, dx);
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                Sc[c] += dx[c];
-                oc[c] = o[c];
-            }
-        }
-        // residue totals, then the sums over later residues
-        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        for (int q = 0; q < na; q++) add_atom(sm.x + 3 * (aoff + q), sm.g + 3 * (aoff + q), o, v, v + 3);
-        float later[6], ttot[6];
-#pragma unroll
-        for (int i = 0; i < 6; i++) {
-            float wt;
-            later[i] = suffix_excl(v[i], lane, wt);
-            if (lane == 0) s_wsum[w][i] = wt;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < 6; i++) {
-            float after = 0.f, all = 0.f;
-#pragma unroll
-            for (int q = 0; q < NW; q++) {
-                const float s = s_wsum[q][i];
-                after += q > w ? s : 0.f;
-                all += s;
-            }
-            later[i] += after + (i < 3 ? Gc[i] : Sc[i - 3]);
-            ttot[i] = all;
-        }
-        if (live) {
-            float G[3] = {later[0], later[1], later[2]}, S[3] = {later[3], later[4], later[5]};
-            const float *X = sm.x + 3 * aoff, *Gg = sm.g + 3 * aoff;
-            float xN[3], xA[3], xC[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                xN[c] = X[c] - o[c];
-                xA[c] = X[3 + c] - o[c];
-                xC[c] = X[3 * (na - 2) + c] - o[c];
-            }
-            float gr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (j + 1 < len) {  // omega_j: the next residue's N joint
-                const float xn[3] = {X[3 * na] - o[0], X[3 * na + 1] - o[1], X[3 * na + 2] - o[2]};
-                gr[2] = joint_grad(xn, xC, inv_dom, G, S);
-            }
-            add_atom(X + 3 * (na - 1), Gg + 3 * (na - 1), o, G, S);  // O
-            gr[1] = joint_grad(xC, xA, inv_dpsi, G, S);
-            add_atom(X + 3 * (na - 2), Gg + 3 * (na - 2), o, G, S);  // C
-            // side chain, groups last to first; chi subtrees hold side-chain atoms only
-            float Gs[3] = {0.f, 0.f, 0.f}, Ss[3] = {0.f, 0.f, 0.f};
-            const int nj = tp.njoints[ty];
-            if (nj == 0) {
-                for (int q = 2; q < na - 2; q++) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);  // Pro ring (none for Gly)
-            }
-            for (int k = nj - 1; k >= 0; k--) {
-                const int f0 = 2 + tp.jfirst[ty][k], f1 = f0 + tp.jna[ty][k];
-                for (int q = f1 - 1; q >= f0; q--) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);
-                const int chi = tp.jchi[ty][k];
-                if (chi >= 0) {
-                    const float *pk = X + 3 * f0;
-                    const float *pp = k == 0 ? X + 3 : X + 3 * (2 + tp.jfirst[ty][k - 1]);
-                    const float ok_[3] = {pk[0] - o[0], pk[1] - o[1], pk[2] - o[2]};
-                    const float op_[3] = {pp[0] - o[0], pp[1] - o[1], pp[2] - o[2]};
-                    const float gk = joint_grad(ok_, op_, 1.f / tp.jd[ty][k], Gs, Ss);
-#pragma unroll
-                    for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
-                        if (chi == q) gr[3 + q] = gk;
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                G[c] += Gs[c];
-                S[c] += Ss[c];
-            }
-            gr[0] = joint_grad(xA, xN, inv_dphi, G, S);
-#pragma unroll
-            for (int k = 0; k < 8; k++) gout[(size_t)k * a.L + j] = gr[k];
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            Gc[c] += ttot[c];
-            Sc[c] += ttot[3 + c];
-        }
-        abase_next = abase;
-        __syncthreads();  // staging, s_wcnt and s_wsum are rewritten by the next tile
-    }
-    // zeros past the chain (and everywhere when the chain was rejected)
-    const int from = ok ? len : 0;
-    for (int k = 0; k < 8; k++)
-        for (int i = from + tid; i < a.L; i += NT) gout[(size_t)k * a.L + i] = 0.f;
-}
-
-// Backward from the coordinates, four warps per chain: a2c_bwd_coords_kernel's
-// per-residue evaluation on chunks of 32 residues (one per lane), chunk k on warp
-// (nchunk - 1 - k) % 4, last chunk first.  The chunks' first atom indices come from
+// The kernel: NW = 4 or 8 warps per chain on chunks of 32 residues (one per lane),
+// chunk k on warp (nchunk - 1 - k) % NW, last chunk first.  The chunks' first atom indices come from
 // one pass over the sequence at the start; per chunk a warp stages the chunk's atom
 // range of coordinates and dL/dx with coalesced loads, sums G and S over each
 // lane's residue about the chunk's first N atom, suffix-scans them over the warp
@@ -1016,19 +841,21 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
 
+template <int NW>
 struct A2cBwdRingSmem {
     Topology<float> topo;
     signed char lut[256];
-    float x[kA2cRingWarps][kA2cStageAtoms * 3];
-    float g[kA2cRingWarps][kA2cStageAtoms * 3];
+    float x[NW][kA2cStageAtoms * 3];
+    float g[NW][kA2cStageAtoms * 3];
     int base[1];  // first atom of each chunk, nchunk + 1 entries (dynamic)
 };
 
-__global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_bwd_coords_ring_kernel(A2cArgs<float> a) {
-    constexpr int NT = 32 * kA2cRingWarps;
+template <int NW>
+__global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<float> a) {
+    constexpr int NT = 32 * NW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    A2cBwdRingSmem &sm = *reinterpret_cast<A2cBwdRingSmem *>(smem_raw);
-    __shared__ __align__(16) float s_ring[kA2cRingWarps][12];
+    A2cBwdRingSmem<NW> &sm = *reinterpret_cast<A2cBwdRingSmem<NW> *>(smem_raw);
+    __shared__ __align__(16) float s_ring[NW][12];
     __shared__ int s_len, s_bad;
 
     // chains last to first: the first CTAs read the rows the forward wrote last, which may still be in L2
@@ -1044,7 +871,7 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_bwd_coords_ring_kernel
     const int nchunk = ok ? (len + kA2cChunk - 1) / kA2cChunk : 0;
 
     // atoms per chunk (warp w counts chunks w, w + 4, ...), then their exclusive prefix
-    for (int c = w; c < nchunk; c += kA2cRingWarps) {
+    for (int c = w; c < nchunk; c += NW) {
         const int j = c * kA2cChunk + lane;
         int n = j < len ? tp.natoms[sm.lut[row[j]]] : 0;
 #pragma unroll
@@ -1079,7 +906,7 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_bwd_coords_ring_kernel
     float *sx = sm.x[w], *sg = sm.g[w];
 
 #pragma unroll 1
-    for (int k = nrun - 1 - w; k >= 0; k -= kA2cRingWarps) {
+    for (int k = nrun - 1 - w; k >= 0; k -= NW) {
         const int j = k * kA2cChunk + lane;
         const bool live = j < len;
         const int ty = live ? sm.lut[row[j]] : 0;
@@ -1109,8 +936,8 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_bwd_coords_ring_kernel
         // the sums over later chunks, moved to this chunk's origin: S_o = S_on + (on - o) x G
         float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, nN[3] = {0.f, 0.f, 0.f};
         if (k + 1 < nrun) {
-            ring_wait(k);
-            const float *cin = s_ring[k & 3];
+            ring_wait<NW>(k);
+            const float *cin = s_ring[k % NW];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 Gc[c] = cin[c];
@@ -1125,7 +952,7 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_bwd_coords_ring_kernel
         }
         if (k > 0) {
             if (lane == 0) {
-                float *cout = s_ring[(k - 1) & 3];
+                float *cout = s_ring[(k - 1) % NW];
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     cout[c] = Gc[c] + ctot[c];
@@ -1133,7 +960,7 @@ __global__ void __launch_bounds__(32 * kA2cRingWarps) a2c_bwd_coords_ring_kernel
                     cout[6 + c] = o[c];
                 }
             }
-            ring_signal(k - 1);
+            ring_signal<NW>(k - 1);
         }
         if (live) {
             float G[3] = {later[0] + Gc[0], later[1] + Gc[1], later[2] + Gc[2]};
@@ -1220,23 +1047,35 @@ static int launch_a2c_bwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t s
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
-// Four warps per chain once the batch gives every SM two chains or more; below that
-// the CTA-per-chain kernels keep more warps busy (GB300, 500-residue chains: 256
-// chains 0.023 against 0.027 ms forward, 4096 chains 0.28 against 0.17 ms).
-static bool a2c_use_ring(int B) {
+// Warps per chain of the float32 kernels: eight while the batch leaves SMs short of
+// chains, four once every SM has several (GB300, forward without names, 0.099 against
+// 0.109 ms at 1024 x 1000 residues and 0.188 against 0.170 ms at 4096 x 500; with
+// names or in the backward the crossing comes at about half the batch).
+static int a2c_ring_warps(int B, int chains_per_sm) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
-    return B >= 2 * sms;
+    return B < chains_per_sm * sms ? 8 : 4;
 }
 
+template <int NW>
 static int launch_a2c_fwd_ring(const A2cArgs<float> &a, int B, int renorm, cudaStream_t st) {
     const bool names = a.res_names && a.atom_names;
-    const size_t smem = names ? sizeof(A2cRingSmem) : kA2cRingSmemNoNames;
-    auto k = names ? a2c_fwd_ring_kernel<true> : a2c_fwd_ring_kernel<false>;
+    const size_t smem = names ? sizeof(A2cRingSmem<NW>) : a2c_ring_smem_no_names<NW>();
+    auto k = names ? a2c_fwd_ring_kernel<NW, true> : a2c_fwd_ring_kernel<NW, false>;
     if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), (int)smem))
         return TPL_ERR_LAUNCH;
-    k<<<B, 32 * kA2cRingWarps, smem, st>>>(a, renorm);
+    k<<<B, 32 * NW, smem, st>>>(a, renorm);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+}
+
+template <int NW>
+static int launch_a2c_bwd_coords_ring(const A2cArgs<float> &a, int B, int L, cudaStream_t st) {
+    const size_t smem = offsetof(A2cBwdRingSmem<NW>, base) + sizeof(int) * (size_t)((L + kA2cChunk - 1) / kA2cChunk + 1);
+    auto k = a2c_bwd_coords_ring_kernel<NW>;
+    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), (int)smem))
+        return TPL_ERR_LAUNCH;
+    k<<<B, 32 * NW, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
@@ -1255,12 +1094,14 @@ int a2c_forward(bool f64, const unsigned char *seq, int seq_stride, const void *
     // threads_per_cta: 128 = 128 threads x 2 residues; 0 / 256 (default) or 512 = one
     // residue per thread
     switch (opt.threads_per_cta) {
-        case 4: return launch_a2c_fwd_ring(a, B, renorm, st);
+        case 4: return launch_a2c_fwd_ring<4>(a, B, renorm, st);
+        case 8: return launch_a2c_fwd_ring<8>(a, B, renorm, st);
         case 128: return launch_a2c_fwd<float, 2, 128>(a, B, renorm, st);
         case 256: return launch_a2c_fwd<float, 1, 256>(a, B, renorm, st);
         case 512: return launch_a2c_fwd<float, 1, 512>(a, B, renorm, st);
     }
-    return a2c_use_ring(B) ? launch_a2c_fwd_ring(a, B, renorm, st) : launch_a2c_fwd<float, 1, 256>(a, B, renorm, st);
+    return a2c_ring_warps(B, res_names && atom_names ? 4 : 8) == 8 ? launch_a2c_fwd_ring<8>(a, B, renorm, st)
+                                                                    : launch_a2c_fwd_ring<4>(a, B, renorm, st);
 }
 
 int a2c_backward(bool f64, void *grad_angles, const void *grad_coords, const unsigned char *seq, int seq_stride,
@@ -1286,20 +1127,8 @@ int a2c_backward_coords(float *grad_angles, const float *grad_coords, const floa
     if (B == 0) return TPL_OK;
     A2cArgs<float> a{seq, seq_stride, nullptr, const_cast<float *>(coords), nullptr, nullptr, grad_angles, grad_coords,
                      (WsHeader *)ws, L, maxA};
-    if (a2c_use_ring(B)) {
-        const size_t smem = offsetof(A2cBwdRingSmem, base) + sizeof(int) * (size_t)((L + kA2cChunk - 1) / kA2cChunk + 1);
-        if (!set_max_dynamic_smem(reinterpret_cast<const void *>(a2c_bwd_coords_ring_kernel), (int)smem))
-            return TPL_ERR_LAUNCH;
-        a2c_bwd_coords_ring_kernel<<<B, 32 * kA2cRingWarps, smem, st>>>(a);
-        return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
-    }
-    constexpr int NT = 256;
-    const size_t smem = sizeof(A2cCoordsSmem<NT>);
-    auto k = a2c_bwd_coords_kernel<NT>;
-    if (!set_max_dynamic_smem(reinterpret_cast<const void *>(k), (int)smem))
-        return TPL_ERR_LAUNCH;
-    k<<<B, NT, smem, st>>>(a);
-    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
+    return a2c_ring_warps(B, 4) == 8 ? launch_a2c_bwd_coords_ring<8>(a, B, L, st)
+                                     : launch_a2c_bwd_coords_ring<4>(a, B, L, st);
 }
 
 int num_atoms_host(const char *seq) {

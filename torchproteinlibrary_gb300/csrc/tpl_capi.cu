@@ -258,7 +258,7 @@ size_t tpl_a2c_workspace_bytes(int batch, int max_len, int max_atoms, const tpl_
 
 // Angles2Coords reads only threads_per_cta (0 / 4, 128, 256 or 512) and renormalize.
 static bool a2c_options_ok(const tpl_options &o) {
-    return o.threads_per_cta == 0 || o.threads_per_cta == 4 || o.threads_per_cta == 128 ||
+    return o.threads_per_cta == 0 || o.threads_per_cta == 4 || o.threads_per_cta == 8 || o.threads_per_cta == 128 ||
            o.threads_per_cta == 256 || o.threads_per_cta == 512;
 }
 

@@ -153,25 +153,37 @@ __device__ __forceinline__ void apply_joint_pair(PairFrame &f, float cb, float s
 
 // Handoff between the warps of a CTA that share one chain (chunk k on one warp,
 // chunk k + 1 on the next): the carry into chunk k passes through shared-memory slot
-// k % 4 under named barrier 1 + k % 4 with 64 threads, the producer warp arriving
-// and the consumer warp syncing.  Literal barrier ids, so that only barriers 1-4 are
-// reserved for the CTA.
+// k % NW under named barrier 1 + k % NW with 64 threads, the producer warp arriving
+// and the consumer warp syncing.  Literal barrier ids, so that only barriers 1..NW
+// (NW = 4 or 8) are reserved for the CTA.
+template <int NW = 4>
 __device__ __forceinline__ void ring_signal(int k) {
+    static_assert(NW == 4 || NW == 8, "four or eight warps per chain");
     __syncwarp();
     __threadfence_block();
-    switch (k & 3) {
+    switch (k & (NW - 1)) {
         case 0: asm volatile("bar.arrive 1, 64;" ::: "memory"); break;
         case 1: asm volatile("bar.arrive 2, 64;" ::: "memory"); break;
         case 2: asm volatile("bar.arrive 3, 64;" ::: "memory"); break;
-        default: asm volatile("bar.arrive 4, 64;" ::: "memory"); break;
+        case 3: asm volatile("bar.arrive 4, 64;" ::: "memory"); break;
+        case 4: asm volatile("bar.arrive 5, 64;" ::: "memory"); break;
+        case 5: asm volatile("bar.arrive 6, 64;" ::: "memory"); break;
+        case 6: asm volatile("bar.arrive 7, 64;" ::: "memory"); break;
+        default: asm volatile("bar.arrive 8, 64;" ::: "memory"); break;
     }
 }
+template <int NW = 4>
 __device__ __forceinline__ void ring_wait(int k) {
-    switch (k & 3) {
+    static_assert(NW == 4 || NW == 8, "four or eight warps per chain");
+    switch (k & (NW - 1)) {
         case 0: asm volatile("bar.sync 1, 64;" ::: "memory"); break;
         case 1: asm volatile("bar.sync 2, 64;" ::: "memory"); break;
         case 2: asm volatile("bar.sync 3, 64;" ::: "memory"); break;
-        default: asm volatile("bar.sync 4, 64;" ::: "memory"); break;
+        case 3: asm volatile("bar.sync 4, 64;" ::: "memory"); break;
+        case 4: asm volatile("bar.sync 5, 64;" ::: "memory"); break;
+        case 5: asm volatile("bar.sync 6, 64;" ::: "memory"); break;
+        case 6: asm volatile("bar.sync 7, 64;" ::: "memory"); break;
+        default: asm volatile("bar.sync 8, 64;" ::: "memory"); break;
     }
 }
 
