@@ -281,7 +281,7 @@ def run_ours(args):
     value = residues / (ms / 1e3)
 
     if args.no_extras:
-        check = plain = e2e = e2e_io = a2c = train = transform = ragged = typed = None
+        check = plain = e2e = e2e_io = a2c = a2c_large = train = transform = ragged = typed = None
     else:
         # correctness of this very run against the FP64 plain form on a slice
         check = accuracy_vs_fp64(rm, ang, lengths, up, coords, gang, dev)
@@ -295,6 +295,7 @@ def run_ours(args):
         # the layer's full I/O through the host link as well: upstream gradient in, coordinates out
         e2e_io = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
         a2c = time_a2c(dev)
+        a2c_large = time_a2c_large(dev)
         train = time_training_step(dev)
         ragged = time_ragged(dev)
         transform = time_coords_transform(dev)
@@ -350,6 +351,7 @@ def run_ours(args):
         "e2e_layer_io": e2e_io,
         "plain_fp64": plain,
         "angles2coords": a2c,
+        "angles2coords_large": a2c_large,
         "training_step": train,
         "ragged_batch": ragged,
         "typed_coords": typed,
@@ -717,6 +719,92 @@ def time_a2c(dev, steps=10, seed=1004):
     return res
 
 
+def time_a2c_large(dev, steps=10, seed=1005):
+    """Angles2Coords FP32 throughput at scale: 4096 chains of 500 random residues
+    (uniform over the 20 letters), inputs resident, the automatic kernel choice.
+    Algorithmic bytes per residue follow the layer's I/O: forward = angles (32 B) +
+    sequence (1 B) + coordinates (12 B per atom), names add 8 B per atom; backward =
+    angles + sequence + dL/dx (12 B per atom) + dL/dangles (32 B).  The backward from
+    the coordinates reads the coordinates in place of the angles (moved bytes)."""
+    import torch
+    from torchproteinlibrary_gb300 import load_extension
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+
+    fm = load_extension("_FullAtomModel")
+    fm.set_options(0)
+    peak_gbs, _ = peaks()
+    g = np.random.default_rng(seed)
+    B, L = 4096, 500
+    aa = np.array(list("ACDEFGHIKLMNPQRSTVWY"))
+    seqs = ["".join(row) for row in g.choice(aa, (B, L))]
+    ang = torch.from_numpy(g.uniform(-np.pi, np.pi, (B, 8, L)).astype(np.float32)).to(dev)
+    seq = convertStringList(seqs).to(dev)
+    na = [fm.getSeqNumAtoms(x) for x in seqs]
+    maxA, atoms, res = max(na), float(sum(na)), float(B * L)
+    c = torch.empty(B, 3 * maxA, device=dev)
+    rn = torch.empty(B, maxA, 4, dtype=torch.uint8, device=dev)
+    an = torch.empty_like(rn)
+    e0 = torch.empty(0, dtype=torch.uint8, device=dev)
+    gup = torch.from_numpy(g.standard_normal((B, 3 * maxA)).astype(np.float32)).to(dev)
+    ga = torch.empty_like(ang)
+    legs = {"fwd": lambda: fm.Angles2Coords_forward(seq, ang, c, e0, e0),
+            "fwd_names": lambda: fm.Angles2Coords_forward(seq, ang, c, rn, an),
+            "bwd": lambda: fm.Angles2Coords_backward_coords(gup, ga, seq, c)}
+    ms = {}
+    for name, f in legs.items():
+        for _ in range(3):
+            f()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        e[0].record()
+        for _ in range(steps):
+            f()
+        e[1].record()
+        torch.cuda.synchronize(dev)
+        ms[name] = e[0].elapsed_time(e[1]) / steps
+    fwd_b, names_b = 33 * res + 12 * atoms, 33 * res + 20 * atoms
+    bwd_b, bwd_moved = 65 * res + 12 * atoms, 65 * res + 24 * atoms - 32 * res
+    gbs = lambda nbytes, t: nbytes / (t / 1e3) / 1e9
+    return {"workload": f"Angles2Coords FP32, {B} chains x {L} random residues ({atoms / res:.2f} atoms per residue)",
+            "fwd_ms": ms["fwd"], "fwd_names_ms": ms["fwd_names"], "bwd_ms": ms["bwd"],
+            "residues_per_s": res / ((ms["fwd"] + ms["bwd"]) / 1e3),
+            "roofline": {"unit": "GB/s of algorithmic bytes", "peak": peak_gbs,
+                         "forward": {"achieved": gbs(fwd_b, ms["fwd"]), "frac": gbs(fwd_b, ms["fwd"]) / peak_gbs},
+                         "forward_names": {"achieved": gbs(names_b, ms["fwd_names"]),
+                                           "frac": gbs(names_b, ms["fwd_names"]) / peak_gbs},
+                         "backward": {"achieved": gbs(bwd_b, ms["bwd"]), "frac": gbs(bwd_b, ms["bwd"]) / peak_gbs,
+                                      "moved_frac": gbs(bwd_moved, ms["bwd"]) / peak_gbs}},
+            "kernels": "a2c_fwd_ring_kernel / a2c_bwd_coords_ring_kernel, four warps per chain"}
+
+
+def a2c_profile_case(dev, B=1024, L=500, seed=5):
+    """One Angles2Coords FP32 forward without names, one with names and one backward
+    from the coordinates on 1024 random chains of 500 residues (numpy seed 5, angles
+    U[-pi, pi)), the automatic kernel choice: a small case for ncu captures."""
+    import torch
+    from torchproteinlibrary_gb300 import load_extension
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+
+    fm = load_extension("_FullAtomModel")
+    fm.set_options(0)
+    g = np.random.default_rng(seed)
+    aa = np.array(list("ACDEFGHIKLMNPQRSTVWY"))
+    seqs = ["".join(g.choice(aa, L)) for _ in range(B)]
+    ang = torch.from_numpy(g.uniform(-np.pi, np.pi, (B, 8, L)).astype(np.float32)).to(dev)
+    seq = convertStringList(seqs).to(dev)
+    maxA = max(fm.getSeqNumAtoms(x) for x in seqs)
+    c = torch.empty(B, 3 * maxA, device=dev)
+    rn = torch.empty(B, maxA, 4, dtype=torch.uint8, device=dev)
+    an = torch.empty_like(rn)
+    e0 = torch.empty(0, dtype=torch.uint8, device=dev)
+    gup = torch.randn(B, 3 * maxA, device=dev)
+    ga = torch.empty_like(ang)
+    fm.Angles2Coords_forward(seq, ang, c, e0, e0)
+    fm.Angles2Coords_forward(seq, ang, c, rn, an)
+    fm.Angles2Coords_backward_coords(gup, ga, seq, c)
+    torch.cuda.synchronize(dev)
+    return {"chains": B, "residues": L, "max_atoms": maxA}
+
+
 def time_training_step(dev, steps=10, seed=1004):
     """The training step on its own workload: 256 chains of U{50..500} random
     residues, angles ~ U[-pi, pi) with omega = pi, target = Angles2Coords(angles +
@@ -1018,7 +1106,8 @@ def main():
     ap.add_argument("--bwd-cta", type=int, default=0, help="coordinate backward: 0 = automatic, 32 = one warp per chain, 4 = one CTA of four warps per chain (with --rpt)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-FP64, end-to-end and CPU-baseline legs (profiling)")
-    ap.add_argument("--leg", default=None, choices=["a2c", "training_step", "coords_transform", "ragged_batch", "e2e", "typed_coords"],
+    ap.add_argument("--leg", default=None, choices=["a2c", "a2c_large", "a2c_profile", "training_step", "coords_transform", "ragged_batch", "e2e",
+                             "typed_coords"],
                     help="run one secondary leg alone and print its result (profiling); no metric line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "ours" else args.warmup
@@ -1032,7 +1121,7 @@ def main():
                     "e2e_eager": time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10, graph=False),
                     "e2e_layer_io": time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=10)}
 
-        fn = {"a2c": time_a2c, "training_step": time_training_step, "coords_transform": time_coords_transform,
+        fn = {"a2c": time_a2c, "a2c_large": time_a2c_large, "a2c_profile": a2c_profile_case, "training_step": time_training_step, "coords_transform": time_coords_transform,
               "ragged_batch": time_ragged, "e2e": e2e_leg, "typed_coords": time_typed_coords}[args.leg]
         print(json.dumps({"leg": args.leg, "result": fn(dev)}, default=float))
         return
