@@ -706,8 +706,9 @@ def time_a2c(dev, steps=10, seed=1004):
         fms, bms = e[0].elapsed_time(e[1]) / n, e[1].elapsed_time(e[2]) / n
         res[name] = {"residues_per_s": float(lens.sum()) / ((fms + bms) / 1e3), "fwd_ms": fms, "bwd_ms": bms}
         if name == "f32":
-            res[name]["bwd_tree_ms"] = e[2].elapsed_time(e[3]) / n
-            res[name]["bwd"] = "from the forward's coordinates (the layer's float32 backward)"
+            res[name]["bwd_reference_signature_ms"] = e[2].elapsed_time(e[3]) / n
+            res[name]["bwd"] = ("from the forward's coordinates (the layer's float32 backward); the reference-signature "
+                                "Angles2Coords_backward recomputes the coordinates first")
         outs[name] = (c.double(), ga.double(), gup)
     d = (outs["f32"][0] - outs["f64"][0]).view(B, -1, 3).norm(dim=-1)
     ge = (outs["f32"][1] - outs["f64"][1]).abs().max() / outs["f64"][1].abs().max()

@@ -72,10 +72,14 @@ def test_golden_fp64(fm):
     check(c, gi, d["coords"], d["grad_angles"], na, COORD_TOL_F64, GRAD_TOL_F64)
 
 
-@pytest.mark.parametrize("dtype,threads", [(torch.float32, 0), (torch.float32, 4), (torch.float32, 8),
-                                           (torch.float32, 128), (torch.float32, 256), (torch.float32, 512),
-                                           (torch.float64, 0)])
-def test_random_batch_matches_oracle(fm, dtype, threads):
+@pytest.mark.parametrize("dtype,threads,tree", [(torch.float32, 0, False), (torch.float32, 0, True),
+                                                (torch.float32, 4, False), (torch.float32, 8, False),
+                                                (torch.float32, 128, True), (torch.float32, 256, True),
+                                                (torch.float32, 512, True), (torch.float64, 0, False)])
+def test_random_batch_matches_oracle(fm, dtype, threads, tree):
+    """Forward and the reference-signature backward against the oracle.  float32:
+    Angles2Coords_backward recomputes the coordinates and runs the backward from them,
+    or (tree = True) rebuilds the tree per joint; float64 always rebuilds it."""
     rng = np.random.default_rng(31)
     seqs = ["".join(rng.choice(list(AA), rng.integers(1, 300))) for _ in range(7)] + ["G", "P", "W", AA]
     L = 300
@@ -93,10 +97,12 @@ def test_random_batch_matches_oracle(fm, dtype, threads):
         a_ref = ang
     rg = oracle.a2c_backward(g, a_ref, seqs)
     fm.set_options(threads)
+    fm.set_backward_tree(tree)
     try:
         c, rn, an, na2, gi = run_gpu(fm, ang, seqs, g, dtype)
     finally:
         fm.set_options(0)
+        fm.set_backward_tree(False)
     np.testing.assert_array_equal(rn, rrn)
     np.testing.assert_array_equal(an, ran)
     tol = (COORD_TOL_F32, GRAD_TOL_F32) if dtype == torch.float32 else (COORD_TOL_F64, GRAD_TOL_F64)
@@ -222,6 +228,16 @@ def test_unknown_letter_and_overflow_reported(fm):
     out = torch.zeros(1, 3 * 20, device=dev)
     fm.Angles2Coords_forward(seq, torch.zeros(1, 8, 3, device=dev), out, e, e)
     assert fm.workspace_status(0) == -4
+    # the backward from the coordinates rejects the same chains, with zero gradients
+    for seqs, L, slots, status in ((["GAXG", "GG"], 4, 8, -5), (["WWW"], 3, 20, -7), (["GGGGG"], 3, 20, -4)):
+        seq = convertStringList(seqs).to(dev)
+        ga = torch.full((len(seqs), 8, L), float("nan"), device=dev)
+        fm.Angles2Coords_backward_coords(torch.ones(len(seqs), 3 * slots, device=dev), ga, seq,
+                                         torch.randn(len(seqs), 3 * slots, device=dev))
+        assert fm.workspace_status(0) == status
+        assert torch.all(ga[0] == 0)
+        if len(seqs) > 1:
+            assert torch.isfinite(ga[1]).all() and torch.any(ga[1] != 0)
 
 
 def test_layer_api_and_gradcheck(built):
@@ -346,8 +362,10 @@ def test_four_warp_kernels_at_batch_size(fm):
 
 def test_backward_from_coordinates_c_abi_and_layer(fm, built):
     """Through the C ABI (status-word workspace only), bit-identical to the
-    extension entry; and the float32 autograd layer's gradient (from coordinates)
-    against the tree-rebuilding backward selected by backward_from_coords = False."""
+    extension entry; and the float32 autograd layer's gradient (from its saved
+    coordinates) against the reference-signature backward selected by
+    backward_from_coords = False, which recomputes the same coordinates (identical
+    gradient) or, with set_backward_tree(True), rebuilds the tree per joint."""
     import ctypes
     from torchproteinlibrary_gb300 import capi
     from torchproteinlibrary_gb300.FullAtomModel import Angles2Coords
@@ -372,15 +390,18 @@ def test_backward_from_coordinates_c_abi_and_layer(fm, built):
     np.testing.assert_array_equal(out.double().cpu().numpy(), gi)
     layer = Angles2Coords()
     grads = {}
-    for flag in (True, False):
+    for flag, tree in ((True, False), (False, False), (False, True)):
         Angles2CoordsFunction.backward_from_coords = flag
+        fm.set_backward_tree(tree)
         try:
             x = torch.tensor(ang, dtype=torch.float32, device=dev, requires_grad=True)
             coords = layer(x, seqs)[0]
             coords.backward(gt)
-            grads[flag] = x.grad.double().cpu().numpy()
+            grads[flag, tree] = x.grad.double().cpu().numpy()
         finally:
             Angles2CoordsFunction.backward_from_coords = True
-    scale = max(1.0, np.abs(grads[False]).max())
-    assert np.abs(grads[True] - grads[False]).max() <= GRAD_TOL_F32 * scale
-    np.testing.assert_array_equal(grads[True], gi)
+            fm.set_backward_tree(False)
+    np.testing.assert_array_equal(grads[True, False], gi)
+    np.testing.assert_array_equal(grads[False, False], gi)
+    scale = max(1.0, np.abs(grads[False, True]).max())
+    assert np.abs(grads[True, False] - grads[False, True]).max() <= GRAD_TOL_F32 * scale

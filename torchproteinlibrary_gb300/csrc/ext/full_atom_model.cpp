@@ -28,8 +28,9 @@
 
 namespace {
 
-// Tuning knobs of the Angles2Coords kernels (threads_per_cta 0 / 256, 512 or 128).
+// Tuning knobs of the Angles2Coords kernels (threads_per_cta 0, 4, 8, 128, 256 or 512).
 tpl_options g_a2c_opt = {};
+bool g_a2c_tree_backward = false;  // float32 Angles2Coords_backward: rebuild the tree per joint
 
 void check_status(int s, const char *what) {
     TORCH_CHECK(s == TPL_OK, what, ": ", tpl_status_string(s), " (", s, ")");
@@ -122,7 +123,18 @@ void Angles2Coords_backward(torch::Tensor grad_atoms, torch::Tensor grad_angles,
     auto ws = status_ws(input_angles.device());
     void *st = stream_of(input_angles);
     int s;
-    if (input_angles.scalar_type() == torch::kFloat) {
+    if (input_angles.scalar_type() == torch::kFloat && !g_a2c_tree_backward) {
+        // the chunked forward into a temporary, then the backward from those coordinates:
+        // 2.2x faster than rebuilding the tree per joint at 4096 x 500 residues
+        auto coords = torch::empty({B, 3 * maxA}, input_angles.options());
+        s = tpl_a2c_forward_f32(seq.data_ptr<uint8_t>(), (int)seq.size(1), input_angles.data_ptr<float>(),
+                                coords.data_ptr<float>(), nullptr, nullptr, ws.data_ptr(), ws.nbytes(), (int)B, (int)L,
+                                (int)maxA, &g_a2c_opt, st);
+        if (s == TPL_OK)
+            s = tpl_a2c_backward_coords_f32(grad_angles.data_ptr<float>(), grad_atoms.data_ptr<float>(),
+                                            coords.data_ptr<float>(), seq.data_ptr<uint8_t>(), (int)seq.size(1),
+                                            ws.data_ptr(), ws.nbytes(), (int)B, (int)L, (int)maxA, st);
+    } else if (input_angles.scalar_type() == torch::kFloat) {
         s = tpl_a2c_backward_f32(grad_angles.data_ptr<float>(), grad_atoms.data_ptr<float>(), seq.data_ptr<uint8_t>(),
                                  (int)seq.size(1), input_angles.data_ptr<float>(), ws.data_ptr(), ws.nbytes(), (int)B,
                                  (int)L, (int)maxA, &g_a2c_opt, st);
@@ -561,6 +573,11 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         "4 or 8 = four or eight warps per chain, chunks of 32 residues)",
         py::arg("threads_per_cta") = 0);
     m.def("get_options", []() { return (int64_t)g_a2c_opt.threads_per_cta; }, "Angles2Coords threads per chain");
+    m.def(
+        "set_backward_tree", [](bool tree) { g_a2c_tree_backward = tree; },
+        "float32 Angles2Coords_backward: false (default) = forward into a temporary, then the backward from "
+        "those coordinates; true = rebuild the tree per joint (tpl_a2c_backward_f32)",
+        py::arg("tree") = false);
     m.def("Coords2TypedCoords_forward", &Coords2TypedCoords_forward, "Coords2TypedCoords forward (GPU)");
     m.def("Coords2TypedCoords_backward", &Coords2TypedCoords_backward, "Coords2TypedCoords backward (GPU)");
     m.def("Angles2Coords_forward", &Angles2Coords_forward, "Angles2Coords forward");
