@@ -180,6 +180,14 @@ __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coord
     // stable scatter, one tile of kTypedThreads atoms at a time
     for (int j0 = 0; j0 < n; j0 += kTypedThreads) {
         const int j = j0 + tid;
+        // the atom's coordinates, loaded before the ranking so that the load overlaps it
+        T x0 = T(0), x1 = T(0), x2 = T(0);
+        if (j < n) {
+            const T *src = coords + 3 * (row + j);
+            x0 = src[0];
+            x1 = src[1];
+            x2 = src[2];
+        }
         const int t = j < n ? (CACHE ? (int)s_ty[j] : atom_type(res_names[row + j], atom_names[row + j])) : -1;
         int rank = 0;
         const unsigned below = (1u << lane) - 1u;
@@ -194,11 +202,10 @@ __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coord
             int before = s_base[t];
             for (int v = 0; v < w; v++) before += s_wc[t][v];
             const int slot = s_off[t] + before + rank;
-            const T *src = coords + 3 * (row + j);
             T *dst = out + 3 * (orow + slot);
-            dst[0] = src[0];
-            dst[1] = src[1];
-            dst[2] = src[2];
+            dst[0] = x0;
+            dst[1] = x1;
+            dst[2] = x2;
             atom_index[orow + slot] = j;
         }
         __syncthreads();
@@ -242,8 +249,10 @@ __global__ void __launch_bounds__(kTypedThreads) typed_bwd_kernel(const T *grad_
 // first inverted into shared memory (in_stride ints), then grad_flat[j] is gathered
 // from grad_typed[slot(j)] with coalesced stores (zero for atoms without a slot).
 template <typename T>
-__global__ void __launch_bounds__(kTypedThreads) typed_bwd_gather_kernel(const T *grad_typed, T *grad_flat,
-                                                                         const int *n_of_type, const int *atom_index,
+__global__ void __launch_bounds__(kTypedThreads) typed_bwd_gather_kernel(const T *__restrict__ grad_typed,
+                                                                         T *__restrict__ grad_flat,
+                                                                         const int *__restrict__ n_of_type,
+                                                                         const int *__restrict__ atom_index,
                                                                          int in_stride, int out_stride) {
     extern __shared__ int s_slot[];
     const int b = blockIdx.x, tid = threadIdx.x;
@@ -260,10 +269,27 @@ __global__ void __launch_bounds__(kTypedThreads) typed_bwd_gather_kernel(const T
     __syncthreads();
     const T *src = grad_typed + 3 * orow;
     T *dst = grad_flat + 3 * row;
-    for (int e = tid; e < 3 * in_stride; e += kTypedThreads) {
-        const int j = e / 3, c = e - 3 * j;
-        const int s = s_slot[j];
-        dst[e] = s >= 0 ? src[3 * s + c] : T(0);
+    // eight gathers per thread in flight before their stores (GB300, 4096 chains of
+    // 2300 atoms: 0.086 / 0.074 / 0.070 / 0.075 ms with 2 / 4 / 8 / 16)
+    constexpr int U = 8;
+    const int ne = 3 * in_stride;
+    for (int e0 = tid; e0 < ne; e0 += U * kTypedThreads) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int e = e0 + u * kTypedThreads;
+            v[u] = T(0);
+            if (e < ne) {
+                const int j = e / 3, c = e - 3 * j;
+                const int s = s_slot[j];
+                if (s >= 0) v[u] = src[3 * s + c];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int e = e0 + u * kTypedThreads;
+            if (e < ne) dst[e] = v[u];
+        }
     }
 }
 
