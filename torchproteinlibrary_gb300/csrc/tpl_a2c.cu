@@ -250,6 +250,82 @@ __device__ __forceinline__ void residue_atoms(const Topology<T> &tp, int ty, Fra
     apply_joint(P, tp.bb_cb[2], tp.bb_sb[2], tp.bb_d[2], cs[2], sn[2]);
 }
 
+// apply_rx and frame_point (tpl_common.cuh) on a PairFrame: the same chain of fused
+// multiply-adds per output, so the same rounding.
+__device__ __forceinline__ void apply_rx_pair(PairFrame &f, float ca, float sa) {
+    const float2 c1 = f.c[1], c2 = f.c[2];
+    f.c[1] = __ffma2_rn(c1, f2(ca), __fmul2_rn(c2, f2(sa)));
+    f.c[2] = __ffma2_rn(c2, f2(ca), __fmul2_rn(c1, f2(-sa)));
+    const float e1 = f.r2[1], e2 = f.r2[2];
+    f.r2[1] = fmaf(e1, ca, e2 * sa);
+    f.r2[2] = fmaf(e2, ca, -e1 * sa);
+}
+
+__device__ __forceinline__ void pair_point(const PairFrame &P, float x, float y, float z, float *out) {
+    const float2 xy = __ffma2_rn(P.c[0], f2(x), __ffma2_rn(P.c[1], f2(y), __ffma2_rn(P.c[2], f2(z), P.p)));
+    out[0] = xy.x;
+    out[1] = xy.y;
+    out[2] = fmaf(P.r2[0], x, fmaf(P.r2[1], y, fmaf(P.r2[2], z, P.p2)));
+}
+
+// residue_atoms for float32 on paired frames, with the chi angles' cos and sin
+// computed beforehand (chi_c[q], chi_s[q] for chi_(q+1)): the same atoms in the
+// same slots, without the frame at the next N.
+template <typename Emit>
+__device__ __forceinline__ void residue_atoms_pair(const Topology<float> &tp, int ty, const PairFrame &P,
+                                                   const float cs[2], const float sn[2], const float chi_c[5],
+                                                   const float chi_s[5], Emit emit) {
+    {
+        const float x[3] = {P.p.x, P.p.y, P.p2};
+        emit(0, x);
+    }
+    PairFrame F = P;
+    apply_joint_pair(F, tp.bb_cb[0], tp.bb_sb[0], tp.bb_d[0], cs[0], sn[0]);
+    {
+        const float x[3] = {F.p.x, F.p.y, F.p2};
+        emit(1, x);
+    }
+    const int na = tp.natoms[ty];
+    if (tp.pro[ty]) {
+        for (int a = 0; a < 3; a++) {
+            float x[3];
+            pair_point(F, tp.pro_local[a][0], tp.pro_local[a][1], tp.pro_local[a][2], x);
+            emit(2 + a, x);
+        }
+    }
+    const int nj = tp.njoints[ty];
+    if (nj > 0) {
+        PairFrame S = F;
+        apply_rx_pair(S, tp.dummy_c, tp.dummy_s);
+        for (int k = 0; k < nj; k++) {
+            const int chi = tp.jchi[ty][k];
+            float c = 1.f, s = 0.f;
+#pragma unroll
+            for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
+                if (chi == q) {
+                    c = chi_c[q];
+                    s = chi_s[q];
+                }
+            apply_joint_pair(S, tp.jcb[ty][k], tp.jsb[ty][k], tp.jd[ty][k], c, s);
+            const int f0 = tp.jfirst[ty][k];
+            for (int a = 0; a < tp.jna[ty][k]; a++) {
+                float x[3];
+                pair_point(S, tp.sc[ty][f0 + a][0], tp.sc[ty][f0 + a][1], tp.sc[ty][f0 + a][2], x);
+                emit(2 + f0 + a, x);
+            }
+        }
+    }
+    PairFrame C = F;
+    apply_joint_pair(C, tp.bb_cb[1], tp.bb_sb[1], tp.bb_d[1], cs[1], sn[1]);
+    {
+        const float x[3] = {C.p.x, C.p.y, C.p2};
+        emit(na - 2, x);
+    }
+    float x[3];
+    pair_point(C, tp.o_local[0], tp.o_local[1], tp.o_local[2], x);
+    emit(na - 1, x);
+}
+
 // Copy n staged values (world coordinates, xyz interleaved) to dst, coalesced.
 template <typename T, int NT>
 __device__ __forceinline__ void store_tile_atoms(T *dst, const T *src, int n) {
@@ -390,7 +466,7 @@ template <int NW>
 constexpr size_t a2c_ring_smem_no_names() { return offsetof(A2cRingSmem<NW>, res_name); }
 
 template <int NW, bool NAMES>
-__global__ void __launch_bounds__(32 * NW) a2c_fwd_ring_kernel(A2cArgs<float> a, int renorm) {
+__global__ void __launch_bounds__(32 * NW, NW == 4 ? 6 : 3) a2c_fwd_ring_kernel(A2cArgs<float> a, int renorm) {
     constexpr int NT = 32 * NW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     A2cRingSmem<NW> &sm = *reinterpret_cast<A2cRingSmem<NW> *>(smem_raw);
@@ -422,21 +498,32 @@ __global__ void __launch_bounds__(32 * NW) a2c_fwd_ring_kernel(A2cArgs<float> a,
         const int ty = live ? sm.lut[row[j]] : 0;
         const int na = live ? tp.natoms[ty] : 0;
         // backbone angles; omega of the chain's last residue moves no atom
+        // cos and sin of the eight angles, in pairs and for every lane at once (the chi
+        // angles' outside the divergent side-chain walk); omega of the chain's last
+        // residue moves no atom
         float cs[3] = {1.f, 1.f, 1.f}, sn[3] = {0.f, 0.f, 0.f};
-        float chi[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // loaded with the backbone angles: one latency per chunk
+        float chc[5] = {1.f, 1.f, 1.f, 1.f, 1.f}, chs[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
         PairFrame t = pair_identity();
         if (live) {
             const float phi = ang[j], psi = ang[a.L + j];
             const float om = j + 1 < len ? ang[2 * a.L + j] : 0.f;
+            float chi[5];
 #pragma unroll
             for (int q = 0; q < 5; q++) chi[q] = ang[(size_t)(3 + q) * a.L + j];
-            if (fmaxf(fabsf(phi), fmaxf(fabsf(psi), fabsf(om))) <= 1.0e4f) {
+            float m = fmaxf(fabsf(phi), fmaxf(fabsf(psi), fabsf(om)));
+#pragma unroll
+            for (int q = 0; q < 5; q++) m = fmaxf(m, fabsf(chi[q]));
+            if (m <= 1.0e4f) {  // NaN passes: sincos_fast2 returns NaN for it
                 sincos_fast2(phi, psi, &sn[0], &cs[0], &sn[1], &cs[1]);
-                sincos_fast(om, &sn[2], &cs[2]);
+                sincos_fast2(om, chi[0], &sn[2], &cs[2], &chs[0], &chc[0]);
+                sincos_fast2(chi[1], chi[2], &chs[1], &chc[1], &chs[2], &chc[2]);
+                sincos_fast2(chi[3], chi[4], &chs[3], &chc[3], &chs[4], &chc[4]);
             } else {
                 sincos_poly(phi, &sn[0], &cs[0]);
                 sincos_poly(psi, &sn[1], &cs[1]);
                 sincos_poly(om, &sn[2], &cs[2]);
+#pragma unroll
+                for (int q = 0; q < 5; q++) sincos_poly(chi[q], &chs[q], &chc[q]);
             }
 #pragma unroll
             for (int q = 0; q < 3; q++) apply_joint_pair(t, tp.bb_cb[q], tp.bb_sb[q], tp.bb_d[q], cs[q], sn[q]);
@@ -475,16 +562,9 @@ __global__ void __launch_bounds__(32 * NW) a2c_fwd_ring_kernel(A2cArgs<float> a,
         Fr.p = make_float2(0.f, 0.f);
         Fr.p2 = 0.f;
         if (live) {
-            Frame<float> P;
-            from_pair(compose_pair(Fr, E), P);
+            const PairFrame P = compose_pair(Fr, E);
             float *dst = stage + 3 * aoff;
-            const auto chi_angle = [&](int q) {  // register selects: a dynamic index would go to local memory
-                float v = chi[0];
-#pragma unroll
-                for (int i = 1; i < 5; i++) v = q == i ? chi[i] : v;
-                return v;
-            };
-            residue_atoms<float>(tp, ty, P, cs, sn, chi_angle, [&](int slot, const float *x) {
+            residue_atoms_pair(tp, ty, P, cs, sn, chc, chs, [&](int slot, const float *x) {
                 dst[3 * slot] = x[0] + org[0];
                 dst[3 * slot + 1] = x[1] + org[1];
                 dst[3 * slot + 2] = x[2] + org[2];
