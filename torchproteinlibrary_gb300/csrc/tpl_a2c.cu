@@ -1008,8 +1008,55 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
         cp_async_wait_all();
         __syncwarp();
         const float o[3] = {sx[0], sx[1], sx[2]};  // chunk origin: its first N atom
+        // One walk over the residue's atoms, last to first, from G = S = 0.  Every
+        // joint gradient u . (S - o x G) is linear in (G, S), so each joint's share of
+        // its own residue is taken here and the share of the later residues is added
+        // after the scan: complete for the chi joints (side-chain atoms only), and
+        // the own parts of psi and phi.  The walk ends with the residue's totals.
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        for (int q = 0; q < na; q++) add_atom(sx + 3 * (aoff + q), sg + 3 * (aoff + q), o, v, v + 3);
+        float gr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float xN[3] = {0.f, 0.f, 0.f}, xA[3] = {0.f, 0.f, 0.f}, xC[3] = {0.f, 0.f, 0.f};
+        if (live) {
+            const float *X = sx + 3 * aoff, *Gg = sg + 3 * aoff;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                xN[c] = X[c] - o[c];
+                xA[c] = X[3 + c] - o[c];
+                xC[c] = X[3 * (na - 2) + c] - o[c];
+            }
+            float *G = v, *S = v + 3;
+            add_atom(X + 3 * (na - 1), Gg + 3 * (na - 1), o, G, S);  // O
+            gr[1] = joint_grad(xC, xA, inv_dpsi, G, S);
+            add_atom(X + 3 * (na - 2), Gg + 3 * (na - 2), o, G, S);  // C
+            // side chain, groups last to first; chi subtrees hold side-chain atoms only
+            float Gs[3] = {0.f, 0.f, 0.f}, Ss[3] = {0.f, 0.f, 0.f};
+            const int nj = tp.njoints[ty];
+            if (nj == 0)
+                for (int q = 2; q < na - 2; q++) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);  // Pro ring (none for Gly)
+            for (int kk = nj - 1; kk >= 0; kk--) {
+                const int f0 = 2 + tp.jfirst[ty][kk], f1 = f0 + tp.jna[ty][kk];
+                for (int q = f1 - 1; q >= f0; q--) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);
+                const int chi = tp.jchi[ty][kk];
+                if (chi >= 0) {
+                    const float *pk = X + 3 * f0;
+                    const float *pp = kk == 0 ? X + 3 : X + 3 * (2 + tp.jfirst[ty][kk - 1]);
+                    const float ok_[3] = {pk[0] - o[0], pk[1] - o[1], pk[2] - o[2]};
+                    const float op_[3] = {pp[0] - o[0], pp[1] - o[1], pp[2] - o[2]};
+                    const float gk = joint_grad(ok_, op_, 1.f / tp.jd[ty][kk], Gs, Ss);
+#pragma unroll
+                    for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
+                        if (chi == q) gr[3 + q] = gk;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                G[c] += Gs[c];
+                S[c] += Ss[c];
+            }
+            gr[0] = joint_grad(xA, xN, inv_dphi, G, S);
+            add_atom(X + 3, Gg + 3, o, G, S);  // CA
+            add_atom(X, Gg, o, G, S);          // N
+        }
         float later[6], ctot[6];
 #pragma unroll
         for (int i = 0; i < 6; i++) later[i] = suffix_excl(v[i], lane, ctot[i]);
@@ -1043,52 +1090,18 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
             ring_signal<NW>(k - 1);
         }
         if (live) {
-            float G[3] = {later[0] + Gc[0], later[1] + Gc[1], later[2] + Gc[2]};
-            float S[3] = {later[3] + Sc[0], later[4] + Sc[1], later[5] + Sc[2]};
-            const float *X = sx + 3 * aoff, *Gg = sg + 3 * aoff;
-            float xN[3], xA[3], xC[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                xN[c] = X[c] - o[c];
-                xA[c] = X[3 + c] - o[c];
-                xC[c] = X[3 * (na - 2) + c] - o[c];
-            }
-            float gr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            // the later residues' share: sums over every atom after this residue
+            const float G[3] = {later[0] + Gc[0], later[1] + Gc[1], later[2] + Gc[2]};
+            const float S[3] = {later[3] + Sc[0], later[4] + Sc[1], later[5] + Sc[2]};
             if (j + 1 < len) {  // omega_j: the next residue's N joint (the next chunk's first N after lane 31)
+                const float *X = sx + 3 * aoff;
                 float xn[3];
 #pragma unroll
                 for (int c = 0; c < 3; c++) xn[c] = (lane == 31 ? nN[c] : X[3 * na + c]) - o[c];
                 gr[2] = joint_grad(xn, xC, inv_dom, G, S);
             }
-            add_atom(X + 3 * (na - 1), Gg + 3 * (na - 1), o, G, S);  // O
-            gr[1] = joint_grad(xC, xA, inv_dpsi, G, S);
-            add_atom(X + 3 * (na - 2), Gg + 3 * (na - 2), o, G, S);  // C
-            // side chain, groups last to first; chi subtrees hold side-chain atoms only
-            float Gs[3] = {0.f, 0.f, 0.f}, Ss[3] = {0.f, 0.f, 0.f};
-            const int nj = tp.njoints[ty];
-            if (nj == 0)
-                for (int q = 2; q < na - 2; q++) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);  // Pro ring (none for Gly)
-            for (int kk = nj - 1; kk >= 0; kk--) {
-                const int f0 = 2 + tp.jfirst[ty][kk], f1 = f0 + tp.jna[ty][kk];
-                for (int q = f1 - 1; q >= f0; q--) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);
-                const int chi = tp.jchi[ty][kk];
-                if (chi >= 0) {
-                    const float *pk = X + 3 * f0;
-                    const float *pp = kk == 0 ? X + 3 : X + 3 * (2 + tp.jfirst[ty][kk - 1]);
-                    const float ok_[3] = {pk[0] - o[0], pk[1] - o[1], pk[2] - o[2]};
-                    const float op_[3] = {pp[0] - o[0], pp[1] - o[1], pp[2] - o[2]};
-                    const float gk = joint_grad(ok_, op_, 1.f / tp.jd[ty][kk], Gs, Ss);
-#pragma unroll
-                    for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
-                        if (chi == q) gr[3 + q] = gk;
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                G[c] += Gs[c];
-                S[c] += Ss[c];
-            }
-            gr[0] = joint_grad(xA, xN, inv_dphi, G, S);
+            gr[1] += joint_grad(xC, xA, inv_dpsi, G, S);
+            gr[0] += joint_grad(xA, xN, inv_dphi, G, S);
 #pragma unroll
             for (int q = 0; q < 8; q++) gout[(size_t)q * a.L + j] = gr[q];
         }
