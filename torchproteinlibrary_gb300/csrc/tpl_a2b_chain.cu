@@ -302,15 +302,27 @@ struct FwdStage {
 
 // store_chunk for the FwdStage layout: float4 q of the chunk (floats 4q..4q+3, in lane
 // segment floor(4q / SEG)) is staged at float 4q + GAP floor(q / SEG).
+__device__ __forceinline__ void st_evict_last(float4 *p, float4 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w), "l"(pol)
+                 : "memory");
+}
+
+// The coordinates are stored with an L2 evict-last hint: the layer's backward reads
+// them back (chains last to first, so the rows written last come first), and the rows
+// still in L2 save their DRAM reads (GB300, 4096 x 1000: backward 0.0601 -> 0.0580 ms
+// in the step; evict-first stores kept fewer of them).
 template <int C>
 __device__ __forceinline__ void store_chunk_fwd(float *dst, const float *stage, int n, int lane, bool vec) {
     using S = FwdStage<C>;
     constexpr int SEG = S::SEG;
     if (vec) {
+        uint64_t pol;
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
 #pragma unroll 2
         for (int q = lane; 4 * q < n; q += 32)
-            __stcs(reinterpret_cast<float4 *>(dst) + q,
-                   *reinterpret_cast<const float4 *>(stage + 4 * q + S::GAP * (q / SEG)));
+            st_evict_last(reinterpret_cast<float4 *>(dst) + q,
+                          *reinterpret_cast<const float4 *>(stage + 4 * q + S::GAP * (q / SEG)), pol);
     } else {
         for (int f = lane; f < n; f += 32) {
             const int sl = f / SEG;
