@@ -288,12 +288,12 @@ def run_ours(args):
         # plain FP64 form on the same workload (the drop-in denominator)
         plain = time_plain_fp64(rm, ang, lengths, up, dev, steps=max(1, min(3, args.steps)))
         # e2e: public autograd layer, host (pinned) inputs in, results back to the host
-        e2e = time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
+        e2e = time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, args.steps))
         e2e["eager"] = {k: v for k, v in time_e2e_train(Angles2Backbone(), ang_np, len_np, up_np, dev,
-                                                         steps=max(4, min(10, args.steps)), graph=False).items()
+                                                         steps=max(4, args.steps), graph=False).items()
                         if k in ("value", "ms_per_step", "host_issue_ms_per_step")}
         # the layer's full I/O through the host link as well: upstream gradient in, coordinates out
-        e2e_io = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, min(10, args.steps)))
+        e2e_io = time_e2e(Angles2Backbone(), ang_np, len_np, up_np, dev, steps=max(4, args.steps))
         a2c = time_a2c(dev)
         a2c_large = time_a2c_large(dev)
         train = time_training_step(dev)
