@@ -3,6 +3,12 @@
 // Layers/FullAtomModel/cConformation.cpp:30-211, OpenMP over chains in
 // Angles2Coords/angles2coords_interface.cpp:27,92).
 //
+// float32 runs the chunked kernels further down by default (a2c_fwd_ring_kernel,
+// a2c_bwd_coords_ring_kernel: four or eight warps per chain on chunks of 32
+// residues, the carry handed between warps).  The CTA kernels described here serve
+// float64, the tree-rebuilding backward and the threads_per_cta options 128, 256
+// and 512.
+//
 // One CTA per chain, looping over tiles of R*NT residues with the carry (frame
 // and atom offset) kept in shared memory.  Inside a tile the backbone is the
 // same parallel scan as Angles2Backbone (per-thread joint products, warp
