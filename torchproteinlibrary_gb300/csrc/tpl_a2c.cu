@@ -460,14 +460,40 @@ __global__ void __launch_bounds__(NT) a2c_fwd_kernel(A2cArgs<T> a, int renorm) {
 constexpr int kA2cChunk = 32;
 constexpr int kA2cStageAtoms = kA2cChunk * kMaxResAtoms;
 
+// The coordinate staging rows carry 4 words of slack: a chunk's values start at the
+// word offset of their global destination inside its 16-byte block (0..3), so that
+// whole blocks move as aligned 16-byte loads and stores (copy_span).
 template <int NW>
 struct A2cRingSmem {
     Topology<float> topo;
     signed char lut[256];
-    float xyz[NW][kA2cStageAtoms * 3];
+    alignas(16) float xyz[NW][kA2cStageAtoms * 3 + 4];
     uint32_t res_name[NW][kA2cStageAtoms];  // present when names are written
     uint32_t atom_name[NW][kA2cStageAtoms];
 };
+
+// Word offset of p inside its 16-byte block.
+__device__ __forceinline__ int block_offset(const void *p) { return (int)((reinterpret_cast<uintptr_t>(p) >> 2) & 3u); }
+
+// Copy n 4-byte words from the 16-byte-aligned staging row src (the values start at
+// src + block_offset(dst)) to dst, by the warp: every 16-byte block of dst that lies
+// whole inside [dst, dst + n) as one vector load and store, the ragged ends word by word.
+template <typename W, typename W4>
+__device__ __forceinline__ void copy_span(W *dst, const W *src, int n, int lane) {
+    const int sh = block_offset(dst);
+    W *base = dst - sh;  // 16-byte aligned; only words inside [dst, dst + n) are written
+    const int nb = (n + sh + 3) >> 2;
+    for (int b = lane; b < nb; b += 32) {
+        const int lo = 4 * b - sh;
+        if (lo >= 0 && lo + 4 <= n) {
+            *reinterpret_cast<W4 *>(base + 4 * b) = *reinterpret_cast<const W4 *>(src + 4 * b);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+                if (lo + e >= 0 && lo + e < n) dst[lo + e] = src[sh + lo + e];
+        }
+    }
+}
 template <int NW>
 constexpr size_t a2c_ring_smem_no_names() { return offsetof(A2cRingSmem<NW>, res_name); }
 
@@ -567,9 +593,11 @@ __global__ void __launch_bounds__(32 * NW, NW == 4 ? 6 : 3) a2c_fwd_ring_kernel(
         PairFrame Fr = F;  // rotation only: positions relative to the chunk origin
         Fr.p = make_float2(0.f, 0.f);
         Fr.p2 = 0.f;
+        float *gdst = out + (size_t)3 * abase;
+        float *stg = stage + block_offset(gdst);  // the chunk's values keep their global 16-byte phase
         if (live) {
             const PairFrame P = compose_pair(Fr, E);
-            float *dst = stage + 3 * aoff;
+            float *dst = stg + 3 * aoff;
             residue_atoms_pair(tp, ty, P, cs, sn, chc, chs, [&](int slot, const float *x) {
                 dst[3 * slot] = x[0] + org[0];
                 dst[3 * slot + 1] = x[1] + org[1];
@@ -583,8 +611,8 @@ __global__ void __launch_bounds__(32 * NW, NW == 4 ? 6 : 3) a2c_fwd_ring_kernel(
         }
         __syncwarp();
         const int nstore = max(0, min(cnt, a.maxA - abase));
-        for (int i = lane; i < 3 * nstore; i += 32) out[(size_t)3 * abase + i] = stage[i];
-        if (NAMES)
+        copy_span<float, float4>(gdst, stage, 3 * nstore, lane);
+        if (NAMES)  // word stores: the names' own block phase would hold two more pointers through the walk
             for (int i = lane; i < nstore; i += 32) {
                 rn[abase + i] = sm.res_name[w][i];
                 an[abase + i] = sm.atom_name[w][i];
@@ -931,10 +959,37 @@ template <int NW>
 struct A2cBwdRingSmem {
     Topology<float> topo;
     signed char lut[256];
-    float x[NW][kA2cStageAtoms * 3];
-    float g[NW][kA2cStageAtoms * 3];
+    alignas(16) float x[NW][kA2cStageAtoms * 3 + 4];  // 4 floats of slack, as in A2cRingSmem
+    alignas(16) float g[NW][kA2cStageAtoms * 3 + 4];
     int base[1];  // first atom of each chunk, nchunk + 1 entries (dynamic)
 };
+
+__device__ __forceinline__ void cp_async16(float *dst_smem, const float *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst_smem)),
+                 "l"(src)
+                 : "memory");
+}
+
+// Stage n floats of src into the 16-byte-aligned row dst, starting at
+// dst + block_offset(src), by the warp: 16-byte asynchronous copies for every block
+// of src that lies whole inside the span, 4-byte ones for the ragged ends.  Returns
+// where the values start.
+__device__ __forceinline__ float *stage_span_async(float *dst, const float *src, int n, int lane) {
+    const int sh = block_offset(src);
+    const float *base = src - sh;  // 16-byte aligned; only [src, src + n) is read
+    const int nb = (n + sh + 3) >> 2;
+    for (int b = lane; b < nb; b += 32) {
+        const int lo = 4 * b - sh;
+        if (lo >= 0 && lo + 4 <= n) {
+            cp_async16(dst + 4 * b, base + 4 * b);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+                if (lo + e >= 0 && lo + e < n) cp_async4(dst + sh + lo + e, src + lo + e);
+        }
+    }
+    return dst + sh;
+}
 
 template <int NW>
 __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<float> a) {
@@ -989,7 +1044,6 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
     }
     const int nrun = total > a.maxA ? 0 : nchunk;  // a chain whose atoms overflow the rows gets zeros
     const float inv_dphi = 1.f / tp.bb_d[0], inv_dpsi = 1.f / tp.bb_d[1], inv_dom = 1.f / tp.bb_d[2];
-    float *sx = sm.x[w], *sg = sm.g[w];
 
 #pragma unroll 1
     for (int k = nrun - 1 - w; k >= 0; k -= NW) {
@@ -1006,11 +1060,9 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
         const int aoff = inc - na;
         const int abase = sm.base[k], n3 = 3 * (sm.base[k + 1] - abase);
         __syncwarp();  // the previous chunk's reads of the staging buffers are done
-        // asynchronous 4-byte copies: every copy of the chunk is in flight before the one wait
-        for (int i = lane; i < n3; i += 32) {
-            cp_async4(sx + i, xin + (size_t)3 * abase + i);
-            cp_async4(sg + i, gin + (size_t)3 * abase + i);
-        }
+        // asynchronous copies: every copy of the chunk is in flight before the one wait
+        const float *sx = stage_span_async(sm.x[w], xin + (size_t)3 * abase, n3, lane);
+        const float *sg = stage_span_async(sm.g[w], gin + (size_t)3 * abase, n3, lane);
         cp_async_wait_all();
         __syncwarp();
         const float o[3] = {sx[0], sx[1], sx[2]};  // chunk origin: its first N atom
