@@ -1278,13 +1278,7 @@ __global__ void __launch_bounds__(kPlainThreads) a2b_bwd_f64_plain_kernel(PlainA
 // ------------------------------------------------------------------- host side
 template <typename K>
 static int persistent_grid(K kernel, int threads, int items, int max_ctas, int dyn_smem = 0) {
-    static int num_sms = 0;
-    if (!num_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (num_sms <= 0) num_sms = 1;
-    }
+    const int num_sms = device_sm_count();
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem) != cudaSuccess ||
         per_sm < 1)
@@ -1312,16 +1306,7 @@ static A2bShape a2b_shape(const tpl_options &opt, bool backward) {
     return s;
 }
 
-static int num_sms() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
-}
+static int num_sms() { return device_sm_count(); }
 
 // threads_per_cta = 0 picks, from the shape, the scheme that measured fastest on
 // GB300 (4-residue-per-lane and 8-residue-per-lane chunks, one warp or one CTA of

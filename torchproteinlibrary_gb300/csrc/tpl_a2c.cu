@@ -1202,12 +1202,7 @@ static int launch_a2c_bwd(const A2cArgs<T> &a, int B, int renorm, cudaStream_t s
 // chains, four once every SM has several (GB300, forward without names, 0.099 against
 // 0.109 ms at 1024 x 1000 residues and 0.188 against 0.170 ms at 4096 x 500; with
 // names or in the backward the crossing comes at about half the batch).
-static int a2c_ring_warps(int B, int chains_per_sm) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
-    return B < chains_per_sm * sms ? 8 : 4;
-}
+static int a2c_ring_warps(int B, int chains_per_sm) { return B < chains_per_sm * device_sm_count() ? 8 : 4; }
 
 template <int NW>
 static int launch_a2c_fwd_ring(const A2cArgs<float> &a, int B, int renorm, cudaStream_t st) {

@@ -98,6 +98,23 @@ bool set_max_dynamic_smem(const void *func, int bytes) {
     return true;
 }
 
+int device_sm_count() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    static std::mutex mu;
+    static std::map<int, int> known;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = known.find(dev);
+        if (it != known.end()) return it->second;
+    }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    std::lock_guard<std::mutex> lk(mu);
+    known[dev] = n;
+    return n;
+}
+
 tpl_options resolve(const tpl_options *opt) {
     tpl_options o{};
     if (opt) o = *opt;

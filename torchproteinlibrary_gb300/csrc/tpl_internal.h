@@ -13,6 +13,9 @@ namespace tpl {
 // repeating it would cost host time on every launch.  false if the call fails.
 bool set_max_dynamic_smem(const void *func, int bytes);
 
+// Number of SMs of the current device, queried once per device (at least 1).
+int device_sm_count();
+
 // FP32 / FP64 (cos, sin) of the three backbone bond angles plus the bond lengths,
 // in joint order phi (N->CA), psi (CA->C), omega (C->N).  The FP32 pairs are picked
 // by bond_constants() so that the rounding errors of their norms cancel over a
