@@ -158,7 +158,7 @@ def run_reference(args):
         return
     import oracle
 
-    oracle.build(os.environ.get("TPL_REFERENCE_DIR", "/root/reference"))
+    oracle.build(oracle.reference_dir())
     threads = os.cpu_count() or 1
     for _ in range(max(0, args.warmup)):
         cpu_reference_rate(sample_chains=threads, threads=threads)
@@ -1083,7 +1083,7 @@ def cpu_baseline_entry():
     try:
         import oracle
 
-        oracle.build(os.environ.get("TPL_REFERENCE_DIR", "/root/reference"))
+        oracle.build(oracle.reference_dir())
         threads = os.cpu_count() or 1
         r, cores, kind, sample = cpu_reference_rate(sample_chains=threads, threads=threads)
         return {"value": r, "unit": "residues/s", "cores": cores, "kind": kind, "sample": sample}

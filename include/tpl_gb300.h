@@ -226,9 +226,22 @@ int tpl_a2c_backward_coords_f32(float *grad_angles, const float *grad_coords, co
  *     call, keeps the last call's contents afterwards, and calls that overlap on
  *     the GPU (two streams, or two host threads) race on it.
  *   - Its records are not kept for a backward pass: run tpl_a2b_forward_f32 with a
- *     workspace when the backward is needed. */
+ *     workspace when the backward is needed.
+ *   - The returned status covers the arguments and the launch.  Errors the kernels
+ *     find on the device (a length outside [0, max_len], a bounded wait that gave
+ *     up) are recorded in the array's status word; tpl_a2b_noalloc_status() reads
+ *     them back.
+ *   - The cached device address does not survive a cudaDeviceReset: do not call
+ *     it across a device reset. */
 int tpl_a2b_forward_f32_noalloc(const float *angles, const int32_t *lengths, float *coords, int batch, int max_len,
                                 const tpl_options *opt, void *stream);
+
+/* Error report of the last tpl_a2b_forward_f32_noalloc call on the current device.
+ * This entry point has no counterpart in the reference.  It synchronises `stream`,
+ * then returns through *status_out the first error the kernels recorded in the
+ * fixed array (TPL_OK if none) and clears it; it allocates nothing.  The next
+ * no-allocation call clears the record as well, so read it before that call. */
+int tpl_a2b_noalloc_status(void *stream, int *status_out);
 
 /* ---------------------------------------------------------------- CoordsTransform
  * Batched coordinate rows [batch, 3 * atoms_stride] (xyz per atom); the first

@@ -30,6 +30,21 @@ _ip = ctypes.POINTER(ctypes.c_int)
 _up = ctypes.POINTER(ctypes.c_ubyte)
 
 
+def reference_dir() -> str | None:
+    """The reference checkout that the oracle's reference builds read: the
+    TPL_REFERENCE_DIR environment variable, else the REF default of
+    oracle/Makefile (the one place that names the conventional location).
+    None when that directory does not exist (e.g. on a machine without it)."""
+    d = os.environ.get("TPL_REFERENCE_DIR")
+    if not d:
+        with open(os.path.join(HERE, "Makefile")) as f:
+            for line in f:
+                if line.startswith("REF") and "?=" in line:
+                    d = line.split("?=", 1)[1].strip()
+                    break
+    return d if d and os.path.isdir(d) else None
+
+
 def build(ref_dir: str | None = None) -> None:
     """Compile the C restatement, and the reference sources when ``ref_dir`` exists."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
@@ -170,6 +185,18 @@ def a2c_backward(grad_coords: np.ndarray, angles: np.ndarray, seqs: list[str], i
     if rc != 0:
         raise RuntimeError(f"a2c_backward failed ({rc})")
     return out
+
+
+def a2c_save_ref(seq: str, angles: np.ndarray, filename: str, mode: str) -> None:
+    """The reference's Angles2Coords_save (angles2coords_interface.cpp:117-137 ->
+    cConformation::save, cConformation.cpp:228-262) for one chain, angles [8, len(seq)]."""
+    angles = np.ascontiguousarray(angles, dtype=np.float64)
+    if angles.shape != (8, len(seq)):
+        raise ValueError("the reference reads angles with the sequence length as row stride")
+    lib = ref()
+    lib.ref_a2c_save.argtypes = [ctypes.c_char_p, _dp, ctypes.c_char_p, ctypes.c_char]
+    if lib.ref_a2c_save(seq.encode(), _ptr(angles, _dp), filename.encode(), mode.encode()) != 0:
+        raise RuntimeError("reference save failed")
 
 
 # ------------------------------------------------------------------ Coords2RMSD

@@ -7,6 +7,7 @@
  * interface for the same call, minus torch:
  *   ref_a2b_forward / ref_a2b_backward  <- Layers/ReducedModel/Angles2Backbone/angles2backbone_interface.cpp:60-111
  *   ref_a2c_forward / ref_a2c_backward  <- Layers/FullAtomModel/Angles2Coords/angles2coords_interface.cpp:8-115
+ *   ref_a2c_save                        <- angles2coords_interface.cpp:117-137 (cConformation::save)
  * The batch is split one chain per call (the reference's batch loops are
  * independent per chain) so that the chains can run on all host threads; the
  * Angles2Coords interface already uses OpenMP over chains
@@ -132,6 +133,21 @@ int ref_a2c_backward(double *grad_atoms, double *grad_angles, const unsigned cha
     return err;
 }
 
+// Angles2Coords_save of one chain: angles [8, len(seq)] (the reference passes the
+// sequence length as the row stride), mode 'w' or 'a'.  Returns 0, or -3 if the
+// reference threw.
+int ref_a2c_save(const char *sequence, double *angles, const char *filename, char mode) {
+    std::string seq(sequence);
+    std::vector<double> dummy_grad((size_t)8 * seq.size(), 0.0);
+    try {
+        std::vector<double> coords((size_t)3 * 16 * (seq.size() + 1), 0.0);
+        cConformation<double> conf(seq, angles, dummy_grad.data(), (unsigned)seq.size(), coords.data());
+        conf.save(std::string(filename), mode);
+    } catch (...) {
+        return -3;
+    }
+    return 0;
+}
 
 // The reference's PDB reader (cPDBLoader, as PDB2CoordsUnordered uses it): fills up
 // to max_atoms atoms (coords xyz, names as NUL-padded 4-byte slots, residue

@@ -32,7 +32,7 @@ def pytest_collection_modifyitems(config, items):
 @pytest.fixture(scope="session")
 def oracle_lib():
     import oracle
-    oracle.build(os.environ.get("TPL_REFERENCE_DIR", "/root/reference"))
+    oracle.build(oracle.reference_dir())
     return oracle
 
 

@@ -61,7 +61,7 @@ def test_atom_counts():
         oracle.num_atoms("ACDX")
 
 
-@pytest.mark.skipif(not oracle.ref_available() and not os.path.isdir("/root/reference"),
+@pytest.mark.skipif(not oracle.ref_available() and oracle.reference_dir() is None,
                     reason="reference sources not present")
 def test_port_matches_reference_build(oracle_lib):
     if not oracle.ref_available():

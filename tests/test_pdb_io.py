@@ -84,3 +84,19 @@ def test_write_read_round_trip_and_sequence(pdb, oracle_lib, tmp_path):
 def test_missing_file_raises(pdb, tmp_path):
     with pytest.raises(RuntimeError):
         pdb.PDB2CoordsUnordered()([str(tmp_path / "absent.pdb")])
+
+
+@pytest.mark.gpu
+def test_angles2coords_save_matches_reference_writer(built, tmp_path):
+    """Angles2Coords_save (GPU forward, then ATOM records) writes the same bytes as
+    the reference's cConformation::save (cConformation.cpp:228-262), whose output for
+    these inputs is tests/golden/a2c_save_ref.pdb: one chain with mode 'w', then two
+    appended as MODEL blocks with mode 'a'."""
+    from torchproteinlibrary_gb300 import load_extension
+    ext = load_extension("_FullAtomModel")
+    d = np.load(os.path.join(HERE, "golden", "a2c_save_ref.npz"))
+    out = str(tmp_path / "saved.pdb")
+    for i, (seq, mode) in enumerate(zip(d["sequences"], "waa")):
+        ext.Angles2Coords_save(str(seq), torch.tensor(d[f"angles{i}"], device="cuda"), out, mode)
+    with open(out, "rb") as f, open(os.path.join(HERE, "golden", "a2c_save_ref.pdb"), "rb") as g:
+        assert f.read() == g.read()

@@ -34,22 +34,16 @@ _FullAtomModel = load_extension("_FullAtomModel")
 
 
 def convertStringList(stringList):
-    '''Converts list of strings to 0-terminated byte tensor'''
-    maxlen = 0
-    for string in stringList:
-        string += '\0'
-        if len(string) > maxlen:
-            maxlen = len(string)
-    ar = np.zeros((len(stringList), maxlen), dtype=np.uint8)
-    for i, string in enumerate(stringList):
-        npstring = np.frombuffer(bytes(string, 'ascii'), dtype=np.uint8)
-        ar[i, :npstring.shape[0]] = npstring
-    return torch.from_numpy(ar)
+    """Sequences -> uint8 tensor [len(stringList), longest + 1], one NUL-terminated row each."""
+    raw = [s.encode("ascii") for s in stringList]
+    width = max(map(len, raw), default=0) + 1
+    packed = b"".join(r.ljust(width, b"\0") for r in raw)
+    return torch.from_numpy(np.frombuffer(packed, dtype=np.uint8).reshape(len(raw), width).copy())
 
 
 def convertString(string):
-    '''Converts a string to 0-terminated byte tensor'''
-    return torch.from_numpy(np.frombuffer(bytes(string + '\0', 'ascii'), dtype=np.uint8).copy())
+    """A sequence -> NUL-terminated uint8 tensor."""
+    return torch.tensor(list(string.encode("ascii")) + [0], dtype=torch.uint8)
 
 
 def _check(t, where, device):

@@ -36,20 +36,20 @@ _THREE_TO_ONE = {"ALA": "A", "ARG": "R", "ASN": "N", "ASP": "D", "CYS": "C", "GL
 
 
 def convertStringList(stringList):
-    """List of strings -> NUL-terminated uint8 tensor [len, max_len + 1]."""
-    maxlen = max([len(s) + 1 for s in stringList] + [1])
-    ar = np.zeros((len(stringList), maxlen), dtype=np.uint8)
-    for i, s in enumerate(stringList):
-        b = s.encode("utf-8")
-        ar[i, :len(b)] = np.frombuffer(b, dtype=np.uint8)
-    return torch.from_numpy(ar)
+    """Strings -> uint8 tensor [len(stringList), longest + 1], one NUL-terminated row each."""
+    raw = [s.encode("utf-8") for s in stringList]
+    width = max(map(len, raw), default=0) + 1
+    packed = b"".join(r.ljust(width, b"\0") for r in raw)
+    return torch.from_numpy(np.frombuffer(packed, dtype=np.uint8).reshape(len(raw), width).copy())
 
 
 def string2tensor(string):
-    return torch.from_numpy(np.frombuffer((string + "\0").encode("utf-8"), dtype=np.uint8).copy())
+    """A string -> NUL-terminated uint8 tensor."""
+    return torch.tensor(list(string.encode("utf-8")) + [0], dtype=torch.uint8)
 
 
 def tensor2string(tensor):
+    """The bytes of a uint8 tensor up to its first NUL, decoded."""
     return bytes(tensor.cpu().numpy().tobytes()).split(b"\x00")[0].decode("utf-8", "strict")
 
 
@@ -63,19 +63,20 @@ class PDB2CoordsOrdered:
 
 
 class PDB2CoordsUnordered:
+    """PDB files -> their heavy-atom ATOM records in file order, padded to the
+    largest file: (coords f64 [B, 3N], chain_names, res_names u8 [B, N, 4],
+    res_nums int32 [B, N], atom_names u8 [B, N, 4], num_atoms int32 [B])."""
+
+    # (dtype, trailing shape) of each output; the native reader resizes them to N atoms
+    _OUTPUTS = ((torch.double, (0,)), (torch.uint8, (0, 4)), (torch.uint8, (0, 4)), (torch.int, (0,)),
+                (torch.uint8, (0, 4)))
+
     def __call__(self, filenames):
-        filenamesTensor = convertStringList(filenames)
-        batch_size = len(filenames)
-        num_atoms = torch.zeros(batch_size, dtype=torch.int)
-        output_coords_cpu = torch.zeros(batch_size, 1, dtype=torch.double)
-        output_chainnames_cpu = torch.zeros(batch_size, 1, 1, dtype=torch.uint8)
-        output_resnames_cpu = torch.zeros(batch_size, 1, 1, dtype=torch.uint8)
-        output_resnums_cpu = torch.zeros(batch_size, 1, dtype=torch.int)
-        output_atomnames_cpu = torch.zeros(batch_size, 1, 1, dtype=torch.uint8)
-        _FullAtomModel.PDB2CoordsUnordered(filenamesTensor, output_coords_cpu, output_chainnames_cpu,
-                                           output_resnames_cpu, output_resnums_cpu, output_atomnames_cpu, num_atoms)
-        return (output_coords_cpu, output_chainnames_cpu, output_resnames_cpu, output_resnums_cpu,
-                output_atomnames_cpu, num_atoms)
+        n = len(filenames)
+        outputs = [torch.empty((n,) + shape, dtype=dtype) for dtype, shape in self._OUTPUTS]
+        num_atoms = torch.empty(n, dtype=torch.int)
+        _FullAtomModel.PDB2CoordsUnordered(convertStringList(filenames), *outputs, num_atoms)
+        return (*outputs, num_atoms)
 
 
 def get_sequence(filename):
@@ -98,41 +99,62 @@ def pdb2sequence(filenames):
     return [get_sequence(f) for f in filenames]
 
 
+def _last_numbers(filename):
+    """The highest MODEL number and ATOM serial already in a PDB file (0 and 0 if none)."""
+    model = serial = 0
+    with open(filename) as f:
+        for record in f:
+            if record.startswith("MODEL"):
+                model = max(model, int(record[5:].split()[0]))
+            elif record.startswith("ATOM"):
+                serial = max(serial, int(record[6:11]))
+    return model, serial
+
+
+def _names(t):
+    """[B, N, 4] NUL-padded name slots -> lists of strings."""
+    raw = t.detach().cpu().numpy()
+    return [[bytes(slot).split(b"\x00")[0].decode("utf-8", "strict") for slot in row] for row in raw]
+
+
+def _atom_record(serial, atom, res, chain, res_num, x, y, z, bfactor=None):
+    """One ATOM record: serial in columns 7-11, atom name left-justified from column
+    14, residue name 18-20, chain 22, residue number 23-26, x / y / z 31-54 (%8.3f),
+    then occupancy 1.00 and the B-factor when one is given."""
+    text = "ATOM  %5d  %-3s %3s %c%4d    %8.3f%8.3f%8.3f" % (serial, atom, res, chain, res_num, x, y, z)
+    if bfactor is not None:
+        text += "%6.2f%6.2f" % (1.0, bfactor)
+    return text + "\n"
+
+
 def writePDB(filename, coords, chainnames, resnames, resnums, atomnames, num_atoms, bfactors=None, add_model=True,
              rewrite=True):
-    """Write a batch as PDB ATOM records, one MODEL per chain (the reference's format)."""
-    batch_size = coords.size(0)
-    last_model_num = 0
-    last_atom_num = 0
+    """Write a batch as PDB ATOM records, chain b as MODEL (first + b) when add_model.
+
+    rewrite=True replaces an existing file.  rewrite=False appends: serials continue
+    after the highest ATOM serial in the file, and the model numbers start at the
+    highest MODEL number already there, as the reference numbers them.  A chain name
+    that is empty is written as "A".  Only MODEL and ATOM records are scanned when
+    appending (the reference matches those words anywhere in a line)."""
+    first_model = first_serial = 0
     if os.path.exists(filename):
         if rewrite:
             os.remove(filename)
         else:
-            with open(filename, "r") as fin:
-                for line in fin:
-                    if line.find("MODEL") != -1:
-                        last_model_num = max(last_model_num, int(line.split()[1]))
-                    if line.find("ATOM") != -1:
-                        last_atom_num = max(last_atom_num, int(line[6:11]))
-    coords = coords.detach().cpu()
-    with open(filename, "a") as fout:
-        for i in range(batch_size):
-            if add_model:
-                fout.write("MODEL %d\n" % (i + last_model_num))
-            for j in range(int(num_atoms[i])):
-                chain_name = tensor2string(chainnames[i, j, :])
-                if len(chain_name) == 0:
-                    chain_name = "A"
-                atom_name = tensor2string(atomnames[i, j, :])
-                res_name = tensor2string(resnames[i, j, :])
-                res_num = int(resnums[i, j])
-                x, y, z = (float(coords[i, 3 * j + k]) for k in range(3))
-                if bfactors is None:
-                    fout.write("ATOM  %5d  %-3s %3s %c%4d    %8.3f%8.3f%8.3f\n" % (
-                        j + last_atom_num + 1, atom_name, res_name, chain_name[0], res_num, x, y, z))
-                else:
-                    fout.write("ATOM  %5d  %-3s %3s %c%4d    %8.3f%8.3f%8.3f%6.2f%6.2f\n" % (
-                        j + last_atom_num + 1, atom_name, res_name, chain_name[0], res_num, x, y, z, 1.0,
-                        float(bfactors[i, j])))
-            if add_model:
-                fout.write("ENDMDL\n")
+            first_model, first_serial = _last_numbers(filename)
+    xyz = coords.detach().cpu().double().numpy()
+    chains, res, atoms = _names(chainnames), _names(resnames), _names(atomnames)
+    nums = resnums.detach().cpu().numpy()
+    counts = [int(v) for v in num_atoms]
+    bf = None if bfactors is None else bfactors.detach().cpu().double().numpy()
+    records = []
+    for b, count in enumerate(counts):
+        if add_model:
+            records.append("MODEL %d\n" % (first_model + b))
+        records.extend(_atom_record(first_serial + j + 1, atoms[b][j], res[b][j], chains[b][j][:1] or "A",
+                                    int(nums[b, j]), *xyz[b, 3 * j:3 * j + 3], None if bf is None else bf[b, j])
+                       for j in range(count))
+        if add_model:
+            records.append("ENDMDL\n")
+    with open(filename, "a") as f:
+        f.writelines(records)

@@ -42,6 +42,7 @@ _SIGNATURES = {
     "tpl_a2c_backward_f64": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _i, _i, _i, _vp, _vp]),
     "tpl_a2c_backward_coords_f32": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _sz, _i, _i, _i, _vp]),
     "tpl_a2b_forward_f32_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "tpl_a2b_noalloc_status": (_i, [_vp, ctypes.POINTER(_i)]),
     "tpl_sincos_f32": (_i, [_vp, _vp, _vp, _i, _vp]),
     "tpl_coords_translate_f32": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp]),
     "tpl_coords_translate_f64": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp]),

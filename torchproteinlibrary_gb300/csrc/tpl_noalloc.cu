@@ -17,7 +17,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 // In host code `g_noalloc_scratch` names a host-side stand-in, not a device
 // address; the device address is looked up once per device, with that device
-// current, and cached.
+// current, and cached.  A cudaDeviceReset (or a release and re-creation of the
+// primary context) reloads the module and leaves the cached address stale, so
+// the entry points below must not be used across a device reset.
 static void *noalloc_scratch_ptr(int *status) {
     static std::mutex mu;
     static void *ptrs[256] = {nullptr};
@@ -58,4 +60,14 @@ extern "C" int tpl_a2b_forward_f32_noalloc(const float *angles, const int32_t *l
     // the look-back flags, tickets and epochs must start at zero
     if (cudaMemsetAsync(scratch, 0, need, (cudaStream_t)stream) != cudaSuccess) return TPL_ERR_LAUNCH;
     return a2b_forward_f32(angles, lengths, coords, scratch, batch, max_len, o, (cudaStream_t)stream);
+}
+
+// The status word sits at the start of the scratch (the workspace header that the
+// kernels write their first error into).  The next no-allocation call clears it.
+extern "C" int tpl_a2b_noalloc_status(void *stream, int *status_out) {
+    if (!status_out) return TPL_ERR_ARGUMENT;
+    int status = TPL_OK;
+    void *scratch = noalloc_scratch_ptr(&status);
+    if (status != TPL_OK) return status;
+    return tpl_workspace_status(scratch, stream, status_out);
 }
