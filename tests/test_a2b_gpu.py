@@ -559,3 +559,32 @@ def test_full_size_geometry_and_fp64_slice(rm):
                                    torch.empty(0, device=dev))
     check(coords[:n].double().cpu().numpy(), gi[:n].double().cpu().numpy(), c64.cpu().numpy(),
           g64.cpu().numpy(), lengths[:n], L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
+def test_config1_exact_shape_fp64_and_fp32(rm):
+    """The reference's CPU configuration exactly: 32 chains of 64 residues (lengths all
+    64), phi, psi ~ U[-pi, pi), omega = pi, float64, upstream gradient ~ N(0, 1).  The
+    plain FP64 form matches the oracle to 1e-9 A and 1e-9 of the largest gradient
+    entry; the batched FP32 path to 1e-3 A and 1e-4 of the largest entry.  omega of
+    the last residue is compared too: the oracle returns 0 there, as this build does."""
+    rng = np.random.default_rng(1001)
+    B, L = 32, 64
+    ang = rng.uniform(-np.pi, np.pi, (B, 3, L))
+    ang[:, 2] = np.pi
+    lengths = np.full(B, L, dtype=np.int32)
+    up = rng.standard_normal((B, 9 * L))
+    rc, A = oracle.a2b_forward(ang, lengths)
+    rg = oracle.a2b_backward(up, ang, lengths, A)
+    dev = torch.device("cuda")
+    ln = torch.tensor(lengths, device=dev)
+    for dt, ctol, gtol in ((torch.float64, 1e-9, 1e-9), (torch.float32, 1e-3, 1e-4)):
+        a = torch.tensor(ang, dtype=dt, device=dev)
+        c = torch.empty(B, 9 * L, dtype=dt, device=dev)
+        g = torch.empty(B, 3, L, dtype=dt, device=dev)
+        ws = torch.zeros(rm.workspace_bytes(B, L), dtype=torch.uint8, device=dev)
+        rm.Angles2BackboneGPU_forward(a, c, ln, ws)
+        rm.Angles2BackboneGPU_backward(g, torch.tensor(up, dtype=dt, device=dev), a, ln, ws,
+                                       torch.empty(0, device=dev))
+        cerr = (c.double().cpu().numpy() - rc).reshape(B, -1, 3)
+        assert np.linalg.norm(cerr, axis=-1).max() <= ctol
+        assert np.abs(g.double().cpu().numpy() - rg).max() <= gtol * np.abs(rg).max()
