@@ -219,9 +219,9 @@ def run_ours(args):
     else:
         tuned = autotune.tune(ang, lengths, up, use_cache=False)
         if not args.no_extras:
-            # FP64 inter-tile carry threshold sweep (-1 = never FP64)
-            # (on warp tiles of 256 residues: the one-warp-per-chain scheme has no inter-tile carry)
-            sweep_rows = autotune.sweep(ang, lengths, up, candidates=[(8, 1)],
+            # FP64 carry threshold sweep on the four-warp scheme (the default for these chains)
+            # and on warp tiles of 256 residues (-1 = never FP64)
+            sweep_rows = autotune.sweep(ang, lengths, up, candidates=[(8, 4), (8, 1)],
                                         carry_thresholds=(128, 256, 512, -1), steps=5)
             rm.set_options(tuned["residues_per_thread"], tuned["fp64_carry_min_len"], 0, 0,
                            tuned["threads_per_cta"])

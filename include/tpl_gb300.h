@@ -63,8 +63,12 @@ typedef struct tpl_options {
                                   (same records); 1 = warp-granular tiles of 32 R residues joined by
                                   look-back; 128 = CTA tiles of 128 R residues.  Angles2Coords
                                   reads it as its threads per chain (0 = 256, 128, 256, 512). */
-    int fp64_carry_min_len;    /* chains at least this long compose inter-tile carries in FP64;
-                                  0 = default (always), -1 = never */
+    int fp64_carry_min_len;    /* chains at least this long compose inter-tile carries in FP64.
+                                  Tile schemes: 0 = default (always), -1 = never.  Four warps per
+                                  chain: a positive length hands the chain frame from warp to warp
+                                  in FP64; 0 (the default) and -1 keep it in FP32 (the tuned
+                                  choice: the FP64 carry does not lower the error measurably).  One
+                                  warp per chain keeps its frame in FP32. */
     int renormalize;           /* 0 = default (on), 1 = on, -1 = off: Newton-Schulz renormalisation
                                   of scan aggregates */
     int max_ctas;              /* cap on persistent CTAs; 0 = occupancy-derived */

@@ -133,6 +133,25 @@ def test_fp64_carry_threshold_and_renorm_off(rm):
         check(c, gi, rc, rg, lengths, L, ctol, GRAD_TOL_F32)
 
 
+@pytest.mark.parametrize("rpt", [4, 8])
+def test_four_warp_fp64_carry_threshold(rm, rpt):
+    """The four-warp forward with an FP64 chain-frame carry for chains of at least
+    300 residues (a positive fp64_carry_min_len): chains above and below the
+    threshold in one batch, coordinates within 1e-3 A of the oracle and the
+    recomputing backward (which starts from the forward's recorded frames) within
+    1e-4; the FP32 carry (threshold 0, the default) on the same batch for contrast."""
+    B, L = 5, 1000
+    ang, lengths, g = make_case(B, L, 91 + rpt, lengths=[1000, 700, 300, 299, 40])
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    for carry in (300, 0):
+        rm.set_options(rpt, carry, 0, 0, 4)
+        try:
+            c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+        finally:
+            rm.set_options(0, 0, 0, 0)
+        check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
 @pytest.mark.parametrize("rpt,cta", [(0, 1), (8, 32), (4, 32)])
 def test_padding_nan_does_not_leak(rm, rpt, cta):
     B, L = 4, 64
@@ -588,3 +607,30 @@ def test_config1_exact_shape_fp64_and_fp32(rm):
         cerr = (c.double().cpu().numpy() - rc).reshape(B, -1, 3)
         assert np.linalg.norm(cerr, axis=-1).max() <= ctol
         assert np.abs(g.double().cpu().numpy() - rg).max() <= gtol * np.abs(rg).max()
+
+
+def test_layer_runs_the_tuned_options(rm):
+    """The float32 layer asks the autotuner for its shape's options (the table shipped
+    for this GPU) and passes them to the kernels: its output equals the extension's
+    with those options given explicitly, bit for bit, and the backward matches too."""
+    from torchproteinlibrary_gb300 import autotune
+    from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+    dev = torch.device("cuda")
+    B, L = 2048, 256
+    tuned = autotune.options_for(dev, B, L)
+    if tuned is None:
+        pytest.skip(f"no tuned table for {torch.cuda.get_device_name(dev)}")
+    (rpt, cta), bwd = tuned
+    ang, lengths, g = make_case(B, L, 5)
+    a = torch.tensor(ang, dtype=torch.float32, device=dev, requires_grad=True)
+    ln = torch.tensor(lengths, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    c = Angles2Backbone()(a, ln)
+    c.backward(gt)
+    ws = torch.zeros(rm.workspace_bytes(B, L, rpt, cta), dtype=torch.uint8, device=dev)
+    c2 = torch.empty_like(c)
+    rm.Angles2BackboneGPU_forward(a.detach(), c2, ln, ws, rpt, cta)
+    g2 = torch.empty_like(a)
+    rm.Angles2BackboneGPU_backward_coords(g2, gt, c2, ln, ws, *bwd)
+    assert torch.equal(c.detach(), c2)
+    assert torch.equal(a.grad, g2)

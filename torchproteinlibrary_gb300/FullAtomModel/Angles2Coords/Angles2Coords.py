@@ -64,7 +64,9 @@ class Angles2CoordsFunction(Function):
     def forward(ctx, input_angles, sequenceTensor, num_atoms):
         input_angles = input_angles.contiguous()
         dev = input_angles.device
-        max_num_atoms = int(torch.max(num_atoms)) if num_atoms.numel() else 0
+        max_num_atoms = getattr(num_atoms, "_tpl_max_atoms", None)  # set by Angles2Coords' sequence cache
+        if max_num_atoms is None:
+            max_num_atoms = int(torch.max(num_atoms)) if num_atoms.numel() else 0
         batch_size = input_angles.size(0)
         seq = sequenceTensor if sequenceTensor.device == dev else sequenceTensor.to(dev)
         coords = torch.empty(batch_size, 3 * max_num_atoms, dtype=input_angles.dtype, device=dev)
@@ -106,7 +108,9 @@ class Angles2Coords(Module):
         if key != self._cache_key:
             seq = convertStringList(sequences).to(device)
             counts = [_FullAtomModel.getSeqNumAtoms(s) for s in sequences]
-            self._cache = (seq, torch.IntTensor(counts), counts)
+            num_atoms = torch.IntTensor(counts)
+            num_atoms._tpl_max_atoms = max(counts, default=0)
+            self._cache = (seq, num_atoms, counts)
             self._cache_key = key
         return self._cache
 

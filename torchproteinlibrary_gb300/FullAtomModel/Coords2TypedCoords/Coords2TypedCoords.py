@@ -50,7 +50,9 @@ class Coords2TypedCoordsFunction(Function):
             raise RuntimeError("Coords2TypedCoords: this build has no CPU path; move the tensors to a CUDA device")
         x = input_coords.contiguous()
         dev = x.device
-        max_num_atoms = int(torch.max(num_atoms)) if num_atoms.numel() else 0
+        max_num_atoms = getattr(num_atoms, "_tpl_max_atoms", None)  # Angles2Coords' counts carry their maximum
+        if max_num_atoms is None:
+            max_num_atoms = int(torch.max(num_atoms)) if num_atoms.numel() else 0
         B = x.size(0)
         na = num_atoms.to(device=dev, dtype=torch.int32).contiguous()
         rn = input_resnames.to(dev).contiguous()

@@ -14,6 +14,7 @@ TPL_CHECK_NAN=1.
 """
 import math
 import os
+import weakref
 
 import torch
 from torch.autograd import Function
@@ -24,8 +25,22 @@ from ... import load_extension
 _RMSD = load_extension("_RMSD")
 
 
+# device int32 copies of host num_atoms tensors, reused while the host tensor is
+# unchanged (its version counter), so that repeated calls with the same counts make
+# no host-to-device copy
+_NA_ON_DEVICE: "weakref.WeakKeyDictionary" = weakref.WeakKeyDictionary()
+
+
 def _na(num_atoms, device):
-    return num_atoms.to(device=device, dtype=torch.int32).contiguous()
+    if num_atoms.device == device:
+        return num_atoms.to(dtype=torch.int32).contiguous()
+    hit = _NA_ON_DEVICE.get(num_atoms)
+    if hit is not None and hit[0] == num_atoms._version and hit[1].device == device:
+        return hit[1]
+    na = num_atoms.to(device=device, dtype=torch.int32).contiguous()
+    if not torch.cuda.is_current_stream_capturing():
+        _NA_ON_DEVICE[num_atoms] = (num_atoms._version, na)
+    return na
 
 
 def _check(t, where):

@@ -20,17 +20,28 @@ Differences from the reference:
     for backward, as the reference saves its frame buffer ``A``), so it does not
     walk the chain again.  Set ``Angles2BackboneGPUFunction.backward_from_coords``
     to False to recompute from the angles instead.
+  * The float32 scan scheme and tile for the batch's shape come from the autotuner
+    (``autotune.options_for``: the user's tuning cache, else the table tuned for this
+    GPU and shipped with the package, else the library's built-in rule).
+  * The float32 path with the backward from coordinates reuses one workspace per
+    (device, stream, shape, options) instead of allocating and zeroing one per call:
+    that backward reads only the workspace's status word, and the forward's chain
+    records, which a later forward of the same shape rewrites, are not read by it.
 """
 import math
 import os
+from collections import OrderedDict
 
 import torch
 from torch.autograd import Function
 from torch.nn.modules.module import Module
 
-from ... import load_extension
+from ... import autotune, load_extension
 
 _ReducedModel = load_extension("_ReducedModel")
+
+_WS_CACHE: "OrderedDict[tuple, torch.Tensor]" = OrderedDict()
+_WS_CACHE_SIZE = 8
 
 
 def _check_nan(t, ws, where):
@@ -42,8 +53,27 @@ def _check_nan(t, ws, where):
             raise Exception(f"Angles2BackboneFunction: {where} Nan")
 
 
-def new_workspace(batch, max_len, device):
-    return torch.zeros(int(_ReducedModel.workspace_bytes(batch, max_len)), dtype=torch.uint8, device=device)
+def new_workspace(batch, max_len, device, residues_per_thread=-1, threads_per_cta=-1):
+    return torch.zeros(int(_ReducedModel.workspace_bytes(batch, max_len, residues_per_thread, threads_per_cta)),
+                       dtype=torch.uint8, device=device)
+
+
+def _shared_workspace(batch, max_len, device, fwd_opts):
+    """A zeroed-once workspace per (device, current stream, shape, options), kept for
+    reuse by later calls (at most _WS_CACHE_SIZE of them).  A graph being captured
+    gets one of its own."""
+    if torch.cuda.is_current_stream_capturing():
+        return new_workspace(batch, max_len, device, *fwd_opts)
+    key = (device.index, torch.cuda.current_stream(device).cuda_stream, batch, max_len) + tuple(fwd_opts)
+    ws = _WS_CACHE.get(key)
+    if ws is None:
+        ws = new_workspace(batch, max_len, device, *fwd_opts)
+        _WS_CACHE[key] = ws
+        if len(_WS_CACHE) > _WS_CACHE_SIZE:
+            _WS_CACHE.popitem(last=False)
+    else:
+        _WS_CACHE.move_to_end(key)
+    return ws
 
 
 class Angles2BackboneGPUFunction(Function):
@@ -57,12 +87,19 @@ class Angles2BackboneGPUFunction(Function):
             raise Exception('Angles2BackboneFunction: ', 'Incorrect input size:', input_angles.size())
         input_angles = input_angles.contiguous()
         batch_size, _, max_len = input_angles.shape
-        coords = torch.empty(batch_size, 9 * max_len, dtype=input_angles.dtype, device=input_angles.device)
-        ctx.A = new_workspace(batch_size, max_len, input_angles.device)
-        _ReducedModel.Angles2BackboneGPU_forward(input_angles, coords, angles_length, ctx.A)
+        dev = input_angles.device
+        coords = torch.empty(batch_size, 9 * max_len, dtype=input_angles.dtype, device=dev)
+        f32 = input_angles.dtype == torch.float32
+        tuned = autotune.options_for(dev, batch_size, max_len) if f32 and dev.type == "cuda" else None
+        fwd_opts, bwd_opts = tuned if tuned is not None else ((-1, -1), (-1, -1, -1))
+        ctx.from_coords = Angles2BackboneGPUFunction.backward_from_coords and f32
+        if ctx.from_coords:
+            ctx.A = _shared_workspace(batch_size, max_len, dev, fwd_opts)
+        else:  # the recomputing backward reads the forward's chain records: a workspace of its own
+            ctx.A = new_workspace(batch_size, max_len, dev, *fwd_opts)
+        _ReducedModel.Angles2BackboneGPU_forward(input_angles, coords, angles_length, ctx.A, *fwd_opts)
         _check_nan(coords, ctx.A, "forward")
-        ctx.from_coords = (Angles2BackboneGPUFunction.backward_from_coords and
-                           input_angles.dtype == torch.float32)
+        ctx.fwd_opts, ctx.bwd_opts = fwd_opts, bwd_opts
         ctx.save_for_backward(input_angles, angles_length, coords if ctx.from_coords else None)
         return coords
 
@@ -72,10 +109,11 @@ class Angles2BackboneGPUFunction(Function):
         gradOutput = gradOutput.contiguous()
         gradInput = torch.empty_like(input_angles)
         if ctx.from_coords:
-            _ReducedModel.Angles2BackboneGPU_backward_coords(gradInput, gradOutput, coords, angles_length, ctx.A)
+            _ReducedModel.Angles2BackboneGPU_backward_coords(gradInput, gradOutput, coords, angles_length, ctx.A,
+                                                             *ctx.bwd_opts)
         else:
             _ReducedModel.Angles2BackboneGPU_backward(gradInput, gradOutput, input_angles, angles_length, ctx.A,
-                                                      gradInput.new_empty(0))
+                                                      gradInput.new_empty(0), *ctx.fwd_opts)
         _check_nan(gradInput, ctx.A, "backward")
         return gradInput, None
 

@@ -1,4 +1,4 @@
-"""Autotuner for the Angles2Backbone FP32 kernels.
+"""Autotuner for the Angles2Backbone FP32 kernels, and the lookup the layer uses.
 
 Knobs (tpl_options): residues per thread R (the scan tile is 32 R residues for
 warp tiles, 128 R for CTA tiles, a 32 R-residue chunk for one warp per chain),
@@ -10,6 +10,11 @@ synthetic chains of that shape with CUDA events and keeps the fastest whose
 coordinates stay within the accuracy bound of the FP64 form.  Results are
 cached per GPU name and shape bucket in a JSON file
 ($TPL_TUNE_CACHE, default ~/.cache/torchproteinlibrary_gb300/tune.json).
+
+The layer (``ReducedModel.Angles2Backbone``) asks ``options_for`` for every float32
+batch: the user's cache first, then the table shipped with the package for this GPU
+(``tuned/<gpu name>.json``, written by ``build_table`` on that GPU), and when
+neither has the shape's bucket, the library's built-in rule (tpl_options left at 0).
 """
 from __future__ import annotations
 
@@ -178,3 +183,96 @@ def tune(ang, lengths, up, use_cache=True, steps=5):
     tune.last_sweep = rows
     tune.last_backward_sweep = brows
     return best
+
+
+# ------------------------------------------------------------ the layer's lookup
+_TABLE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned")
+_LOOKUP: dict = {}
+_TABLES: dict = {}
+
+
+def table_file(gpu_name: str) -> str:
+    """Path of the shipped table for a GPU name."""
+    return os.path.join(_TABLE_DIR, "".join(c if c.isalnum() else "_" for c in gpu_name) + ".json")
+
+
+def _shipped_table(gpu_name: str) -> dict:
+    if gpu_name not in _TABLES:
+        try:
+            with open(table_file(gpu_name)) as f:
+                _TABLES[gpu_name] = json.load(f)
+        except (OSError, ValueError):
+            _TABLES[gpu_name] = {}
+    return _TABLES[gpu_name]
+
+
+def _entry_options(entry: dict):
+    bc = entry["backward_coords"]
+    return ((int(entry["residues_per_thread"]), int(entry["threads_per_cta"])),
+            (int(bc["residues_per_thread"]), int(bc.get("copy_buffers", 0)), int(bc.get("threads_per_cta", 0))))
+
+
+def options_for(device, batch: int, max_len: int):
+    """((residues_per_thread, threads_per_cta) of the forward, (residues_per_thread,
+    copy_buffers, threads_per_cta) of the backward from coordinates) tuned for this
+    shape's bucket on this GPU, or None (the library's built-in rule then applies).
+    Looked up once per (device, batch, max_len) in the process."""
+    key = (device.index, int(batch), int(max_len))
+    hit = _LOOKUP.get(key, False)
+    if hit is not False:
+        return hit
+    name = torch.cuda.get_device_name(device)
+    bucket = _bucket(batch, max_len)
+    entry = _load_cache().get(f"{name}|{bucket}|v2") or _shipped_table(name).get(bucket)
+    res = None
+    if entry and "backward_coords" in entry:
+        try:
+            res = _entry_options(entry)
+        except (KeyError, TypeError, ValueError):
+            res = None
+    _LOOKUP[key] = res
+    return res
+
+
+def clear_lookup() -> None:
+    """Forget the options looked up so far (after the cache or a table changed)."""
+    _LOOKUP.clear()
+    _TABLES.clear()
+
+
+TABLE_BATCHES = (32, 128, 512, 1024, 2048, 4096, 16384)
+TABLE_LENGTHS = (64, 128, 256, 384, 512, 768, 1024)
+
+
+def build_table(device=None, batches=TABLE_BATCHES, lengths=TABLE_LENGTHS, steps=5, seed=0) -> dict:
+    """Tune every (batch, max_len) bucket of the grid on this GPU and return the table
+    (bucket -> tuned entry) that ``options_for`` reads.  Each bucket is tuned on
+    synthetic chains at the bucket's upper shape: lengths uniform on [max_len / 4,
+    max_len], phi and psi uniform on [-pi, pi), omega = pi, an N(0, 1) upstream
+    gradient.
+
+        python -c "from torchproteinlibrary_gb300 import autotune as t; t.write_table()"
+    """
+    device = torch.device("cuda") if device is None else device
+    g = torch.Generator(device=device).manual_seed(seed)
+    table = {}
+    for B in batches:
+        for L in lengths:
+            ang = (torch.rand(B, 3, L, device=device, generator=g) * 2 - 1) * math.pi
+            ang[:, 2] = math.pi
+            lens = torch.randint(max(1, L // 4), L + 1, (B,), device=device, generator=g, dtype=torch.int32)
+            up = torch.randn(B, 9 * L, device=device, generator=g)
+            best = dict(tune(ang, lens, up, use_cache=False, steps=steps))
+            best["tuned_on"] = f"{B}x{L}, lengths U[{max(1, L // 4)}, {L}]"
+            table[_bucket(B, L)] = best
+    return table
+
+
+def write_table(path=None, **kw) -> str:
+    """build_table on the current GPU, written where options_for looks for it (or to path)."""
+    table = build_table(**kw)
+    path = path or table_file(torch.cuda.get_device_name(torch.device("cuda")))
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    return path

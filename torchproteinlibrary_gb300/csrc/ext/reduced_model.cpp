@@ -34,10 +34,21 @@ void *stream_of(const torch::Tensor &t) {
     return (void *)c10::cuda::getCurrentCUDAStream(t.device().index()).stream();
 }
 
-size_t ws_bytes(int64_t B, int64_t L) { return tpl_a2b_workspace_bytes((int)B, (int)L, &g_opt); }
+// The options of one call: the module-wide ones (set_options), with the scheme and
+// residues per thread replaced where the caller passes them (>= 0), as the layer
+// does with the autotuner's choice for the batch's shape.
+tpl_options call_options(int64_t residues_per_thread, int64_t threads_per_cta) {
+    tpl_options o = g_opt;
+    if (residues_per_thread >= 0) o.residues_per_thread = (int)residues_per_thread;
+    if (threads_per_cta >= 0) o.threads_per_cta = (int)threads_per_cta;
+    return o;
+}
+
+size_t ws_bytes(int64_t B, int64_t L, const tpl_options &o) { return tpl_a2b_workspace_bytes((int)B, (int)L, &o); }
 
 void Angles2BackboneGPU_forward(torch::Tensor input_angles, torch::Tensor output_coords,
-                                torch::Tensor angles_length, torch::Tensor A) {
+                                torch::Tensor angles_length, torch::Tensor A, int64_t residues_per_thread,
+                                int64_t threads_per_cta) {
     check_cuda(input_angles, "input_angles");
     check_cuda(output_coords, "output_coords");
     check_cuda(angles_length, "angles_length");
@@ -52,9 +63,9 @@ void Angles2BackboneGPU_forward(torch::Tensor input_angles, torch::Tensor output
     void *st = stream_of(input_angles);
     int s;
     if (input_angles.scalar_type() == torch::kFloat) {
+        const tpl_options o = call_options(residues_per_thread, threads_per_cta);
         s = tpl_a2b_forward_f32(input_angles.data_ptr<float>(), angles_length.data_ptr<int32_t>(),
-                                output_coords.data_ptr<float>(), A.data_ptr(), A.nbytes(), (int)B, (int)L, &g_opt,
-                                st);
+                                output_coords.data_ptr<float>(), A.data_ptr(), A.nbytes(), (int)B, (int)L, &o, st);
     } else if (input_angles.scalar_type() == torch::kDouble) {
         s = tpl_a2b_forward_f64(input_angles.data_ptr<double>(), angles_length.data_ptr<int32_t>(),
                                 output_coords.data_ptr<double>(), (int)B, (int)L, st);
@@ -65,7 +76,8 @@ void Angles2BackboneGPU_forward(torch::Tensor input_angles, torch::Tensor output
 }
 
 void Angles2BackboneGPU_backward(torch::Tensor gradInput, torch::Tensor gradOutput, torch::Tensor input_angles,
-                                 torch::Tensor angles_length, torch::Tensor A, torch::Tensor dr_dangle) {
+                                 torch::Tensor angles_length, torch::Tensor A, torch::Tensor dr_dangle,
+                                 int64_t residues_per_thread, int64_t threads_per_cta) {
     (void)dr_dangle;
     check_cuda(gradInput, "gradInput");
     check_cuda(gradOutput, "gradOutput");
@@ -84,9 +96,10 @@ void Angles2BackboneGPU_backward(torch::Tensor gradInput, torch::Tensor gradOutp
     void *st = stream_of(input_angles);
     int s;
     if (input_angles.scalar_type() == torch::kFloat) {
+        const tpl_options o = call_options(residues_per_thread, threads_per_cta);  // the forward's options
         s = tpl_a2b_backward_f32(gradInput.data_ptr<float>(), gradOutput.data_ptr<float>(),
                                  input_angles.data_ptr<float>(), angles_length.data_ptr<int32_t>(), A.data_ptr(),
-                                 A.nbytes(), (int)B, (int)L, &g_opt, st);
+                                 A.nbytes(), (int)B, (int)L, &o, st);
     } else if (input_angles.scalar_type() == torch::kDouble) {
         s = tpl_a2b_backward_f64(gradInput.data_ptr<double>(), gradOutput.data_ptr<double>(),
                                  input_angles.data_ptr<double>(), angles_length.data_ptr<int32_t>(), A.data_ptr(),
@@ -105,7 +118,8 @@ int g_bwd_buffers = 0;  // chunk buffers of the coordinate backward: 0 (= 1), 1 
 int g_bwd_scheme = 0;   // 0 (automatic) or 32 = one warp per chain, 4 = one CTA of four warps per chain
 
 void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor gradOutput, torch::Tensor output_coords,
-                                        torch::Tensor angles_length, torch::Tensor A) {
+                                        torch::Tensor angles_length, torch::Tensor A, int64_t residues_per_thread,
+                                        int64_t copy_buffers, int64_t threads_per_cta) {
     check_cuda(gradInput, "gradInput");
     check_cuda(gradOutput, "gradOutput");
     check_cuda(output_coords, "output_coords");
@@ -121,9 +135,9 @@ void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor g
                 "gradOutput and output_coords must hold batch * 9 * max_len values");
     const at::cuda::CUDAGuard guard(gradInput.device());
     tpl_options o = g_opt;
-    o.residues_per_thread = g_bwd_rpt;
-    o.copy_buffers = g_bwd_buffers;
-    o.threads_per_cta = g_bwd_scheme;
+    o.residues_per_thread = residues_per_thread >= 0 ? (int)residues_per_thread : g_bwd_rpt;
+    o.copy_buffers = copy_buffers >= 0 ? (int)copy_buffers : g_bwd_buffers;
+    o.threads_per_cta = threads_per_cta >= 0 ? (int)threads_per_cta : g_bwd_scheme;
     const int s = tpl_a2b_backward_coords_f32(gradInput.data_ptr<float>(), gradOutput.data_ptr<float>(),
                                               output_coords.data_ptr<float>(), angles_length.data_ptr<int32_t>(),
                                               A.data_ptr(), A.nbytes(), (int)B, (int)L, &o, stream_of(gradInput));
@@ -150,7 +164,9 @@ void no_cpu_path_bwd(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor,
     TORCH_CHECK(false, "Angles2Backbone: this build has no CPU path; move the tensors to a CUDA device");
 }
 
-int64_t workspace_bytes(int64_t B, int64_t L) { return (int64_t)ws_bytes(B, L); }
+int64_t workspace_bytes(int64_t B, int64_t L, int64_t residues_per_thread, int64_t threads_per_cta) {
+    return (int64_t)ws_bytes(B, L, call_options(residues_per_thread, threads_per_cta));
+}
 
 int64_t workspace_status(torch::Tensor A) {
     check_cuda(A, "A");
@@ -185,18 +201,25 @@ std::vector<int64_t> get_options() {
 }  // namespace
 
 PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
-    m.def("Angles2BackboneGPU_forward", &Angles2BackboneGPU_forward, "Angles2Backbone gpu forward");
-    m.def("Angles2BackboneGPU_backward", &Angles2BackboneGPU_backward, "Angles2Backbone gpu backward");
+    m.def("Angles2BackboneGPU_forward", &Angles2BackboneGPU_forward, "Angles2Backbone gpu forward",
+          py::arg("input_angles"), py::arg("output_coords"), py::arg("angles_length"), py::arg("A"),
+          py::arg("residues_per_thread") = -1, py::arg("threads_per_cta") = -1);
+    m.def("Angles2BackboneGPU_backward", &Angles2BackboneGPU_backward, "Angles2Backbone gpu backward",
+          py::arg("gradInput"), py::arg("gradOutput"), py::arg("input_angles"), py::arg("angles_length"), py::arg("A"),
+          py::arg("dr_dangle"), py::arg("residues_per_thread") = -1, py::arg("threads_per_cta") = -1);
     m.def("Angles2BackboneCPU_forward", &no_cpu_path, "not available: no CPU path");
     m.def("Angles2BackboneCPU_backward", &no_cpu_path_bwd, "not available: no CPU path");
-    m.def("workspace_bytes", &workspace_bytes, "bytes of the A workspace for (batch, max_len)");
+    m.def("workspace_bytes", &workspace_bytes, "bytes of the A workspace for (batch, max_len)", py::arg("batch"),
+          py::arg("max_len"), py::arg("residues_per_thread") = -1, py::arg("threads_per_cta") = -1);
     m.def("workspace_status", &workspace_status, "synchronise and read the first device-detected error");
     m.def("set_options", &set_options, "tuning knobs", py::arg("residues_per_thread") = 0,
           py::arg("fp64_carry_min_len") = 0, py::arg("renormalize") = 0, py::arg("max_ctas") = 0,
           py::arg("threads_per_cta") = 0);
     m.def("get_options", &get_options, "current tuning knobs");
     m.def("Angles2BackboneGPU_backward_coords", &Angles2BackboneGPU_backward_coords,
-          "float32 backward from the forward's output coordinates");
+          "float32 backward from the forward's output coordinates", py::arg("gradInput"), py::arg("gradOutput"),
+          py::arg("output_coords"), py::arg("angles_length"), py::arg("A"), py::arg("residues_per_thread") = -1,
+          py::arg("copy_buffers") = -1, py::arg("threads_per_cta") = -1);
     m.def("set_backward_options", &set_backward_options,
           "residues per lane, chunk buffers and scheme of the coordinate backward",
           py::arg("residues_per_thread") = 0, py::arg("copy_buffers") = 0, py::arg("threads_per_cta") = 0);

@@ -56,6 +56,7 @@ struct ChainArgs {
     int B, L, nrec;
     int renorm;
     int vec;  // rows are 16-byte aligned (L % 4 == 0, aligned bases): float4 accesses
+    int fp64_min;  // four-warp forward: chains at least this long hand the chain frame on in FP64 (0 = never)
     BondConsts bc;
 };
 
@@ -925,6 +926,30 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, coords_min_blocks(C, NB)) a
 // arrivals always match the syncs.
 
 constexpr int kRingWarps = 4;
+
+// FP64 carry of the four-warp forward: the chain frame at the start of chunk k + 1 is
+// F_k o T_k with F_k the FP64 frame of slot `in` (identity when null) and T_k the
+// FP32 chunk total.  Lanes 0..11 each compute one entry (rotation row-major, then
+// the translation) with three FP64 fused multiply-adds and write it to slot `out`.
+__device__ __forceinline__ void carry_f64(const double *in, const PairFrame &tot, double *out, int lane) {
+    if (lane < 12) {
+        Frame<float> t;
+        from_pair(tot, t);
+        const int r = lane < 9 ? lane / 3 : lane - 9;  // output row
+        double f[4];                                    // row r of F: rotation, translation
+#pragma unroll
+        for (int j = 0; j < 3; j++) f[j] = in ? in[3 * r + j] : (j == r ? 1.0 : 0.0);
+        f[3] = in ? in[9 + r] : 0.0;
+        double v;
+        if (lane < 9) {
+            const int c = lane % 3;
+            v = fma(f[0], (double)t.r[c], fma(f[1], (double)t.r[3 + c], f[2] * (double)t.r[6 + c]));
+        } else {
+            v = fma(f[0], (double)t.p[0], fma(f[1], (double)t.p[1], fma(f[2], (double)t.p[2], f[3])));
+        }
+        out[lane] = v;
+    }
+}
 // 6 CTAs of 9.3 KB staging per warp (C = 8) or 7 (C = 4) fit an SM's shared memory
 constexpr int ring_fwd_min_blocks(int C) { return C >= 8 ? 6 : 7; }
 
@@ -933,6 +958,9 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
     constexpr int CH = 32 * C;
     extern __shared__ __align__(16) float s_dyn[];
     __shared__ __align__(16) float s_ring[kRingWarps][12];
+    // FP64 carries, after the staging buffers: the launch adds their 384 bytes only
+    // when fp64_min is set, so that the FP32 default keeps six CTAs per SM
+    double(*s_ring64)[12] = reinterpret_cast<double(*)[12]>(s_dyn + kRingWarps * FwdStage<C>::FLOATS);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;  // one CTA per chain: the grid is the batch
     float *stage = s_dyn + w * FwdStage<C>::FLOATS;
@@ -943,6 +971,9 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
     ChainRecord *rec = a.rec + (size_t)b * a.nrec;
     const bool vec = a.vec != 0;
     const int nchunk = (a.L + CH - 1) / CH;
+    // chains at least fp64_min long hand the chain frame on in FP64 (the same for the
+    // whole CTA, so every warp takes the same branch at every handoff)
+    const bool carry64 = a.fp64_min > 0 && len >= a.fp64_min;
 
 #pragma unroll 1
     for (int k = w; k < nchunk; k += kRingWarps) {
@@ -956,12 +987,16 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
         PairFrame F = pair_identity();  // chain frame at the chunk start
         if (k > 0) {
             ring_wait(k);
-            F = pair_load(s_ring[k & 3]);
+            F = carry64 ? pair_load(s_ring64[k & 3]) : pair_load(s_ring[k & 3]);
         }
         if (k + 1 < nchunk) {
-            PairFrame Fn = compose_pair(F, tot);
-            if (a.renorm) renormalize_pair(Fn);
-            if (lane == 0) pair_store(s_ring[(k + 1) & 3], Fn);
+            if (carry64) {
+                carry_f64(k > 0 ? s_ring64[k & 3] : nullptr, tot, s_ring64[(k + 1) & 3], lane);
+            } else {
+                PairFrame Fn = compose_pair(F, tot);
+                if (a.renorm) renormalize_pair(Fn);
+                if (lane == 0) pair_store(s_ring[(k + 1) & 3], Fn);
+            }
             ring_signal(k + 1);
         }
         float *dst = out + (size_t)9 * s0;
@@ -1261,6 +1296,7 @@ ChainArgs chain_args(const float *angles, const int32_t *lengths, void *ws, int 
     a.L = L;
     a.nrec = (L + kRecordStride - 1) / kRecordStride;
     a.renorm = opt.renormalize >= 0 ? 1 : 0;
+    a.fp64_min = opt.fp64_carry_min_len > 0 ? opt.fp64_carry_min_len : 0;
     a.bc = bond_constants();
     return a;
 }
@@ -1296,12 +1332,13 @@ int a2b_forward_chain(const float *angles, const int32_t *lengths, float *coords
     a.vec = (L % 4 == 0) && aligned16(angles) && aligned16(coords);
     const int C = opt.residues_per_thread > 0 ? opt.residues_per_thread : 8;
     const bool ring = opt.threads_per_cta == kRingWarps;
+    const int carry_bytes = a.fp64_min > 0 ? kRingWarps * 12 * (int)sizeof(double) : 0;  // FP64 carry slots
     switch (C) {
         case 4:
-            return ring ? launch_ring(a2b_fwd_ring_kernel<4>, fwd_smem<4>(), B, a, st)
+            return ring ? launch_ring(a2b_fwd_ring_kernel<4>, fwd_smem<4>() + carry_bytes, B, a, st)
                         : launch_chain(a2b_fwd_chain_kernel<4>, fwd_smem<4>(), B, a, st);
         case 8:
-            return ring ? launch_ring(a2b_fwd_ring_kernel<8>, fwd_smem<8>(), B, a, st)
+            return ring ? launch_ring(a2b_fwd_ring_kernel<8>, fwd_smem<8>() + carry_bytes, B, a, st)
                         : launch_chain(a2b_fwd_chain_kernel<8>, fwd_smem<8>(), B, a, st);
     }
     return TPL_ERR_UNSUPPORTED;

@@ -127,7 +127,8 @@ __device__ __forceinline__ void pair_store(float *dst, const PairFrame &g) {
     frame_store(dst, f);
 }
 
-__device__ __forceinline__ PairFrame pair_load(const float *src) {
+template <typename S>  // float, or double rounded to FP32
+__device__ __forceinline__ PairFrame pair_load(const S *src) {
     Frame<float> f;
     frame_load(f, src);
     return to_pair(f);
