@@ -377,8 +377,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_
         }
         const int j0 = s0 + C * lane;
         PairFrame tot;
+        // lane transforms compose 3C joints: no renormalisation before the scan (the
+        // chain frame carried from chunk to chunk is renormalised)
         const PairFrame E = warp_exclusive_total_pair(to_pair(walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg)),
-                                                      lane, a.renorm, tot);
+                                                      lane, false, tot);
         // E composes at most 31 renormalised lane transforms: P needs no renormalisation
         const PairFrame P = compose_pair(F, E);
         if ((C * lane) % kRecordStride == 0 && j0 < len) pair_store(rec[j0 / kRecordStride].f, P);
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, bwd_min_blocks(C)) a2b_bwd_
         stage_chunk<SEG, SP>(sg, gin + (size_t)9 * s0, 9 * nreal, lane, vec);
         const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, xs);
         Frame<float> tot;
-        const Frame<float> E = warp_exclusive_total(t, lane, a.renorm, tot);
+        const Frame<float> E = warp_exclusive_total(t, lane, false, tot);  // as the forward's scan
         F.p[0] = F.p[1] = F.p[2] = 0.f;  // lane frames relative to the chunk origin
         Frame<float> P = compose(F, E);
         if (a.renorm) renormalize(P);
@@ -982,8 +984,9 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
         const bool live = s0 < len;
         const int j0 = s0 + C * lane;
         PairFrame E = pair_identity(), tot = pair_identity();
-        if (live) E = warp_exclusive_total_pair(to_pair(walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg)), lane,
-                                                a.renorm, tot);
+        if (live)  // no renormalisation of the lane transforms (3C joints each), as in a2b_fwd_chain_kernel
+            E = warp_exclusive_total_pair(to_pair(walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg)), lane, false,
+                                          tot);
         PairFrame F = pair_identity();  // chain frame at the chunk start
         if (k > 0) {
             ring_wait(k);

@@ -303,18 +303,20 @@ __device__ __forceinline__ void residue_atoms_pair(const Topology<float> &tp, in
     if (nj > 0) {
         PairFrame S = F;
         apply_rx_pair(S, tp.dummy_c, tp.dummy_s);
-        for (int k = 0; k < nj; k++) {
-            const int chi = tp.jchi[ty][k];
-            float c = 1.f, s = 0.f;
+        // unrolled over the joints: joint k reads chi angle k or none (Ala's fixed
+        // alpha; topology_layout_ok), so the angle is a register, not a select
 #pragma unroll
-            for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
-                if (chi == q) {
-                    c = chi_c[q];
-                    s = chi_s[q];
-                }
-            apply_joint_pair(S, tp.jcb[ty][k], tp.jsb[ty][k], tp.jd[ty][k], c, s);
+        for (int k = 0; k < kMaxScJoints; k++) {
+            if (k >= nj) break;
+            const bool fixed = tp.jchi[ty][k] < 0;
+            apply_joint_pair(S, tp.jcb[ty][k], tp.jsb[ty][k], tp.jd[ty][k], fixed ? 1.f : chi_c[k],
+                             fixed ? 0.f : chi_s[k]);
             const int f0 = tp.jfirst[ty][k];
-            for (int a = 0; a < tp.jna[ty][k]; a++) {
+            {  // the group's first atom sits at the joint's origin
+                const float x[3] = {S.p.x, S.p.y, S.p2};
+                emit(2 + f0, x);
+            }
+            for (int a = 1; a < tp.jna[ty][k]; a++) {
                 float x[3];
                 pair_point(S, tp.sc[ty][f0 + a][0], tp.sc[ty][f0 + a][1], tp.sc[ty][f0 + a][2], x);
                 emit(2 + f0 + a, x);

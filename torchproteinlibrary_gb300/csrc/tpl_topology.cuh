@@ -68,6 +68,9 @@ struct Topology {
     T dummy_c, dummy_s;               // Rx of the N-C-CA-CB dihedral constant
     T o_local[3];                     // carbonyl O in the C frame
     T pro_local[3][3];                // Pro CB, CG, CD in the CA frame
+    // side-chain atoms past the first of their group (the first sits at the joint's
+    // origin), and the groups that carry such atoms, per residue type
+    int nextra[kResTypes], nframes[kResTypes];
 };
 
 struct TopologyBuilder {
@@ -315,7 +318,14 @@ constexpr Topology<T> make_topology() {
     // atom counts, backbone names
     for (int r = 0; r < kResTypes; r++) {
         int sc = 0;
-        for (int k = 0; k < tp.njoints[r]; k++) sc += tp.jna[r][k];
+        tp.nextra[r] = tp.nframes[r] = 0;
+        for (int k = 0; k < tp.njoints[r]; k++) {
+            sc += tp.jna[r][k];
+            if (tp.jna[r][k] > 1) {
+                tp.nextra[r] += tp.jna[r][k] - 1;
+                tp.nframes[r]++;
+            }
+        }
         if (tp.pro[r]) sc = 3;
         tp.natoms[r] = 4 + sc;
         tp.atom_name[r][0] = pack_name('N');
@@ -342,5 +352,23 @@ constexpr Topology<T> make_topology() {
         for (int c = 0; c < 3; c++) tp.pro_local[a][c] = T(pro[a][c]);
     return tp;
 }
+
+// Facts the chunked Angles2Coords forward relies on: side-chain joint k reads chi
+// angle k (or none: alpha fixed at 0, Ala), every group's first atom sits at its
+// joint's origin, and at most two groups per residue carry further atoms.
+constexpr bool topology_layout_ok() {
+    const Topology<double> tp = make_topology<double>();
+    for (int t = 0; t < kResTypes; t++) {
+        if (tp.nframes[t] > 2) return false;
+        for (int k = 0; k < tp.njoints[t]; k++) {
+            if (tp.jchi[t][k] != k && tp.jchi[t][k] != -1) return false;
+            const int f0 = tp.jfirst[t][k];
+            if (tp.jna[t][k] < 1 || tp.sc[t][f0][0] != 0.0 || tp.sc[t][f0][1] != 0.0 || tp.sc[t][f0][2] != 0.0)
+                return false;
+        }
+    }
+    return true;
+}
+static_assert(topology_layout_ok(), "side-chain layout assumed by the chunked forward");
 
 }  // namespace tpl
