@@ -405,3 +405,33 @@ def test_backward_from_coordinates_c_abi_and_layer(fm, built):
     np.testing.assert_array_equal(grads[False, False], gi)
     scale = max(1.0, np.abs(grads[False, True]).max())
     assert np.abs(grads[True, False] - grads[False, True]).max() <= GRAD_TOL_F32 * scale
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_cpp_autograd_path_matches_python_function(built, dtype):
+    """The Angles2Coords and Coords2RMSD modules run the extensions' C++ autograd
+    functions; their outputs and gradients equal those of the Python autograd
+    functions (Angles2CoordsFunction, _Coords2RMSDCentering) bit for bit, since both
+    call the same entry points."""
+    from torchproteinlibrary_gb300.FullAtomModel import Angles2Coords
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import Angles2CoordsFunction
+    from torchproteinlibrary_gb300.RMSD import Coords2RMSD
+    from torchproteinlibrary_gb300.RMSD.Coords2RMSD.Coords2RMSD import _Coords2RMSDCentering
+    rng = np.random.default_rng(12)
+    seqs = ["".join(rng.choice(list(AA), n)) for n in (40, 17, 33)]
+    dev = torch.device("cuda")
+    ang = rng.uniform(-np.pi, np.pi, (3, 8, 40))
+    layer = Angles2Coords()
+    x1 = torch.tensor(ang, dtype=dtype, device=dev, requires_grad=True)
+    c1, r1, a1, n1 = layer(x1, seqs)
+    tgt = (c1.detach() + 0.5 * torch.randn_like(c1)).contiguous()
+    loss1 = Coords2RMSD()(c1, tgt, n1).sum()
+    loss1.backward()
+    x2 = torch.tensor(ang, dtype=dtype, device=dev, requires_grad=True)
+    seq, num_atoms, _ = layer._prepare(seqs, dev)
+    c2, r2, a2, n2 = Angles2CoordsFunction.apply(x2, seq, num_atoms)
+    rmsd2, _ = _Coords2RMSDCentering.apply(c2, tgt, n2)
+    rmsd2.sum().backward()
+    assert torch.equal(c1, c2) and torch.equal(r1, r2) and torch.equal(a1, a2)
+    assert torch.equal(loss1.detach(), rmsd2.sum().detach())
+    assert torch.equal(x1.grad, x2.grad)

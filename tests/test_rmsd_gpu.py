@@ -79,3 +79,21 @@ def test_gradcheck_and_function_api(built):
     r1, UT = Coords2RMSDFunction.apply(xc, yc, n)
     r2 = Coords2RMSD()(x.detach(), y, n)
     assert torch.allclose(r1, r2, rtol=1e-9)
+
+
+def test_host_num_atoms_reused_and_refreshed(built):
+    """A host num_atoms tensor is copied to the device once and reused on later calls;
+    changing it in place makes the next call copy the new counts."""
+    from torchproteinlibrary_gb300.RMSD import Coords2RMSD
+    src, dst, na = case(B=4, N=50, seed=3)
+    layer = Coords2RMSD()
+    x = torch.tensor(src, device="cuda")
+    y = torch.tensor(dst, device="cuda")
+    n = torch.tensor(na, dtype=torch.int32)
+    r1 = layer(x, y, n)
+    r2 = layer(x, y, n)
+    assert torch.equal(r1, r2)
+    n[0] = 3
+    r3 = layer(x, y, n)
+    ref, _, _ = oracle.rmsd(src, dst, n.numpy())
+    assert np.allclose(r3.cpu().numpy(), ref, rtol=1e-9, atol=0)

@@ -46,6 +46,10 @@ def convertString(string):
     return torch.tensor(list(string.encode("ascii")) + [0], dtype=torch.uint8)
 
 
+def _check_nan_enabled():
+    return os.environ.get("TPL_CHECK_NAN", "0") == "1"
+
+
 def _check(t, where, device):
     if os.environ.get("TPL_CHECK_NAN", "0") == "1":
         status = _FullAtomModel.workspace_status(device.index if device.index is not None else 0)
@@ -118,5 +122,11 @@ class Angles2Coords(Module):
         if not input_angles_cpu.is_cuda:
             raise RuntimeError("Angles2Coords: this build has no CPU path; move the angles to a CUDA device")
         seq, num_atoms, counts = self._prepare(sequences, input_angles_cpu.device)
-        self.num_atoms = list(counts)
-        return Angles2CoordsFunction.apply(input_angles_cpu, seq, num_atoms)
+        self.num_atoms = counts
+        if not Angles2CoordsFunction.backward_from_coords or _check_nan_enabled():
+            return Angles2CoordsFunction.apply(input_angles_cpu, seq, num_atoms)
+        # the same entries as Angles2CoordsFunction, through the extension's C++ autograd
+        # function: no Python frame in the backward, less host time per call
+        coords, res_names, atom_names = _FullAtomModel.angles2coords_autograd(input_angles_cpu, seq,
+                                                                               num_atoms._tpl_max_atoms, True)
+        return coords, res_names, atom_names, num_atoms

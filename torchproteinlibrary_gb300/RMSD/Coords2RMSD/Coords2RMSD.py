@@ -14,7 +14,6 @@ TPL_CHECK_NAN=1.
 """
 import math
 import os
-import weakref
 
 import torch
 from torch.autograd import Function
@@ -25,21 +24,18 @@ from ... import load_extension
 _RMSD = load_extension("_RMSD")
 
 
-# device int32 copies of host num_atoms tensors, reused while the host tensor is
-# unchanged (its version counter), so that repeated calls with the same counts make
-# no host-to-device copy
-_NA_ON_DEVICE: "weakref.WeakKeyDictionary" = weakref.WeakKeyDictionary()
-
-
 def _na(num_atoms, device):
+    """num_atoms as int32 on `device`.  A host tensor's device copy is kept on the
+    tensor itself and reused while the tensor is unchanged (its version counter), so
+    repeated calls with the same counts make no host-to-device copy."""
     if num_atoms.device == device:
         return num_atoms.to(dtype=torch.int32).contiguous()
-    hit = _NA_ON_DEVICE.get(num_atoms)
+    hit = getattr(num_atoms, "_tpl_on_device", None)
     if hit is not None and hit[0] == num_atoms._version and hit[1].device == device:
         return hit[1]
     na = num_atoms.to(device=device, dtype=torch.int32).contiguous()
     if not torch.cuda.is_current_stream_capturing():
-        _NA_ON_DEVICE[num_atoms] = (num_atoms._version, na)
+        num_atoms._tpl_on_device = (num_atoms._version, na)
     return na
 
 
@@ -114,5 +110,10 @@ class Coords2RMSD(Module):
     def forward(self, input, target, num_atoms):
         if not input.is_cuda:
             raise RuntimeError("Coords2RMSD: this build has no CPU path; move the tensors to a CUDA device")
-        rmsd, self.UT = _Coords2RMSDCentering.apply(input, target, num_atoms)
+        if os.environ.get("TPL_CHECK_NAN", "0") == "1":
+            rmsd, self.UT = _Coords2RMSDCentering.apply(input, target, num_atoms)
+            return rmsd
+        # the same entries as _Coords2RMSDCentering through the extension's C++ autograd
+        # function: no Python frame in the backward
+        rmsd, self.UT = _RMSD.coords2rmsd_autograd(input, target, _na(num_atoms, input.device))
         return rmsd

@@ -176,6 +176,45 @@ void Angles2Coords_backward_coords(torch::Tensor grad_atoms, torch::Tensor grad_
     check_status(s, "Angles2Coords_backward_coords");
 }
 
+// The Angles2Coords autograd function in C++: the same forward and backward entries
+// as the Python Angles2CoordsFunction, with the autograd engine calling the backward
+// without a Python frame.  The float32 path saves its output coordinates and its
+// backward reads every joint from them; float64 rebuilds the tree.
+struct Angles2CoordsAutograd : public torch::autograd::Function<Angles2CoordsAutograd> {
+    static torch::autograd::variable_list forward(torch::autograd::AutogradContext *ctx, torch::Tensor angles,
+                                                  torch::Tensor sequences, int64_t max_atoms, bool names) {
+        auto x = angles.contiguous();
+        const int64_t B = x.size(0);
+        auto coords = torch::empty({B, 3 * max_atoms}, x.options());
+        auto byte = x.options().dtype(torch::kByte);
+        auto rn = names ? torch::empty({B, max_atoms, 4}, byte) : torch::empty({0}, byte);
+        auto an = names ? torch::empty({B, max_atoms, 4}, byte) : torch::empty({0}, byte);
+        Angles2Coords_forward(sequences, x, coords, rn, an);
+        const bool from_coords = x.scalar_type() == torch::kFloat;
+        ctx->saved_data["from_coords"] = from_coords;
+        ctx->save_for_backward({x, sequences, from_coords ? coords : torch::Tensor()});
+        ctx->mark_non_differentiable({rn, an});
+        return {coords, rn, an};
+    }
+    static torch::autograd::variable_list backward(torch::autograd::AutogradContext *ctx,
+                                                   torch::autograd::variable_list grads) {
+        auto saved = ctx->get_saved_variables();
+        auto g = grads[0].contiguous();
+        auto grad_angles = torch::empty_like(saved[0]);
+        if (ctx->saved_data["from_coords"].toBool())
+            Angles2Coords_backward_coords(g, grad_angles, saved[1], saved[2]);
+        else
+            Angles2Coords_backward(g, grad_angles, saved[1], saved[0]);
+        return {grad_angles, torch::Tensor(), torch::Tensor(), torch::Tensor()};
+    }
+};
+
+std::vector<torch::Tensor> angles2coords_autograd(torch::Tensor angles, torch::Tensor sequences, int64_t max_atoms,
+                                                  bool names) {
+    TORCH_CHECK(angles.is_cuda(), "Angles2Coords: this build has no CPU path; move the angles to a CUDA device");
+    return Angles2CoordsAutograd::apply(angles, sequences, max_atoms, names);
+}
+
 int64_t getSeqNumAtoms(const std::string &sequence) {
     int n = tpl_num_atoms(sequence.c_str());
     TORCH_CHECK(n >= 0, "Unknown atom/res names in sequence '", sequence, "'");
@@ -586,5 +625,7 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
           "float32 Angles2Coords backward from the forward's output coordinates");
     m.def("Angles2Coords_save", &Angles2Coords_save, "Angles2Coords save");
     m.def("getSeqNumAtoms", &getSeqNumAtoms, "Get number of atoms in a sequence");
+    m.def("angles2coords_autograd", &angles2coords_autograd,
+          "Angles2Coords forward as a C++ autograd function: (coords, res_names, atom_names)");
     m.def("workspace_status", &workspace_status, "synchronise and read the first device-detected error");
 }

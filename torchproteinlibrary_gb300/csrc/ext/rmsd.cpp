@@ -89,6 +89,36 @@ void Coords2RMSDGPU_backward(torch::Tensor grad_rmsd, torch::Tensor src, torch::
     check_status(s, "Coords2RMSD backward");
 }
 
+// Coords2RMSD with the centring folded in, as a C++ autograd function (the same
+// entries as the Python _Coords2RMSDCentering, without a Python frame in the
+// backward).  num_atoms: int32 on the coordinates' device.
+struct Coords2RMSDAutograd : public torch::autograd::Function<Coords2RMSDAutograd> {
+    static torch::autograd::variable_list forward(torch::autograd::AutogradContext *ctx, torch::Tensor input,
+                                                  torch::Tensor target, torch::Tensor num_atoms) {
+        auto x = input.contiguous(), y = target.contiguous();
+        const int64_t B = x.size(0);
+        auto output = torch::empty({B}, x.options());
+        auto UT = torch::empty({B, 3, 3}, x.options());
+        auto cent = torch::empty({B, 6}, x.options().dtype(torch::kDouble));
+        forward_impl(x, y, output, num_atoms, UT, cent, 1);
+        ctx->save_for_backward({output, num_atoms, UT, x, y, cent});
+        ctx->mark_non_differentiable({UT});
+        return {output, UT};
+    }
+    static torch::autograd::variable_list backward(torch::autograd::AutogradContext *ctx,
+                                                   torch::autograd::variable_list grads) {
+        auto s = ctx->get_saved_variables();
+        auto grad = torch::empty_like(s[3]);
+        Coords2RMSDGPU_backward(grads[0], s[3], s[4], s[1], s[0], s[2], s[5], grad, 1);
+        return {grad, torch::Tensor(), torch::Tensor()};
+    }
+};
+
+std::vector<torch::Tensor> coords2rmsd_autograd(torch::Tensor input, torch::Tensor target, torch::Tensor num_atoms) {
+    TORCH_CHECK(input.is_cuda(), "Coords2RMSD: this build has no CPU path; move the tensors to a CUDA device");
+    return Coords2RMSDAutograd::apply(input, target, num_atoms);
+}
+
 void no_cpu_path(torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor, torch::Tensor) {
     TORCH_CHECK(false, "Coords2RMSD: this build has no CPU path; move the tensors to a CUDA device");
 }
@@ -101,4 +131,6 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("Coords2RMSDGPU_forward_centering", &Coords2RMSDGPU_forward_centering,
           "Coords2RMSD gpu forward with the centring folded in");
     m.def("Coords2RMSDGPU_backward", &Coords2RMSDGPU_backward, "Coords2RMSD gpu backward");
+    m.def("coords2rmsd_autograd", &coords2rmsd_autograd,
+          "Coords2RMSD with centring as a C++ autograd function: (rmsd, UT)");
 }

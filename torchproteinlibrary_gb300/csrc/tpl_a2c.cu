@@ -1093,19 +1093,19 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
             const int nj = tp.njoints[ty];
             if (nj == 0)
                 for (int q = 2; q < na - 2; q++) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);  // Pro ring (none for Gly)
-            for (int kk = nj - 1; kk >= 0; kk--) {
+            // unrolled over the joints: joint kk reads chi angle kk or none (Ala;
+            // topology_layout_ok), so its gradient goes to a register, not a select
+#pragma unroll
+            for (int kk = kMaxScJoints - 1; kk >= 0; kk--) {
+                if (kk >= nj) continue;
                 const int f0 = 2 + tp.jfirst[ty][kk], f1 = f0 + tp.jna[ty][kk];
                 for (int q = f1 - 1; q >= f0; q--) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);
-                const int chi = tp.jchi[ty][kk];
-                if (chi >= 0) {
+                if (tp.jchi[ty][kk] >= 0) {
                     const float *pk = X + 3 * f0;
                     const float *pp = kk == 0 ? X + 3 : X + 3 * (2 + tp.jfirst[ty][kk - 1]);
                     const float ok_[3] = {pk[0] - o[0], pk[1] - o[1], pk[2] - o[2]};
                     const float op_[3] = {pp[0] - o[0], pp[1] - o[1], pp[2] - o[2]};
-                    const float gk = joint_grad(ok_, op_, 1.f / tp.jd[ty][kk], Gs, Ss);
-#pragma unroll
-                    for (int q = 0; q < 5; q++)  // register selects: a dynamic index would go to local memory
-                        if (chi == q) gr[3 + q] = gk;
+                    gr[3 + kk] = joint_grad(ok_, op_, 1.f / tp.jd[ty][kk], Gs, Ss);
                 }
             }
 #pragma unroll
