@@ -634,3 +634,35 @@ def test_layer_runs_the_tuned_options(rm):
     rm.Angles2BackboneGPU_backward_coords(g2, gt, c2, ln, ws, *bwd)
     assert torch.equal(c.detach(), c2)
     assert torch.equal(a.grad, g2)
+
+
+def test_layer_uses_cpp_autograd_function(rm):
+    """The float32 layer records the extension's C++ autograd node (no Python frame
+    in the backward); float64 and the recomputing backward keep the Python function.
+    Both float32 routes give the same coordinates and the same gradient within the
+    float32 tolerance."""
+    from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+    from torchproteinlibrary_gb300.ReducedModel.Angles2Backbone.Angles2Backbone import Angles2BackboneGPUFunction
+    dev = torch.device("cuda")
+    B, L = 6, 90
+    ang, lengths, g = make_case(B, L, 41)
+    ln = torch.tensor(lengths, device=dev)
+    gt = torch.tensor(g, dtype=torch.float32, device=dev)
+    layer = Angles2Backbone()
+    x = torch.tensor(ang, dtype=torch.float32, device=dev, requires_grad=True)
+    out = layer(x, ln)
+    assert "Angles2BackboneAutograd" in out.grad_fn.name()
+    out.backward(gt)
+    Angles2BackboneGPUFunction.backward_from_coords = False
+    try:
+        x2 = torch.tensor(ang, dtype=torch.float32, device=dev, requires_grad=True)
+        out2 = layer(x2, ln)
+        assert "Angles2BackboneGPUFunction" in out2.grad_fn.name()
+        out2.backward(gt)
+    finally:
+        Angles2BackboneGPUFunction.backward_from_coords = True
+    assert torch.equal(out.detach(), out2.detach())
+    scale = x2.grad.abs().max().item()
+    assert (x.grad - x2.grad).abs().max().item() <= GRAD_TOL_F32 * scale
+    x64 = torch.tensor(ang, dtype=torch.float64, device=dev, requires_grad=True)
+    assert "Angles2BackboneGPUFunction" in layer(x64, ln).grad_fn.name()

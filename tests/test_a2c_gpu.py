@@ -424,8 +424,11 @@ def test_cpp_autograd_path_matches_python_function(built, dtype):
     layer = Angles2Coords()
     x1 = torch.tensor(ang, dtype=dtype, device=dev, requires_grad=True)
     c1, r1, a1, n1 = layer(x1, seqs)
+    assert "Angles2CoordsAutograd" in c1.grad_fn.name()
     tgt = (c1.detach() + 0.5 * torch.randn_like(c1)).contiguous()
-    loss1 = Coords2RMSD()(c1, tgt, n1).sum()
+    rmsd1 = Coords2RMSD()(c1, tgt, n1)
+    assert "Coords2RMSDAutograd" in rmsd1.grad_fn.name()
+    loss1 = rmsd1.sum()
     loss1.backward()
     x2 = torch.tensor(ang, dtype=dtype, device=dev, requires_grad=True)
     seq, num_atoms, _ = layer._prepare(seqs, dev)

@@ -141,4 +141,15 @@ class Angles2Backbone(Module):
     def forward(self, input, angles_length):
         if not input.is_cuda:
             raise RuntimeError("Angles2Backbone: this build has no CPU path; move the tensors to a CUDA device")
-        return Angles2BackboneGPUFunction.apply(input, angles_length)
+        if (input.dtype != torch.float32 or input.dim() != 3 or not Angles2BackboneGPUFunction.backward_from_coords
+                or os.environ.get("TPL_CHECK_NAN", "0") == "1"):
+            return Angles2BackboneGPUFunction.apply(input, angles_length)
+        # the float32 path of Angles2BackboneGPUFunction (the same kernels, options and
+        # shared workspace) through the extension's C++ autograd function: no Python
+        # frame in the backward
+        batch_size, _, max_len = input.shape
+        dev = input.device
+        tuned = autotune.options_for(dev, batch_size, max_len)
+        fwd_opts, bwd_opts = tuned if tuned is not None else ((-1, -1), (-1, -1, -1))
+        ws = _shared_workspace(batch_size, max_len, dev, fwd_opts)
+        return _ReducedModel.angles2backbone_autograd(input, angles_length, ws, list(fwd_opts), list(bwd_opts))

@@ -194,10 +194,13 @@ struct Angles2CoordsAutograd : public torch::autograd::Function<Angles2CoordsAut
         ctx->saved_data["from_coords"] = from_coords;
         ctx->save_for_backward({x, sequences, from_coords ? coords : torch::Tensor()});
         ctx->mark_non_differentiable({rn, an});
+        // no zero-filled gradients for the name outputs (two fill kernels per call)
+        ctx->set_materialize_grads(false);
         return {coords, rn, an};
     }
     static torch::autograd::variable_list backward(torch::autograd::AutogradContext *ctx,
                                                    torch::autograd::variable_list grads) {
+        if (!grads[0].defined()) return {torch::Tensor(), torch::Tensor(), torch::Tensor(), torch::Tensor()};
         auto saved = ctx->get_saved_variables();
         auto g = grads[0].contiguous();
         auto grad_angles = torch::empty_like(saved[0]);

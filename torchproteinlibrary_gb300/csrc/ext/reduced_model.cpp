@@ -144,6 +144,42 @@ void Angles2BackboneGPU_backward_coords(torch::Tensor gradInput, torch::Tensor g
     check_status(s, "Angles2BackboneGPU_backward_coords");
 }
 
+// The float32 Angles2Backbone autograd function in C++ (forward, then the backward
+// from the coordinates it returned), so that the autograd engine calls the backward
+// without a Python frame.  The caller passes the workspace and the per-call options
+// (the layer's autotuned choice; -1 = the module-wide ones).
+struct Angles2BackboneAutograd : public torch::autograd::Function<Angles2BackboneAutograd> {
+    static torch::Tensor forward(torch::autograd::AutogradContext *ctx, torch::Tensor angles, torch::Tensor lengths,
+                                 torch::Tensor A, std::vector<int64_t> fwd_opts, std::vector<int64_t> bwd_opts) {
+        TORCH_CHECK(fwd_opts.size() == 2 && bwd_opts.size() == 3,
+                    "fwd_opts = (residues_per_thread, threads_per_cta), bwd_opts = (residues_per_thread, "
+                    "copy_buffers, threads_per_cta)");
+        TORCH_CHECK(angles.scalar_type() == torch::kFloat, "the C++ Angles2Backbone function is float32");
+        auto x = angles.contiguous();
+        TORCH_CHECK(x.dim() == 3, "input_angles must be [batch, 3, max_len]");
+        auto coords = torch::empty({x.size(0), 9 * x.size(2)}, x.options());
+        Angles2BackboneGPU_forward(x, coords, lengths, A, fwd_opts[0], fwd_opts[1]);
+        ctx->saved_data["bwd_opts"] = c10::IValue(bwd_opts);
+        ctx->saved_data["angles_shape"] = c10::IValue(x.sizes().vec());
+        ctx->save_for_backward({lengths, coords, A});
+        return coords;
+    }
+    static torch::autograd::variable_list backward(torch::autograd::AutogradContext *ctx,
+                                                   torch::autograd::variable_list grads) {
+        auto s = ctx->get_saved_variables();
+        const auto o = ctx->saved_data["bwd_opts"].toIntVector();
+        auto g = grads[0].contiguous();
+        auto grad = torch::empty(ctx->saved_data["angles_shape"].toIntVector(), g.options());
+        Angles2BackboneGPU_backward_coords(grad, g, s[1], s[0], s[2], o[0], o[1], o[2]);
+        return {grad, torch::Tensor(), torch::Tensor(), torch::Tensor(), torch::Tensor()};
+    }
+};
+
+torch::Tensor angles2backbone_autograd(torch::Tensor angles, torch::Tensor lengths, torch::Tensor A,
+                                       std::vector<int64_t> fwd_opts, std::vector<int64_t> bwd_opts) {
+    return Angles2BackboneAutograd::apply(angles, lengths, A, fwd_opts, bwd_opts);
+}
+
 void set_backward_options(int64_t residues_per_thread, int64_t copy_buffers, int64_t threads_per_cta) {
     TORCH_CHECK(residues_per_thread == 0 || residues_per_thread == 4 || residues_per_thread == 8,
                 "residues_per_thread of the coordinate backward must be 0, 4 or 8");
@@ -225,4 +261,7 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
           py::arg("residues_per_thread") = 0, py::arg("copy_buffers") = 0, py::arg("threads_per_cta") = 0);
     m.def("get_backward_options", []() { return std::vector<int64_t>{g_bwd_rpt, g_bwd_buffers, g_bwd_scheme}; },
           "residues per lane, chunk buffers and scheme of the coordinate backward");
+    m.def("angles2backbone_autograd", &angles2backbone_autograd,
+          "float32 Angles2Backbone as a C++ autograd function (backward from the coordinates)", py::arg("angles"),
+          py::arg("lengths"), py::arg("A"), py::arg("fwd_opts"), py::arg("bwd_opts"));
 }

@@ -103,10 +103,13 @@ struct Coords2RMSDAutograd : public torch::autograd::Function<Coords2RMSDAutogra
         forward_impl(x, y, output, num_atoms, UT, cent, 1);
         ctx->save_for_backward({output, num_atoms, UT, x, y, cent});
         ctx->mark_non_differentiable({UT});
+        // no zero-filled gradient for the unused UT output (one fill kernel per call)
+        ctx->set_materialize_grads(false);
         return {output, UT};
     }
     static torch::autograd::variable_list backward(torch::autograd::AutogradContext *ctx,
                                                    torch::autograd::variable_list grads) {
+        if (!grads[0].defined()) return {torch::Tensor(), torch::Tensor(), torch::Tensor()};
         auto s = ctx->get_saved_variables();
         auto grad = torch::empty_like(s[3]);
         Coords2RMSDGPU_backward(grads[0], s[3], s[4], s[1], s[0], s[2], s[5], grad, 1);

@@ -170,7 +170,18 @@ __device__ __noinline__ void walk4_any(const BondConsts &bc, Frame<float> &f, co
     walk4<false>(bc, f, a0, a1, a2, seg);
 }
 
-template <int C>
+// The rare path inline (INL) or as a call.  Inline is faster wherever the registers
+// allow it (GB300, 4096 x 1000: a2b_fwd_chain_kernel<8> 59.3 -> 52.8 us, the ring
+// forwards 3-7 % faster); a2b_fwd_chain_kernel<4> spills with it inline, so it keeps
+// the call.
+template <bool INL>
+__device__ __forceinline__ void walk4_rare(const BondConsts &bc, Frame<float> &f, const float (&a0)[4],
+                                           const float (&a1)[4], const float (&a2)[4], float *seg) {
+    if constexpr (INL) walk4<false>(bc, f, a0, a1, a2, seg);
+    else walk4_any(bc, f, a0, a1, a2, seg);
+}
+
+template <int C, bool INL>
 __device__ __forceinline__ Frame<float> walk_chunk(const BondConsts &bc, const float *ang, int L, int j0, int len,
                                                    bool vec, float *seg) {
     Frame<float> f;
@@ -196,7 +207,72 @@ __device__ __forceinline__ Frame<float> walk_chunk(const BondConsts &bc, const f
 #pragma unroll
         for (int i = 0; i < 4; i++) m = fmaxf(m, fmaxf(fabsf(v0[i]), fmaxf(fabsf(v1[i]), fabsf(v2[i]))));
         if (m <= 1.0e4f) walk4<true>(bc, f, v0, v1, v2, seg + 36 * g);
-        else walk4_any(bc, f, v0, v1, v2, seg + 36 * g);
+        else walk4_rare<INL>(bc, f, v0, v1, v2, seg + 36 * g);
+    }
+    return f;
+}
+
+// Angles of a chunk prefetched into shared memory with cp.async while the warp works
+// on the previous chunk (C = 4 only: the double buffer costs 3 KB per warp, which
+// still lets seven CTAs of four warps share an SM; at C = 8 it would cost a CTA).
+// Lane l copies, and later reads, only its own float4s of the three rows, so no
+// barrier is needed between lanes; a buffer is refilled one chunk after its walk read
+// it, by which time those values have been consumed.  GB300, 4096 x 1000:
+// a2b_fwd_chain_kernel<4> 57.4 -> 55.7 us.
+template <int C>
+struct AngBuf {
+    static constexpr bool ON = C == 4;
+    static constexpr int FLOATS = ON ? 2 * 3 * 32 * C : 0;  // per warp: two chunks of three rows
+};
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Copy the lane's float4s of the chunk starting at s0 (rows phi, psi, omega) into buf
+// (three rows of 32 C floats).  Requires L % 4 == 0 and 16-byte aligned rows.
+template <int C>
+__device__ __forceinline__ void prefetch_angles(float *buf, const float *ang, int L, int s0, int lane) {
+    constexpr int CH = 32 * C;
+#pragma unroll
+    for (int g = 0; g < C / 4; g++) {
+        const int o = C * lane + 4 * g, j = s0 + o;
+        if (j < L) {
+#pragma unroll
+            for (int r = 0; r < 3; r++) cp_async16(buf + r * CH + o, ang + (size_t)r * L + j);
+        }
+    }
+}
+
+// walk_chunk with the angles read from the prefetch buffer (masked as load4 does).
+template <int C, bool INL>
+__device__ __forceinline__ Frame<float> walk_chunk_smem(const BondConsts &bc, const float *buf, int lane, int j0,
+                                                        int len, float *seg) {
+    constexpr int CH = 32 * C;
+    Frame<float> f;
+    frame_identity(f);
+#pragma unroll 1
+    for (int g = 0; g < C / 4; g++) {
+        const int j = j0 + 4 * g, o = C * lane + 4 * g;
+        const float4 x0 = *reinterpret_cast<const float4 *>(buf + o);
+        const float4 x1 = *reinterpret_cast<const float4 *>(buf + CH + o);
+        const float4 x2 = *reinterpret_cast<const float4 *>(buf + 2 * CH + o);
+        float v0[4] = {x0.x, x0.y, x0.z, x0.w}, v1[4] = {x1.x, x1.y, x1.z, x1.w}, v2[4] = {x2.x, x2.y, x2.z, x2.w};
+        if (!(j + 4 < len)) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                v0[i] = j + i < len ? v0[i] : 0.f;
+                v1[i] = j + i < len ? v1[i] : 0.f;
+                v2[i] = j + i < len - 1 ? v2[i] : 0.f;
+            }
+        }
+        float m = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; i++) m = fmaxf(m, fmaxf(fabsf(v0[i]), fmaxf(fabsf(v1[i]), fabsf(v2[i]))));
+        if (m <= 1.0e4f) walk4<true>(bc, f, v0, v1, v2, seg + 36 * g);
+        else walk4_rare<INL>(bc, f, v0, v1, v2, seg + 36 * g);
     }
     return f;
 }
@@ -368,7 +444,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_
     const bool vec = a.vec != 0;
 
     PairFrame F = pair_identity();  // chain frame at the chunk start (world)
-    for (int s0 = 0; s0 < a.L; s0 += CH) {
+    constexpr bool PF = AngBuf<C>::ON;
+    float *abuf = s_dyn + kWarpsPerCta * FwdStage<C>::FLOATS + w * AngBuf<C>::FLOATS;
+    const bool pf = PF && vec;
+    if (pf) {
+        if (len > 0) prefetch_angles<C>(abuf, ang, a.L, 0, lane);
+        cp_async_commit();
+    }
+    int it = 0;
+    for (int s0 = 0; s0 < a.L; s0 += CH, it ^= 1) {
         const int nout = min(CH, a.L - s0);
         float *dst = out + (size_t)9 * s0;
         if (s0 >= len) {
@@ -377,10 +461,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, fwd_min_blocks(C)) a2b_fwd_
         }
         const int j0 = s0 + C * lane;
         PairFrame tot;
+        Frame<float> T;
+        if (pf) {
+            if (s0 + CH < len) prefetch_angles<C>(abuf + (it ^ 1) * 3 * CH, ang, a.L, s0 + CH, lane);
+            cp_async_commit();
+            cp_async_wait1();  // this chunk's copies (all groups but the newest) have landed
+            T = walk_chunk_smem<C, C != 4>(a.bc, abuf + it * 3 * CH, lane, j0, len, seg);
+        } else {
+            T = walk_chunk<C, C != 4>(a.bc, ang, a.L, j0, len, vec, seg);
+        }
         // lane transforms compose 3C joints: no renormalisation before the scan (the
         // chain frame carried from chunk to chunk is renormalised)
-        const PairFrame E = warp_exclusive_total_pair(to_pair(walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg)),
-                                                      lane, false, tot);
+        const PairFrame E = warp_exclusive_total_pair(to_pair(T), lane, false, tot);
         // E composes at most 31 renormalised lane transforms: P needs no renormalisation
         const PairFrame P = compose_pair(F, E);
         if ((C * lane) % kRecordStride == 0 && j0 < len) pair_store(rec[j0 / kRecordStride].f, P);
@@ -435,7 +527,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, bwd_min_blocks(C)) a2b_bwd_
             }
         }
         stage_chunk<SEG, SP>(sg, gin + (size_t)9 * s0, 9 * nreal, lane, vec);
-        const Frame<float> t = walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, xs);
+        const Frame<float> t = walk_chunk<C, true>(a.bc, ang, a.L, j0, len, vec, xs);
         Frame<float> tot;
         const Frame<float> E = warp_exclusive_total(t, lane, false, tot);  // as the forward's scan
         F.p[0] = F.p[1] = F.p[2] = 0.f;  // lane frames relative to the chunk origin
@@ -952,7 +1044,8 @@ __device__ __forceinline__ void carry_f64(const double *in, const PairFrame &tot
         out[lane] = v;
     }
 }
-// 6 CTAs of 9.3 KB staging per warp (C = 8) or 7 (C = 4) fit an SM's shared memory
+// Six CTAs of four warps with 9.3 KB of staging per warp (C = 8), or seven with 4.5 KB
+// of staging plus the 3 KB angle buffer per warp (C = 4), fit an SM's shared memory
 constexpr int ring_fwd_min_blocks(int C) { return C >= 8 ? 6 : 7; }
 
 template <int C>
@@ -962,7 +1055,8 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
     __shared__ __align__(16) float s_ring[kRingWarps][12];
     // FP64 carries, after the staging buffers: the launch adds their 384 bytes only
     // when fp64_min is set, so that the FP32 default keeps six CTAs per SM
-    double(*s_ring64)[12] = reinterpret_cast<double(*)[12]>(s_dyn + kRingWarps * FwdStage<C>::FLOATS);
+    double(*s_ring64)[12] =
+        reinterpret_cast<double(*)[12]>(s_dyn + kRingWarps * (FwdStage<C>::FLOATS + AngBuf<C>::FLOATS));
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;  // one CTA per chain: the grid is the batch
     float *stage = s_dyn + w * FwdStage<C>::FLOATS;
@@ -977,16 +1071,34 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
     // whole CTA, so every warp takes the same branch at every handoff)
     const bool carry64 = a.fp64_min > 0 && len >= a.fp64_min;
 
+    constexpr bool PF = AngBuf<C>::ON;
+    float *abuf = s_dyn + kRingWarps * FwdStage<C>::FLOATS + w * AngBuf<C>::FLOATS;
+    const bool pf = PF && vec;
+    if (pf) {
+        if (w * CH < len) prefetch_angles<C>(abuf, ang, a.L, w * CH, lane);
+        cp_async_commit();
+    }
+    int it = 0;
 #pragma unroll 1
-    for (int k = w; k < nchunk; k += kRingWarps) {
+    for (int k = w; k < nchunk; k += kRingWarps, it ^= 1) {
         const int s0 = k * CH;
         const int nout = min(CH, a.L - s0);
         const bool live = s0 < len;
         const int j0 = s0 + C * lane;
         PairFrame E = pair_identity(), tot = pair_identity();
-        if (live)  // no renormalisation of the lane transforms (3C joints each), as in a2b_fwd_chain_kernel
-            E = warp_exclusive_total_pair(to_pair(walk_chunk<C>(a.bc, ang, a.L, j0, len, vec, seg)), lane, false,
-                                          tot);
+        if (live) {  // no renormalisation of the lane transforms (3C joints each), as in a2b_fwd_chain_kernel
+            Frame<float> T;
+            if (pf) {
+                const int sn = s0 + kRingWarps * CH;
+                if (sn < len) prefetch_angles<C>(abuf + (it ^ 1) * 3 * CH, ang, a.L, sn, lane);
+                cp_async_commit();
+                cp_async_wait1();
+                T = walk_chunk_smem<C, true>(a.bc, abuf + it * 3 * CH, lane, j0, len, seg);
+            } else {
+                T = walk_chunk<C, true>(a.bc, ang, a.L, j0, len, vec, seg);
+            }
+            E = warp_exclusive_total_pair(to_pair(T), lane, false, tot);
+        }
         PairFrame F = pair_identity();  // chain frame at the chunk start
         if (k > 0) {
             ring_wait(k);
@@ -1282,7 +1394,7 @@ __global__ void sincos_poly_kernel(const float *a, float *s, float *c, int n) {
 
 template <int C>
 constexpr int fwd_smem() {
-    return kWarpsPerCta * FwdStage<C>::FLOATS * (int)sizeof(float);
+    return kWarpsPerCta * (FwdStage<C>::FLOATS + AngBuf<C>::FLOATS) * (int)sizeof(float);
 }
 template <int C>
 constexpr int bwd_smem() {  // positions and dL/dx of every lane, padded lane stride 9C + 4
