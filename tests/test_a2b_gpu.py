@@ -139,10 +139,16 @@ def test_four_warp_fp64_carry_threshold(rm, rpt):
     300 residues (a positive fp64_carry_min_len): chains above and below the
     threshold in one batch, coordinates within 1e-3 A of the oracle and the
     recomputing backward (which starts from the forward's recorded frames) within
-    1e-4; the FP32 carry (threshold 0, the default) on the same batch for contrast."""
-    B, L = 5, 1000
-    ang, lengths, g = make_case(B, L, 91 + rpt, lengths=[1000, 700, 300, 299, 40])
+    1e-4; the FP32 carry (threshold 0, the default) on the same batch for contrast.
+    The FP64 carry must not be less accurate than the FP32 one: its maximum and RMS
+    coordinate errors over the 1000-residue chains stay within 10 % of the FP32
+    carry's (an FP64 product of chunk totals that are not renormalised drifts in
+    scale, to about 1.5e-3 A at 1000 residues)."""
+    B, L = 40, 1000
+    lengths = [1000] * 35 + [700, 300, 299, 40, 1000]
+    ang, lengths, g = make_case(B, L, 91 + rpt, lengths=lengths)
     rc, rg = oracle_ref(ang, lengths, g, True)
+    errs = {}
     for carry in (300, 0):
         rm.set_options(rpt, carry, 0, 0, 4)
         try:
@@ -150,6 +156,10 @@ def test_four_warp_fp64_carry_threshold(rm, rpt):
         finally:
             rm.set_options(0, 0, 0, 0)
         check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+        e = np.linalg.norm((c - rc).reshape(B, -1, 3), axis=-1)[:35]
+        errs[carry] = (e.max(), np.sqrt((e ** 2).mean()))
+    assert errs[300][0] <= 1.1 * errs[0][0], errs
+    assert errs[300][1] <= 1.1 * errs[0][1], errs
 
 
 @pytest.mark.parametrize("rpt,cta", [(0, 1), (8, 32), (4, 32)])

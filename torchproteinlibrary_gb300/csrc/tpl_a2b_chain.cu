@@ -1106,7 +1106,12 @@ __global__ void __launch_bounds__(32 * kRingWarps, ring_fwd_min_blocks(C)) a2b_f
         }
         if (k + 1 < nchunk) {
             if (carry64) {
-                carry_f64(k > 0 ? s_ring64[k & 3] : nullptr, tot, s_ring64[(k + 1) & 3], lane);
+                // the chunk total composes 96C unrenormalised joints: pull it back onto SO(3)
+                // first, or the FP64 product of the totals drifts in scale chunk by chunk
+                // (the FP32 carry below renormalises the carried frame instead)
+                PairFrame t = tot;
+                if (a.renorm) renormalize_pair(t);
+                carry_f64(k > 0 ? s_ring64[k & 3] : nullptr, t, s_ring64[(k + 1) & 3], lane);
             } else {
                 PairFrame Fn = compose_pair(F, tot);
                 if (a.renorm) renormalize_pair(Fn);
