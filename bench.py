@@ -1074,10 +1074,15 @@ def time_coords_transform(dev, steps=20):
                     dim=1).view(B, 3, 3).contiguous()
     peak, _ = peaks()
     res = {"workload": f"{B} rows x {S} atoms, float32", "bytes_per_call": 2 * x.numel() * 4}
-    cen = torch.empty(B, 3, device=dev)
+    # the centre only reads its input: twice the rows (196 MB), so that back-to-back
+    # calls cannot be served from the 129 MB L2
+    xc = torch.randn(2 * B, 3 * S, device=dev, generator=g)
+    nac = torch.full((2 * B,), S, dtype=torch.int32, device=dev)
+    cen = torch.empty(2 * B, 3, device=dev)
+    res["center_workload"] = f"{2 * B} rows x {S} atoms, float32 (read only)"
     for name, fn, nbytes in (("translate", lambda: fm.CoordsTranslateGPU_forward(x, out, T, na), 2 * x.numel() * 4),
                              ("rotate", lambda: fm.CoordsRotateGPU_forward(x, out, R, na), 2 * x.numel() * 4),
-                             ("center", lambda: fm.Coords2CenterGPU_forward(x, cen, na), x.numel() * 4)):
+                             ("center", lambda: fm.Coords2CenterGPU_forward(xc, cen, nac), xc.numel() * 4)):
         for _ in range(3):
             fn()
         torch.cuda.synchronize(dev)
