@@ -360,6 +360,29 @@ def test_four_warp_kernels_at_batch_size(fm):
     np.testing.assert_array_equal(gi[:n], gi[(reps - 1) * n:])
 
 
+def test_persistent_kernels_take_several_chains_per_cta(fm):
+    """The four- and eight-warp kernels are persistent: a grid of (resident CTAs per
+    SM) x (SMs) takes the chains in turn.  With 60 replicas of coords_case (1020
+    chains) every kernel's CTAs take more than one chain: the forward with names (four
+    warps, at most 6 x SMs CTAs), the reference-signature backward's forward without
+    names (eight warps, 3 x SMs) and the backward from the coordinates.  Every
+    replica must equal the first bit for bit, and the first the oracle."""
+    seqs, ang, rc, na, g = coords_case(67)
+    rg = oracle.a2c_backward(g, ang, seqs)
+    reps, n = 60, len(seqs)
+    assert reps * n > 6 * torch.cuda.get_device_properties(0).multi_processor_count
+    for from_coords in (True, False):
+        c, rn, an, _, gi = run_gpu(fm, np.tile(ang, (reps, 1, 1)), seqs * reps, np.tile(g, (reps, 1)),
+                                   torch.float32, from_coords=from_coords)
+        check(c[:n], gi[:n], rc, rg, na, COORD_TOL_F32, GRAD_TOL_F32)
+        for r in range(1, reps):
+            sl = slice(r * n, (r + 1) * n)
+            np.testing.assert_array_equal(c[sl], c[:n])
+            np.testing.assert_array_equal(gi[sl], gi[:n])
+            np.testing.assert_array_equal(rn[sl], rn[:n])
+            np.testing.assert_array_equal(an[sl], an[:n])
+
+
 def test_backward_from_coordinates_c_abi_and_layer(fm, built):
     """Through the C ABI (status-word workspace only), bit-identical to the
     extension entry; and the float32 autograd layer's gradient (from its saved
