@@ -99,3 +99,16 @@ def test_c_abi_translate_rotate(built):
     torch.cuda.synchronize()
     assert np.abs(out.cpu().numpy() - oracle.coords_rotate(x, R, na)).max() <= 2e-6 * np.abs(x).max()
     assert lib.tpl_coords_rotate_f32(None, out.data_ptr(), Rt.data_ptr(), 0, nat.data_ptr(), 5, 33, None) == -1
+
+
+@pytest.mark.parametrize("S", [700, 33, 4000])
+def test_center_vector_and_scalar_paths(ct, S):
+    """Coords2Center in float32 reads 16-byte rows (stride a multiple of 4 atoms) as
+    float4 groups of four atoms plus a scalar tail, and other strides atom by atom;
+    both against the oracle within 1e-6 of the coordinate scale, with counts of every
+    residue mod 4 and a chain far from the origin."""
+    x, na, _, _ = case(torch.float32, B=12, S=S, seed=11)
+    na[3:7] = [max(0, S - 1), max(0, S - 2), max(0, S - 3), min(5, S)]
+    x[4] += 500.0
+    c = ct.Coords2Center()(torch.tensor(x, device="cuda"), torch.tensor(na)).cpu().numpy()
+    assert np.abs(c - oracle.coords_center(x, na)).max() <= 1e-6 * np.abs(x).max()

@@ -168,7 +168,7 @@ __device__ __forceinline__ R block_reduce(R v, Op op, R *s_warp) {
 // 0 for an empty chain.
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) center_kernel(const T *in, T *center, const int *num_atoms,
-                                                                int stride) {
+                                                                int stride, int vec) {
     constexpr int NW = kReduceThreads / 32;
     __shared__ double s_warp[NW][3];
     const int b = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -179,7 +179,22 @@ __global__ void __launch_bounds__(kReduceThreads) center_kernel(const T *in, T *
     // wherever the chain sits, and GB300's FP64 rate is a small fraction of its FP32 rate
     const T p0 = n > 0 ? x[0] : T(0), p1 = n > 0 ? x[1] : T(0), p2 = n > 0 ? x[2] : T(0);
     T s[3] = {T(0), T(0), T(0)};
-    for (int i = threadIdx.x; i < n; i += kReduceThreads) {
+    int i0 = 0;  // first atom of the scalar loop
+    if constexpr (sizeof(T) == 4) {
+        if (vec) {  // 16-byte rows: a thread reads 4 atoms as three float4s, two groups in flight
+            const float4 *x4 = reinterpret_cast<const float4 *>(x);
+            const int ng = n >> 2;
+#pragma unroll 2
+            for (int g = threadIdx.x; g < ng; g += kReduceThreads) {
+                const float4 a = x4[3 * g], b = x4[3 * g + 1], c = x4[3 * g + 2];
+                s[0] += ((a.x - p0) + (a.w - p0)) + ((b.z - p0) + (c.y - p0));
+                s[1] += ((a.y - p1) + (b.x - p1)) + ((b.w - p1) + (c.z - p1));
+                s[2] += ((a.z - p2) + (b.y - p2)) + ((c.x - p2) + (c.w - p2));
+            }
+            i0 = 4 * ng;
+        }
+    }
+    for (int i = i0 + threadIdx.x; i < n; i += kReduceThreads) {
         s[0] += x[3 * i] - p0;
         s[1] += x[3 * i + 1] - p1;
         s[2] += x[3 * i + 2] - p2;
@@ -275,7 +290,8 @@ int coords_rotate(const T *in, T *out, const T *R, int transpose, const int *num
 template <typename T>
 int coords_center(const T *in, T *center, const int *num_atoms, int B, int stride, cudaStream_t st) {
     if (B == 0) return TPL_OK;
-    center_kernel<T><<<B, kReduceThreads, 0, st>>>(in, center, num_atoms, stride);
+    const int vec = stride % 4 == 0 && (reinterpret_cast<uintptr_t>(in) & 15u) == 0;
+    center_kernel<T><<<B, kReduceThreads, 0, st>>>(in, center, num_atoms, stride, vec);
     return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
