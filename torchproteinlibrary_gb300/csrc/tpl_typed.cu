@@ -116,9 +116,22 @@ __device__ __forceinline__ uint32_t squeeze(uint32_t w) {
     return out;
 }
 
-// The 0-based type of an atom, or -1 for a name pair the reference rejects.
-__device__ __forceinline__ int atom_type(uint32_t res, uint32_t atom) {
-    atom = squeeze(atom);
+// squeeze() without the byte loop when the name has no byte below '!' before its
+// first NUL (the names Angles2Coords writes): the word up to that NUL.  Per byte,
+// (w - 0x01) & ~w & 0x80 flags a NUL and (w - 0x21) & ~w & 0x80 a byte below 0x21;
+// borrows only make false flags above a true one, so the lowest flag is exact.
+__device__ __forceinline__ uint32_t squeeze_fast(uint32_t w) {
+    const uint32_t nul = (w - 0x01010101u) & ~w & 0x80808080u;
+    const uint32_t valid = nul ? (((nul & (0u - nul)) >> 7) - 1u) : 0xffffffffu;  // bytes before the first NUL
+    const uint32_t low = (w - 0x21212121u) & ~w & 0x80808080u;
+    if ((low & valid) == 0u) return w & valid;
+    return squeeze(w);
+}
+
+// The 0-based type of an atom, or -1 for a name pair the reference rejects; h is the
+// name hash (global memory, or a copy in shared memory).
+__device__ __forceinline__ int atom_type(uint32_t res, uint32_t atom, const TypedHash &h) {
+    atom = squeeze_fast(atom);
     res = res & 0x00ffffffu;  // the residue is its 3-letter code
     if (atom == nm("O")) return 5;  // not a terminal oxygen (the reference's call passes false)
     if (atom == nm("OXT") || atom == nm("OT2")) return 7;
@@ -127,26 +140,25 @@ __device__ __forceinline__ int atom_type(uint32_t res, uint32_t atom) {
     if (atom == nm("CA")) return 10;
     uint32_t k = typed_hash(res, atom);
     for (int probe = 0; probe < kHashSlots; probe++) {
-        const uint32_t r = g_typed_hash.res[k];
+        const uint32_t r = h.res[k];
         if (r == 0u) return -1;
-        if (r == res && g_typed_hash.atom[k] == atom) return g_typed_hash.type[k];
+        if (r == res && h.atom[k] == atom) return h.type[k];
         k = (k + 1) & (kHashSlots - 1);
     }
     return -1;
 }
+__device__ __forceinline__ int atom_type(uint32_t res, uint32_t atom) { return atom_type(res, atom, g_typed_hash); }
 
 // Input rows hold in_stride atoms (coordinates and names); typed rows and atom
-// indexes hold out_stride slots.
-// CACHE: each atom's type from the counting pass is kept in shared memory (in_stride
-// bytes of dynamic shared memory) for the scatter pass, instead of looked up again.
-template <typename T, bool CACHE>
+// indexes hold out_stride slots.  One CTA per chain, for chains too long for
+// typed_fwd_seg_kernel's type cache: the scatter pass looks the types up again.
+template <typename T>
 __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coords, const uint32_t *res_names,
                                                                   const uint32_t *atom_names, const int *num_atoms,
                                                                   int in_stride, int out_stride, T *out,
                                                                   int *n_of_type, int *offsets, int *atom_index,
                                                                   WsHeader *hdr) {
     constexpr int NW = kTypedThreads / 32;
-    extern __shared__ signed char s_ty[];
     __shared__ int s_count[kTypes], s_off[kTypes], s_base[kTypes];
     __shared__ int s_wc[kTypes][NW];
     const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -159,7 +171,6 @@ __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coord
     __syncthreads();
     for (int j = tid; j < n; j += kTypedThreads) {
         const int t = atom_type(res_names[row + j], atom_names[row + j]);
-        if (CACHE) s_ty[j] = (signed char)t;
         if (t >= 0) atomicAdd(&s_count[t], 1);
         else atomicCAS(&hdr->status, 0u, (unsigned)TPL_ERR_ATOM_TYPE);
     }
@@ -188,7 +199,7 @@ __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coord
             x1 = src[1];
             x2 = src[2];
         }
-        const int t = j < n ? (CACHE ? (int)s_ty[j] : atom_type(res_names[row + j], atom_names[row + j])) : -1;
+        const int t = j < n ? atom_type(res_names[row + j], atom_names[row + j]) : -1;
         int rank = 0;
         const unsigned below = (1u << lane) - 1u;
 #pragma unroll
@@ -219,6 +230,133 @@ __global__ void __launch_bounds__(kTypedThreads) typed_fwd_kernel(const T *coord
         dst[0] = dst[1] = dst[2] = T(0);
         atom_index[orow + s] = 0;
     }
+}
+
+// The same regrouping by four warps per chain with three CTA barriers in all: each
+// warp takes a quarter of the chain's 32-atom tiles.  Pass 1 types the atoms of the
+// warp's tiles and counts them per type (per tile, __match_any_sync groups the lanes
+// of each type and the lowest of them adds their number); after a barrier every warp
+// knows where its atoms of each type start (the type's offset plus the counts of the
+// earlier warps), and pass 2 scatters its tiles in order: an atom's slot is its
+// type's next free slot plus its rank among the tile's atoms of that type, so the
+// order within a type is the input order.  Both passes load kTypedUnroll tiles
+// before working on them, so that a warp has several tiles' loads in flight.  Pass
+// 1's types stay in shared memory (in_stride bytes) for pass 2, and the name hash is
+// copied there too.  GB300, 4096 chains of U{50..500} residues: 0.158 -> 0.145 ms
+// against typed_fwd_kernel, which keeps chains of more than kTypeCacheMax atoms.
+constexpr int kTypedWarps = 4;  // warps per chain
+constexpr int kTypedUnroll = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kTypedWarps) typed_fwd_seg_kernel(
+    const T *__restrict__ coords, const uint32_t *__restrict__ res_names, const uint32_t *__restrict__ atom_names,
+    const int *__restrict__ num_atoms, int in_stride, int out_stride, T *__restrict__ out,
+    int *__restrict__ n_of_type, int *__restrict__ offsets, int *__restrict__ atom_index, WsHeader *hdr) {
+    extern __shared__ signed char s_ty[];
+    __shared__ int s_cnt[kTypedWarps][kTypes];
+    __shared__ int s_ntyped;
+    __shared__ TypedHash s_hash;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, b = blockIdx.x;
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(&g_typed_hash);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&s_hash);
+        for (int i = threadIdx.x; i < (int)(sizeof(TypedHash) / 4); i += 32 * kTypedWarps) dst[i] = src[i];
+    }
+    const int n = max(0, min(num_atoms[b], min(in_stride, out_stride)));
+    const size_t row = (size_t)b * in_stride, orow = (size_t)b * out_stride;
+    const uint32_t *rn = res_names + row, *an = atom_names + row;
+    const unsigned below = (1u << lane) - 1u;
+    const int ntiles = (n + 31) >> 5, per = (ntiles + kTypedWarps - 1) / kTypedWarps;
+    const int t0 = min(ntiles, w * per), t1 = min(ntiles, t0 + per);
+
+    if (lane < kTypes) s_cnt[w][lane] = 0;
+    __syncthreads();  // the hash copy and the zeroed counts
+    bool bad = false;
+    for (int tb = t0; tb < t1; tb += kTypedUnroll) {
+        uint32_t r[kTypedUnroll], a[kTypedUnroll];
+#pragma unroll
+        for (int u = 0; u < kTypedUnroll; u++) {
+            const int j = 32 * (tb + u) + lane;
+            const bool in = tb + u < t1 && j < n;
+            r[u] = in ? rn[j] : 0u;
+            a[u] = in ? an[j] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kTypedUnroll; u++) {
+            const int j = 32 * (tb + u) + lane;
+            const bool in = tb + u < t1 && j < n;
+            const int t = in ? atom_type(r[u], a[u], s_hash) : -2;  // -1: a name pair the reference rejects
+            if (in) s_ty[j] = (signed char)t;
+            bad |= t == -1;
+            // the lanes of each type: the lowest of them adds their number
+            const unsigned m = __match_any_sync(0xffffffffu, t);
+            if (t >= 0 && (m & below) == 0u) s_cnt[w][t] += __popc(m);
+            __syncwarp();
+        }
+    }
+    if (bad) atomicCAS(&hdr->status, 0u, (unsigned)TPL_ERR_ATOM_TYPE);
+    __syncthreads();
+    // lane k < kTypes: the type's total, its offset, and this warp's first slot of it
+    int tot = 0, before = 0;
+    if (lane < kTypes)
+#pragma unroll
+        for (int v = 0; v < kTypedWarps; v++) {
+            const int c = s_cnt[v][lane];
+            tot += c;
+            before += v < w ? c : 0;
+        }
+    int inc = tot;
+#pragma unroll
+    for (int off = 1; off < 16; off <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc += v;
+    }
+    const int type_off = inc - tot;
+    if (w == 0 && lane < kTypes) {
+        n_of_type[(size_t)b * kTypes + lane] = tot;
+        offsets[(size_t)b * kTypes + lane] = type_off;
+    }
+    if (w == 0 && lane == kTypes - 1) s_ntyped = inc;
+    __syncthreads();  // every warp has read the counts
+    int *s_next = s_cnt[w];  // reused: this warp's next free slot of each type
+    if (lane < kTypes) s_next[lane] = type_off + before;
+    __syncwarp();
+
+    for (int tb = t0; tb < t1; tb += kTypedUnroll) {
+        T x[kTypedUnroll][3];
+        int ty[kTypedUnroll];
+#pragma unroll
+        for (int u = 0; u < kTypedUnroll; u++) {
+            const int j = 32 * (tb + u) + lane;
+            const bool in = tb + u < t1 && j < n;
+            const T *src = coords + 3 * (row + j);
+#pragma unroll
+            for (int c = 0; c < 3; c++) x[u][c] = in ? src[c] : T(0);
+            ty[u] = in ? (int)s_ty[j] : -2;
+        }
+#pragma unroll
+        for (int u = 0; u < kTypedUnroll; u++) {
+            const int j = 32 * (tb + u) + lane, t = ty[u];
+            const unsigned m = __match_any_sync(0xffffffffu, t);
+            if (t >= 0) {
+                const int slot = s_next[t] + __popc(m & below);
+                T *dst = out + 3 * (orow + slot);
+                dst[0] = x[u][0];
+                dst[1] = x[u][1];
+                dst[2] = x[u][2];
+                atom_index[orow + slot] = j;
+            }
+            __syncwarp();
+            if (t >= 0 && (m & below) == 0u) s_next[t] += __popc(m);
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    // slots past the typed atoms are zero, as in the reference's zero-filled outputs
+    const int ntyped = s_ntyped;
+    T *o = out + 3 * orow;
+    for (int e = 3 * ntyped + threadIdx.x; e < 3 * out_stride; e += 32 * kTypedWarps) o[e] = T(0);
+    for (int q = ntyped + threadIdx.x; q < out_stride; q += 32 * kTypedWarps) atom_index[orow + q] = 0;
 }
 
 // grad_flat[atom_index[s]] = grad_typed[s] for the typed slots, zero elsewhere;
@@ -294,7 +432,7 @@ __global__ void __launch_bounds__(kTypedThreads) typed_bwd_gather_kernel(const T
 }
 
 constexpr int kGatherMaxAtoms = 16384;  // 64 KB of slots per CTA
-constexpr int kTypeCacheMax = 32768;    // forward type cache: one byte per input atom
+constexpr int kTypeCacheMax = 32768;    // typed_fwd_seg_kernel's type cache: one byte per input atom
 
 }  // namespace
 
@@ -303,23 +441,30 @@ int typed_forward(bool f64, const void *coords, const uint32_t *res_names, const
                   int *atom_index, void *ws, cudaStream_t st) {
     if (B == 0) return TPL_OK;
     WsHeader *hdr = reinterpret_cast<WsHeader *>(ws);
-    const bool cache = in_stride <= kTypeCacheMax;
-    const size_t smem = cache ? (size_t)in_stride : 0;
-    auto launch = [&](auto kernel, auto *out_t, auto *coords_t) -> int {
-        if (smem > 48 * 1024 && !set_max_dynamic_smem(reinterpret_cast<const void *>(kernel), (int)smem))
-            return TPL_ERR_LAUNCH;
-        kernel<<<B, kTypedThreads, smem, st>>>(coords_t, res_names, atom_names, num_atoms, in_stride, out_stride,
-                                               out_t, n_of_type, offsets, atom_index, hdr);
-        return cudaGetLastError() == cudaSuccess ? (int)TPL_OK : (int)TPL_ERR_LAUNCH;
-    };
-    if (f64) {
-        auto *o = static_cast<double *>(out);
-        auto *c = static_cast<const double *>(coords);
-        return cache ? launch(typed_fwd_kernel<double, true>, o, c) : launch(typed_fwd_kernel<double, false>, o, c);
+    if (in_stride <= kTypeCacheMax) {  // four warps per chain, types cached in shared memory
+        const size_t smem = (size_t)in_stride;
+        auto launch_s = [&](auto kernel, auto *out_t, auto *coords_t) -> int {
+            if (smem > 48 * 1024 && !set_max_dynamic_smem(reinterpret_cast<const void *>(kernel), (int)smem))
+                return TPL_ERR_LAUNCH;
+            kernel<<<B, 32 * kTypedWarps, smem, st>>>(coords_t, res_names, atom_names, num_atoms, in_stride,
+                                                       out_stride, out_t, n_of_type, offsets, atom_index, hdr);
+            return cudaGetLastError() == cudaSuccess ? (int)TPL_OK : (int)TPL_ERR_LAUNCH;
+        };
+        if (f64)
+            return launch_s(typed_fwd_seg_kernel<double>, static_cast<double *>(out),
+                            static_cast<const double *>(coords));
+        return launch_s(typed_fwd_seg_kernel<float>, static_cast<float *>(out), static_cast<const float *>(coords));
     }
-    auto *o = static_cast<float *>(out);
-    auto *c = static_cast<const float *>(coords);
-    return cache ? launch(typed_fwd_kernel<float, true>, o, c) : launch(typed_fwd_kernel<float, false>, o, c);
+    // longer chains: one CTA per chain, the types looked up again in the scatter pass
+    if (f64)
+        typed_fwd_kernel<double><<<B, kTypedThreads, 0, st>>>(
+            static_cast<const double *>(coords), res_names, atom_names, num_atoms, in_stride, out_stride,
+            static_cast<double *>(out), n_of_type, offsets, atom_index, hdr);
+    else
+        typed_fwd_kernel<float><<<B, kTypedThreads, 0, st>>>(
+            static_cast<const float *>(coords), res_names, atom_names, num_atoms, in_stride, out_stride,
+            static_cast<float *>(out), n_of_type, offsets, atom_index, hdr);
+    return cudaGetLastError() == cudaSuccess ? TPL_OK : TPL_ERR_LAUNCH;
 }
 
 int typed_backward(bool f64, const void *grad_typed, void *grad_flat, const int *n_of_type, const int *atom_index,
