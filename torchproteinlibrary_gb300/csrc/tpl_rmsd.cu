@@ -10,8 +10,9 @@
 // type per thread and per warp, in FP64 across the warps: GB300's FP64 rate is a
 // small fraction of its FP32 rate), the 4x4 matrix T (same layout as the
 // reference), its largest eigenpair by the characteristic-polynomial method on one
-// warp (key_eigen_warp: lane-parallel coefficients, FP32 Newton polished in FP64),
-// U from the unit quaternion, UT = U^T and
+// warp (key_eigen_warp: lane-parallel coefficients, FP32 Newton polished in FP64;
+// key_eigen_warp_f32 for float32 inputs, all in FP32 on K / e0: GB300, 256 chains of
+// about 2300 atoms, 18.5 -> 12.5 us per forward), U from the unit quaternion, UT = U^T and
 // rmsd = sqrt((R2 - 2 |lambda_max| + 1e-10) / N).  The backward is one launch with
 // one thread per atom (chains on x, blocks of atoms on y):
 // dL/dx_i = g (x_i - UT y_i) / (rmsd N) on the centred coordinates.
@@ -174,6 +175,133 @@ __device__ void key_eigen_warp(const double *sK, double e0, double &lam, double 
     }
 }
 
+__device__ __forceinline__ float det3f(float a, float b, float c, float d, float e, float f, float g, float h, float i) {
+    return fmaf(a, fmaf(e, i, -f * h), fmaf(-b, fmaf(d, i, -f * g), c * fmaf(d, h, -e * g)));
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// key_eigen_warp in FP32 for the float32 forward, on K / e0 (entries of order one):
+// the same characteristic-polynomial coefficients, Newton from s = 1 down to the
+// largest root s_max = l_max / e0, and the eigenvector from the cofactors of
+// K / e0 - s_max I.  The float32 sums that build K already limit l_max to about
+// FP32 precision, so FP64 (a small fraction of GB300's FP32 rate) buys nothing here.
+__device__ void key_eigen_warp_f32(const float *sK, double e0, double &lam, float (&q)[4]) {
+    const int lane = threadIdx.x & 31;
+    const float ie = e0 > 0.0 ? (float)(1.0 / e0) : 0.f;
+    float k[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++) k[m] = sK[m] * ie;
+    float t2 = 0.f, t3 = 0.f, c0 = 0.f;
+    if (lane < 16) {
+        const int i = lane >> 2, j = lane & 3;
+        float k2 = 0.f;
+#pragma unroll
+        for (int m = 0; m < 4; m++) k2 = fmaf(k[4 * i + m], k[4 * m + j], k2);
+        const float kij = k[4 * i + j];
+        t2 = kij * kij;
+        t3 = k2 * k[4 * j + i];
+    } else if (lane < 20) {
+        const int j = lane - 16;
+        const int ca = j == 0 ? 1 : 0, cb = j <= 1 ? 2 : 1, cc = j <= 2 ? 3 : 2;
+        c0 = k[j] * det3f(k[4 + ca], k[4 + cb], k[4 + cc], k[8 + ca], k[8 + cb], k[8 + cc], k[12 + ca], k[12 + cb],
+                          k[12 + cc]);
+        if (j & 1) c0 = -c0;
+    }
+    t2 = warp_sum_f(t2);
+    t3 = warp_sum_f(t3);
+    c0 = warp_sum_f(c0);
+    const float a2 = -0.5f * t2, a1 = t3 * (-1.0f / 3.0f), a0 = c0;
+    float s = 0.f;
+    if (e0 > 0.0) {
+        s = 1.f;
+        for (int it = 0; it < 64; it++) {
+            const float P = fmaf(fmaf(fmaf(s, s, a2), s, a1), s, a0);
+            const float dP = fmaf(fmaf(4.f * s, s, 2.f * a2), s, a1);
+            if (!(dP != 0.f)) break;
+            const float d = P / dP;
+            s -= d;
+            if (fabsf(d) <= 1e-7f) break;
+        }
+    }
+    lam = (double)s * e0;
+    float cof = 0.f;
+    if (lane < 16) {
+        const int i = lane >> 2, j = lane & 3;
+        float m[9];
+        int t = 0;
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+            if (r != i)
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    if (c != j) m[t++] = k[4 * r + c] - (r == c ? s : 0.f);
+        cof = det3f(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
+        if ((i + j) & 1) cof = -cof;
+    }
+    float nrm = cof * cof;
+    nrm += __shfl_xor_sync(0xffffffffu, nrm, 1);
+    nrm += __shfl_xor_sync(0xffffffffu, nrm, 2);
+    int best = 0;
+    float bn = __shfl_sync(0xffffffffu, nrm, 0);
+    for (int i = 1; i < 4; i++) {
+        const float v = __shfl_sync(0xffffffffu, nrm, 4 * i);
+        if (v > bn) {
+            bn = v;
+            best = i;
+        }
+    }
+    const bool ok = bn > 1e-30f;
+    const float inv = ok ? rsqrtf(bn) : 0.f;
+    for (int kk = 0; kk < 4; kk++) q[kk] = __shfl_sync(0xffffffffu, cof, 4 * best + kk) * inv;
+    if (!ok) {
+        q[0] = 1.f;
+        q[1] = q[2] = q[3] = 0.f;
+    }
+}
+
+// The end of the float32 forward on warp 0: the key matrix (float), its top
+// eigenpair, UT, rmsd and the centroids.
+__device__ void rmsd_finish_f32(const RmsdArgs<float> &a, int b, int n, const double *s_out, float *s_Kf,
+                                const double *s_c) {
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        float R[9];
+        for (int k = 0; k < 9; k++) R[k] = (float)s_out[k];
+        const float F[16] = {R[0] + R[4] + R[8], R[5] - R[7], R[6] - R[2], R[1] - R[3],
+                             R[5] - R[7], R[0] - R[4] - R[8], R[1] + R[3], R[2] + R[6],
+                             R[6] - R[2], R[1] + R[3], -R[0] + R[4] - R[8], R[5] + R[7],
+                             R[1] - R[3], R[2] + R[6], R[5] + R[7], -R[0] - R[4] + R[8]};
+        for (int k = 0; k < 16; k++) s_Kf[k] = F[k];
+    }
+    __syncwarp();
+    const double r2 = s_out[9];
+    double lam;
+    float q[4];
+    key_eigen_warp_f32(s_Kf, 0.5 * r2, lam, q);
+    if (tid != 0) return;
+    float U[9];
+    U[0] = q[0] * q[0] + q[1] * q[1] - q[2] * q[2] - q[3] * q[3];
+    U[1] = 2.f * (q[1] * q[2] - q[0] * q[3]);
+    U[2] = 2.f * (q[1] * q[3] + q[0] * q[2]);
+    U[3] = 2.f * (q[1] * q[2] + q[0] * q[3]);
+    U[4] = q[0] * q[0] - q[1] * q[1] + q[2] * q[2] - q[3] * q[3];
+    U[5] = 2.f * (q[2] * q[3] - q[0] * q[1]);
+    U[6] = 2.f * (q[1] * q[3] - q[0] * q[2]);
+    U[7] = 2.f * (q[2] * q[3] + q[0] * q[1]);
+    U[8] = q[0] * q[0] - q[1] * q[1] - q[2] * q[2] + q[3] * q[3];
+    float *ut = a.ut + (size_t)9 * b;
+    for (int j = 0; j < 3; j++)
+        for (int k = 0; k < 3; k++) ut[3 * j + k] = U[3 * k + j];
+    const double msd = n > 0 ? (r2 - 2.0 * fabs(lam) + 1e-10) / (double)n : 0.0;
+    a.rmsd[b] = sqrtf(msd > 0.0 ? (float)msd : 0.f);
+    if (a.centroids)
+        for (int k = 0; k < 6; k++) a.centroids[6 * b + k] = s_c[k];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
     __shared__ double s_red[kRmsdWarps * 10];
@@ -223,6 +351,11 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
         acc[9] += xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2] + yi[0] * yi[0] + yi[1] * yi[1] + yi[2] * yi[2];
     }
     block_sums<T, 10>(acc, s_red, s_out);
+    if constexpr (sizeof(T) == 4) {
+        __shared__ float s_Kf[16];
+        if (tid < 32) rmsd_finish_f32(a, b, n, s_out, s_Kf, s_c);
+        return;
+    }
     if (tid < 32) {
         const double *R = s_out;
         double tot[10];
