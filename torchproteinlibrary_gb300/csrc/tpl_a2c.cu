@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(32 * NW, NW == 4 ? 6 : 3) a2c_fwd_ring_kernel(
         float *stage = sm.xyz[w];
         const int nchunk = ok ? (len + kA2cChunk - 1) / kA2cChunk : 0;
 
-    #pragma unroll 1
+#pragma unroll 1
         for (int k = w; k < nchunk; k += NW) {
             const int j = k * kA2cChunk + lane;
             const bool live = j < len;
@@ -548,10 +548,10 @@ __global__ void __launch_bounds__(32 * NW, NW == 4 ? 6 : 3) a2c_fwd_ring_kernel(
                 const float phi = ang[j], psi = ang[a.L + j];
                 const float om = j + 1 < len ? ang[2 * a.L + j] : 0.f;
                 float chi[5];
-    #pragma unroll
+#pragma unroll
                 for (int q = 0; q < 5; q++) chi[q] = ang[(size_t)(3 + q) * a.L + j];
                 float m = fmaxf(fabsf(phi), fmaxf(fabsf(psi), fabsf(om)));
-    #pragma unroll
+#pragma unroll
                 for (int q = 0; q < 5; q++) m = fmaxf(m, fabsf(chi[q]));
                 if (m <= 1.0e4f) {  // NaN passes: sincos_fast2 returns NaN for it
                     sincos_fast2(phi, psi, &sn[0], &cs[0], &sn[1], &cs[1]);
@@ -562,16 +562,16 @@ __global__ void __launch_bounds__(32 * NW, NW == 4 ? 6 : 3) a2c_fwd_ring_kernel(
                     sincos_poly(phi, &sn[0], &cs[0]);
                     sincos_poly(psi, &sn[1], &cs[1]);
                     sincos_poly(om, &sn[2], &cs[2]);
-    #pragma unroll
+#pragma unroll
                     for (int q = 0; q < 5; q++) sincos_poly(chi[q], &chs[q], &chc[q]);
                 }
-    #pragma unroll
+#pragma unroll
                 for (int q = 0; q < 3; q++) apply_joint_pair(t, tp.bb_cb[q], tp.bb_sb[q], tp.bb_d[q], cs[q], sn[q]);
             }
             PairFrame tot;
             const PairFrame E = warp_exclusive_total_pair(t, lane, renorm != 0, tot);
             int ci = na;  // atoms of the lanes up to this one
-    #pragma unroll
+#pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const int o = __shfl_up_sync(0xffffffffu, ci, off);
                 if (lane >= off) ci += o;
@@ -1028,7 +1028,7 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
         for (int c = w; c < nchunk; c += NW) {
             const int j = c * kA2cChunk + lane;
             int n = j < len ? tp.natoms[sm.lut[row[j]]] : 0;
-    #pragma unroll
+#pragma unroll
             for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(0xffffffffu, n, off);
             if (lane == 0) sm.base[c + 1] = n;
         }
@@ -1038,7 +1038,7 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
             for (int c0 = 0; c0 < nchunk; c0 += 32) {
                 const int c = c0 + lane;
                 int v = c < nchunk ? sm.base[c + 1] : 0;
-    #pragma unroll
+#pragma unroll
                 for (int off = 1; off < 32; off <<= 1) {
                     const int o = __shfl_up_sync(0xffffffffu, v, off);
                     if (lane >= off) v += o;
@@ -1058,14 +1058,14 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
         const int nrun = total > a.maxA ? 0 : nchunk;  // a chain whose atoms overflow the rows gets zeros
         const float inv_dphi = 1.f / tp.bb_d[0], inv_dpsi = 1.f / tp.bb_d[1], inv_dom = 1.f / tp.bb_d[2];
 
-    #pragma unroll 1
+#pragma unroll 1
         for (int k = nrun - 1 - w; k >= 0; k -= NW) {
             const int j = k * kA2cChunk + lane;
             const bool live = j < len;
             const int ty = live ? sm.lut[row[j]] : 0;
             const int na = live ? tp.natoms[ty] : 0;
             int inc = na;  // the residue's first atom inside the chunk: warp exclusive scan
-    #pragma unroll
+#pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const int v = __shfl_up_sync(0xffffffffu, inc, off);
                 if (lane >= off) inc += v;
@@ -1089,7 +1089,7 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
             float xN[3] = {0.f, 0.f, 0.f}, xA[3] = {0.f, 0.f, 0.f}, xC[3] = {0.f, 0.f, 0.f};
             if (live) {
                 const float *X = sx + 3 * aoff, *Gg = sg + 3 * aoff;
-    #pragma unroll
+#pragma unroll
                 for (int c = 0; c < 3; c++) {
                     xN[c] = X[c] - o[c];
                     xA[c] = X[3 + c] - o[c];
@@ -1106,7 +1106,7 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
                     for (int q = 2; q < na - 2; q++) add_atom(X + 3 * q, Gg + 3 * q, o, Gs, Ss);  // Pro ring (none for Gly)
                 // unrolled over the joints: joint kk reads chi angle kk or none (Ala;
                 // topology_layout_ok), so its gradient goes to a register, not a select
-    #pragma unroll
+#pragma unroll
                 for (int kk = kMaxScJoints - 1; kk >= 0; kk--) {
                     if (kk >= nj) continue;
                     const int f0 = 2 + tp.jfirst[ty][kk], f1 = f0 + tp.jna[ty][kk];
@@ -1119,7 +1119,7 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
                         gr[3 + kk] = joint_grad(ok_, op_, 1.f / tp.jd[ty][kk], Gs, Ss);
                     }
                 }
-    #pragma unroll
+#pragma unroll
                 for (int c = 0; c < 3; c++) {
                     G[c] += Gs[c];
                     S[c] += Ss[c];
@@ -1129,14 +1129,14 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
                 add_atom(X, Gg, o, G, S);          // N
             }
             float later[6], ctot[6];
-    #pragma unroll
+#pragma unroll
             for (int i = 0; i < 6; i++) later[i] = suffix_excl(v[i], lane, ctot[i]);
             // the sums over later chunks, moved to this chunk's origin: S_o = S_on + (on - o) x G
             float Gc[3] = {0.f, 0.f, 0.f}, Sc[3] = {0.f, 0.f, 0.f}, nN[3] = {0.f, 0.f, 0.f};
             if (k + 1 < nrun) {
                 ring_wait<NW>(k);
                 const float *cin = s_ring[k % NW];
-    #pragma unroll
+#pragma unroll
                 for (int c = 0; c < 3; c++) {
                     Gc[c] = cin[c];
                     Sc[c] = cin[3 + c];
@@ -1145,13 +1145,13 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
                 const float d[3] = {nN[0] - o[0], nN[1] - o[1], nN[2] - o[2]};
                 float dx[3];
                 cross3(d, Gc, dx);
-    #pragma unroll
+#pragma unroll
                 for (int c = 0; c < 3; c++) Sc[c] += dx[c];
             }
             if (k > 0) {
                 if (lane == 0) {
                     float *cout = s_ring[(k - 1) % NW];
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 3; c++) {
                         cout[c] = Gc[c] + ctot[c];
                         cout[3 + c] = Sc[c] + ctot[3 + c];
@@ -1167,13 +1167,13 @@ __global__ void __launch_bounds__(32 * NW) a2c_bwd_coords_ring_kernel(A2cArgs<fl
                 if (j + 1 < len) {  // omega_j: the next residue's N joint (the next chunk's first N after lane 31)
                     const float *X = sx + 3 * aoff;
                     float xn[3];
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 3; c++) xn[c] = (lane == 31 ? nN[c] : X[3 * na + c]) - o[c];
                     gr[2] = joint_grad(xn, xC, inv_dom, G, S);
                 }
                 gr[1] += joint_grad(xC, xA, inv_dpsi, G, S);
                 gr[0] += joint_grad(xA, xN, inv_dphi, G, S);
-    #pragma unroll
+#pragma unroll
                 for (int q = 0; q < 8; q++) gout[(size_t)q * a.L + j] = gr[q];
             }
         }
