@@ -41,8 +41,10 @@ SCRIPT = textwrap.dedent("""
     assert not dup, dup
 
     for name in ("Angles2BackboneGPU_forward", "Angles2BackboneGPU_backward",
-                 "Angles2BackboneCPU_forward", "Angles2BackboneCPU_backward"):
+                 "Angles2BackboneCPU_forward", "Angles2BackboneCPU_backward", "angles2backbone_autograd"):
         assert hasattr(_ReducedModel, name), name
+    # the C++ autograd functions the modules run
+    assert hasattr(_FullAtomModel, "angles2coords_autograd") and hasattr(_RMSD, "coords2rmsd_autograd")
     for name in ("Angles2Coords_forward", "Angles2Coords_backward", "Angles2Coords_save", "getSeqNumAtoms",
                  "PDB2CoordsUnordered", "Coords2TypedCoords_forward", "Coords2TypedCoords_backward",
                  "CoordsTranslate_forward", "CoordsTranslateGPU_forward", "CoordsTranslate_backward",
