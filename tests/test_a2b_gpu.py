@@ -676,3 +676,45 @@ def test_layer_uses_cpp_autograd_function(rm):
     assert (x.grad - x2.grad).abs().max().item() <= GRAD_TOL_F32 * scale
     x64 = torch.tensor(ang, dtype=torch.float64, device=dev, requires_grad=True)
     assert "Angles2BackboneGPUFunction" in layer(x64, ln).grad_fn.name()
+
+
+def test_layer_on_two_streams_concurrently(rm):
+    """The float32 layer keeps one shared workspace per (device, stream, shape): two
+    streams running forward and backward of the same shape at the same time get
+    their own, and give exactly the results of the same calls run one after the
+    other on the default stream (the recomputing backward too, whose workspace is
+    per call)."""
+    from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+    from torchproteinlibrary_gb300.ReducedModel.Angles2Backbone.Angles2Backbone import Angles2BackboneGPUFunction
+    dev = torch.device("cuda")
+    B, L = 512, 300
+    layer = Angles2Backbone()
+    cases = [make_case(B, L, 71 + i) for i in range(2)]
+    ln = [torch.tensor(c[1], device=dev) for c in cases]
+    gt = [torch.tensor(c[2], dtype=torch.float32, device=dev) for c in cases]
+    for from_coords in (True, False):
+        Angles2BackboneGPUFunction.backward_from_coords = from_coords
+        try:
+            ref = []
+            for i, c in enumerate(cases):
+                x = torch.tensor(c[0], dtype=torch.float32, device=dev, requires_grad=True)
+                out = layer(x, ln[i])
+                out.backward(gt[i])
+                ref.append((out.detach().clone(), x.grad.clone()))
+            xs = [torch.tensor(c[0], dtype=torch.float32, device=dev, requires_grad=True) for c in cases]
+            streams = [torch.cuda.Stream() for _ in cases]
+            outs = [None, None]
+            for s in streams:
+                s.wait_stream(torch.cuda.current_stream())
+            for i, s in enumerate(streams):
+                with torch.cuda.stream(s):
+                    outs[i] = layer(xs[i], ln[i])
+                    outs[i].backward(gt[i])
+            for s in streams:
+                torch.cuda.current_stream().wait_stream(s)
+            torch.cuda.synchronize()
+        finally:
+            Angles2BackboneGPUFunction.backward_from_coords = True
+        for i in range(2):
+            assert torch.equal(outs[i].detach(), ref[i][0])
+            assert torch.equal(xs[i].grad, ref[i][1])
