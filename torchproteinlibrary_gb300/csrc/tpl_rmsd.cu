@@ -11,8 +11,8 @@
 // small fraction of its FP32 rate), the 4x4 matrix T (same layout as the
 // reference), its largest eigenpair by the characteristic-polynomial method on one
 // warp (key_eigen_warp: lane-parallel coefficients, FP32 Newton polished in FP64;
-// key_eigen_warp_f32 for float32 inputs, all in FP32 on K / e0: GB300, 256 chains of
-// about 2300 atoms, 18.5 -> 12.5 us per forward), U from the unit quaternion, UT = U^T and
+// for float32 inputs the eigenvector, U and rmsd then in FP32: GB300, 256 chains of
+// about 2300 atoms, 18.6 -> 15.8 us per forward), U from the unit quaternion, UT = U^T and
 // rmsd = sqrt((R2 - 2 |lambda_max| + 1e-10) / N).  The backward is one launch with
 // one thread per atom (chains on x, blocks of atoms on y):
 // dL/dx_i = g (x_i - UT y_i) / (rmsd N) on the centred coordinates.
@@ -78,6 +78,51 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
+// The eigenvector for lam of key_eigen_warp<true>, in FP32: the largest row of the
+// cofactor matrix of K / e0 - (lam / e0) I (entries of order one), one cofactor per
+// lane.  The root itself stays FP64: when the top two eigenvalues nearly meet it is
+// ill-conditioned, and an all-FP32 solve moved it by up to 3e-5 relative (a 2.4e-4
+// gradient error on one of 256 training-step chains), where this form matches the
+// FP64 solve to 1e-5 of the largest gradient.
+__device__ void eigvec_f32(const double *sK, double e0, double l, double (&q)[4]) {
+    const int lane = threadIdx.x & 31;
+    const float ief = e0 > 0.0 ? 1.f / (float)e0 : 0.f, sf = (float)l * ief;
+    float cf = 0.f;
+    if (lane < 16) {
+        const int i = lane >> 2, j = lane & 3;
+        float m[9];
+        int t = 0;
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+            if (r != i)
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    if (c != j) m[t++] = (float)sK[4 * r + c] * ief - (r == c ? sf : 0.f);
+        cf = fmaf(m[0], fmaf(m[4], m[8], -m[5] * m[7]),
+                  fmaf(-m[1], fmaf(m[3], m[8], -m[5] * m[6]), m[2] * fmaf(m[3], m[7], -m[4] * m[6])));
+        if ((i + j) & 1) cf = -cf;
+    }
+    float nrm = cf * cf;
+    nrm += __shfl_xor_sync(0xffffffffu, nrm, 1);
+    nrm += __shfl_xor_sync(0xffffffffu, nrm, 2);
+    int best = 0;
+    float bn = __shfl_sync(0xffffffffu, nrm, 0);
+    for (int i = 1; i < 4; i++) {
+        const float v = __shfl_sync(0xffffffffu, nrm, 4 * i);
+        if (v > bn) {
+            bn = v;
+            best = i;
+        }
+    }
+    const bool ok = bn > 1e-30f;
+    const float inv = ok ? rsqrtf(bn) : 0.f;
+    for (int k = 0; k < 4; k++) q[k] = (double)(__shfl_sync(0xffffffffu, cf, 4 * best + k) * inv);
+    if (!ok) {
+        q[0] = 1.0;
+        q[1] = q[2] = q[3] = 0.0;
+    }
+}
+
 // Largest eigenpair of the 4x4 key matrix K (symmetric and traceless, row-major in
 // shared memory) by its characteristic polynomial, as in Theobald's
 // quaternion-characteristic-polynomial method (Acta Cryst. A61, 478, 2005):
@@ -92,8 +137,10 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 //     digits), so that only a handful of FP64 operations remain.
 //   * The eigenvector is the largest row of the cofactor matrix of K - l_max I
 //     (rank one for a simple root), one cofactor per lane.
+//   * F32_VEC (float32 inputs): the eigenvector in FP32 instead (eigvec_f32).
 // Executed by a full warp; every lane returns lam and the unit q (q = 1, 0, 0, 0
 // when every cofactor vanishes).
+template <bool F32_VEC>
 __device__ void key_eigen_warp(const double *sK, double e0, double &lam, double (&q)[4]) {
     const int lane = threadIdx.x & 31;
     double t2 = 0.0, t3 = 0.0, c0 = 0.0;
@@ -139,6 +186,10 @@ __device__ void key_eigen_warp(const double *sK, double e0, double &lam, double 
         }
     }
     lam = l;
+    if (F32_VEC) {
+        eigvec_f32(sK, e0, l, q);
+        return;
+    }
     // cofactor (i, j) of M = K - l I on lane 4 i + j
     double cof = 0.0;
     if (lane < 16) {
@@ -175,114 +226,26 @@ __device__ void key_eigen_warp(const double *sK, double e0, double &lam, double 
     }
 }
 
-__device__ __forceinline__ float det3f(float a, float b, float c, float d, float e, float f, float g, float h, float i) {
-    return fmaf(a, fmaf(e, i, -f * h), fmaf(-b, fmaf(d, i, -f * g), c * fmaf(d, h, -e * g)));
-}
-__device__ __forceinline__ float warp_sum_f(float v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
-
-// key_eigen_warp in FP32 for the float32 forward, on K / e0 (entries of order one):
-// the same characteristic-polynomial coefficients, Newton from s = 1 down to the
-// largest root s_max = l_max / e0, and the eigenvector from the cofactors of
-// K / e0 - s_max I.  The float32 sums that build K already limit l_max to about
-// FP32 precision, so FP64 (a small fraction of GB300's FP32 rate) buys nothing here.
-__device__ void key_eigen_warp_f32(const float *sK, double e0, double &lam, float (&q)[4]) {
-    const int lane = threadIdx.x & 31;
-    const float ie = e0 > 0.0 ? (float)(1.0 / e0) : 0.f;
-    float k[16];
-#pragma unroll
-    for (int m = 0; m < 16; m++) k[m] = sK[m] * ie;
-    float t2 = 0.f, t3 = 0.f, c0 = 0.f;
-    if (lane < 16) {
-        const int i = lane >> 2, j = lane & 3;
-        float k2 = 0.f;
-#pragma unroll
-        for (int m = 0; m < 4; m++) k2 = fmaf(k[4 * i + m], k[4 * m + j], k2);
-        const float kij = k[4 * i + j];
-        t2 = kij * kij;
-        t3 = k2 * k[4 * j + i];
-    } else if (lane < 20) {
-        const int j = lane - 16;
-        const int ca = j == 0 ? 1 : 0, cb = j <= 1 ? 2 : 1, cc = j <= 2 ? 3 : 2;
-        c0 = k[j] * det3f(k[4 + ca], k[4 + cb], k[4 + cc], k[8 + ca], k[8 + cb], k[8 + cc], k[12 + ca], k[12 + cb],
-                          k[12 + cc]);
-        if (j & 1) c0 = -c0;
-    }
-    t2 = warp_sum_f(t2);
-    t3 = warp_sum_f(t3);
-    c0 = warp_sum_f(c0);
-    const float a2 = -0.5f * t2, a1 = t3 * (-1.0f / 3.0f), a0 = c0;
-    float s = 0.f;
-    if (e0 > 0.0) {
-        s = 1.f;
-        for (int it = 0; it < 64; it++) {
-            const float P = fmaf(fmaf(fmaf(s, s, a2), s, a1), s, a0);
-            const float dP = fmaf(fmaf(4.f * s, s, 2.f * a2), s, a1);
-            if (!(dP != 0.f)) break;
-            const float d = P / dP;
-            s -= d;
-            if (fabsf(d) <= 1e-7f) break;
-        }
-    }
-    lam = (double)s * e0;
-    float cof = 0.f;
-    if (lane < 16) {
-        const int i = lane >> 2, j = lane & 3;
-        float m[9];
-        int t = 0;
-#pragma unroll
-        for (int r = 0; r < 4; r++)
-            if (r != i)
-#pragma unroll
-                for (int c = 0; c < 4; c++)
-                    if (c != j) m[t++] = k[4 * r + c] - (r == c ? s : 0.f);
-        cof = det3f(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
-        if ((i + j) & 1) cof = -cof;
-    }
-    float nrm = cof * cof;
-    nrm += __shfl_xor_sync(0xffffffffu, nrm, 1);
-    nrm += __shfl_xor_sync(0xffffffffu, nrm, 2);
-    int best = 0;
-    float bn = __shfl_sync(0xffffffffu, nrm, 0);
-    for (int i = 1; i < 4; i++) {
-        const float v = __shfl_sync(0xffffffffu, nrm, 4 * i);
-        if (v > bn) {
-            bn = v;
-            best = i;
-        }
-    }
-    const bool ok = bn > 1e-30f;
-    const float inv = ok ? rsqrtf(bn) : 0.f;
-    for (int kk = 0; kk < 4; kk++) q[kk] = __shfl_sync(0xffffffffu, cof, 4 * best + kk) * inv;
-    if (!ok) {
-        q[0] = 1.f;
-        q[1] = q[2] = q[3] = 0.f;
-    }
-}
-
-// The end of the float32 forward on warp 0: the key matrix (float), its top
-// eigenpair, UT, rmsd and the centroids.
-__device__ void rmsd_finish_f32(const RmsdArgs<float> &a, int b, int n, const double *s_out, float *s_Kf,
+// The end of the float32 forward on warp 0: the FP64 key-matrix eigen solve (its
+// largest root is ill-conditioned in FP32 when the top two eigenvalues nearly meet),
+// then UT and rmsd in FP32.
+__device__ void rmsd_finish_f32(const RmsdArgs<float> &a, int b, int n, const double *s_out, double *s_K,
                                 const double *s_c) {
     const int tid = threadIdx.x;
     if (tid == 0) {
-        float R[9];
-        for (int k = 0; k < 9; k++) R[k] = (float)s_out[k];
-        const float F[16] = {R[0] + R[4] + R[8], R[5] - R[7], R[6] - R[2], R[1] - R[3],
-                             R[5] - R[7], R[0] - R[4] - R[8], R[1] + R[3], R[2] + R[6],
-                             R[6] - R[2], R[1] + R[3], -R[0] + R[4] - R[8], R[5] + R[7],
-                             R[1] - R[3], R[2] + R[6], R[5] + R[7], -R[0] - R[4] + R[8]};
-        for (int k = 0; k < 16; k++) s_Kf[k] = F[k];
+        const double *R = s_out;
+        const double F[16] = {R[0] + R[4] + R[8], R[5] - R[7], R[6] - R[2], R[1] - R[3],
+                              R[5] - R[7], R[0] - R[4] - R[8], R[1] + R[3], R[2] + R[6],
+                              R[6] - R[2], R[1] + R[3], -R[0] + R[4] - R[8], R[5] + R[7],
+                              R[1] - R[3], R[2] + R[6], R[5] + R[7], -R[0] - R[4] + R[8]};
+        for (int k = 0; k < 16; k++) s_K[k] = F[k];
     }
     __syncwarp();
     const double r2 = s_out[9];
-    double lam;
-    float q[4];
-    key_eigen_warp_f32(s_Kf, 0.5 * r2, lam, q);
+    double lam, qd[4];
+    key_eigen_warp<true>(s_K, 0.5 * r2, lam, qd);
     if (tid != 0) return;
+    const float q[4] = {(float)qd[0], (float)qd[1], (float)qd[2], (float)qd[3]};
     float U[9];
     U[0] = q[0] * q[0] + q[1] * q[1] - q[2] * q[2] - q[3] * q[3];
     U[1] = 2.f * (q[1] * q[2] - q[0] * q[3]);
@@ -296,8 +259,8 @@ __device__ void rmsd_finish_f32(const RmsdArgs<float> &a, int b, int n, const do
     float *ut = a.ut + (size_t)9 * b;
     for (int j = 0; j < 3; j++)
         for (int k = 0; k < 3; k++) ut[3 * j + k] = U[3 * k + j];
-    const double msd = n > 0 ? (r2 - 2.0 * fabs(lam) + 1e-10) / (double)n : 0.0;
-    a.rmsd[b] = sqrtf(msd > 0.0 ? (float)msd : 0.f);
+    const float msd = n > 0 ? (float)(r2 - 2.0 * fabs(lam) + 1e-10) * (1.f / (float)n) : 0.f;
+    a.rmsd[b] = sqrtf(msd > 0.f ? msd : 0.f);
     if (a.centroids)
         for (int k = 0; k < 6; k++) a.centroids[6 * b + k] = s_c[k];
 }
@@ -327,7 +290,7 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
             }
         block_sums<T, 6>(sx, s_red, s_out);
         if (tid < 6) {  // one division per value, on six lanes (FP64 is slow on GB300)
-            const double v = n > 0 ? s_out[tid] / n : 0.0;
+            const double v = n > 0 ? (sizeof(T) == 4 ? s_out[tid] * (double)(1.f / (float)n) : s_out[tid] / n) : 0.0;
             s_c[tid] = v;
             s_ct[tid] = (T)v;
         }
@@ -352,8 +315,7 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
     }
     block_sums<T, 10>(acc, s_red, s_out);
     if constexpr (sizeof(T) == 4) {
-        __shared__ float s_Kf[16];
-        if (tid < 32) rmsd_finish_f32(a, b, n, s_out, s_Kf, s_c);
+        if (tid < 32) rmsd_finish_f32(a, b, n, s_out, s_K, s_c);
         return;
     }
     if (tid < 32) {
@@ -370,7 +332,7 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
         }
         __syncwarp();
         double lam, q[4];
-        key_eigen_warp(s_K, 0.5 * tot[9], lam, q);
+        key_eigen_warp<false>(s_K, 0.5 * tot[9], lam, q);
         if (tid != 0) return;
         // rotation from the unit quaternion (coords2rmsd_interface.cpp:36-46)
         double U[9];
