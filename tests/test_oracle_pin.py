@@ -110,7 +110,8 @@ def test_a2b_central_differences(oracle_lib):
 
 
 def test_a2c_central_differences(oracle_lib):
-    # BASELINE config 2 check, scaled down: 16 random entries per chain, h = 1e-6
+    # the finite-difference check of the 64-chain x 150-residue full-atom case, scaled down:
+    # 16 random entries per chain, h = 1e-6
     rng = np.random.default_rng(12)
     seqs = [AA, "".join(rng.choice(list(AA), 25))]
     L = 25 if len(AA) < 25 else len(AA)
