@@ -461,3 +461,53 @@ def test_cpp_autograd_path_matches_python_function(built, dtype):
     assert torch.equal(c1, c2) and torch.equal(r1, r2) and torch.equal(a1, a2)
     assert torch.equal(loss1.detach(), rmsd2.sum().detach())
     assert torch.equal(x1.grad, x2.grad)
+
+
+def test_full_size_backbone_geometry(fm):
+    """At the 4096-chain x 500-residue scale (random sequences, angles U[-pi, pi)),
+    properties that hold whatever the size: every N-CA, CA-C and C-N(next) bond of
+    every chain has its template length (1.46, 1.525 and 1.33 A) within 2e-4 A in
+    FP32, each residue's N-CA-C angle is the template's, and the rows past each
+    chain's atoms are exactly zero.  The FP32 forward against the FP64 form on a
+    16-chain slice within the float32 tolerance."""
+    from torchproteinlibrary_gb300.FullAtomModel.Angles2Coords import convertStringList
+    rng = np.random.default_rng(2024)
+    B, L = 4096, 500
+    aa = np.array(list(AA))
+    seqs = ["".join(rng.choice(aa, L)) for _ in range(B)]
+    nat_of = {c: fm.getSeqNumAtoms(c) for c in AA}
+    dev = torch.device("cuda")
+    ang = torch.tensor(rng.uniform(-np.pi, np.pi, (B, 8, L)), dtype=torch.float32, device=dev)
+    seq = convertStringList(seqs).to(dev)
+    counts = np.array([[nat_of[c] for c in s] for s in seqs], dtype=np.int64)
+    maxA = int(counts.sum(1).max())
+    coords = torch.full((B, 3 * maxA), float("nan"), device=dev)
+    e = torch.empty(0, dtype=torch.uint8, device=dev)
+    fm.Angles2Coords_forward(seq, ang, coords, e, e)
+    assert fm.workspace_status(0) == 0
+    off = np.concatenate([np.zeros((B, 1), np.int64), np.cumsum(counts, 1)[:, :-1]], 1)
+    n_idx = torch.tensor(off, device=dev)
+    ca_idx = n_idx + 1
+    c_idx = torch.tensor(off + counts - 2, device=dev)
+    X = coords.view(B, maxA, 3).double()
+
+    def at(idx):
+        return torch.gather(X, 1, idx.unsqueeze(-1).expand(-1, -1, 3))
+
+    N, CA, C = at(n_idx), at(ca_idx), at(c_idx)
+    for p, q, d in ((N, CA, 1.46), (CA, C, 1.525), (C[:, :-1], N[:, 1:], 1.33)):
+        err = ((p - q).norm(dim=-1) - d).abs().max().item()
+        assert err <= 2e-4, (d, err)
+    u, v = N - CA, C - CA
+    cosang = (u * v).sum(-1) / (u.norm(dim=-1) * v.norm(dim=-1))
+    ang_err = (torch.acos(cosang.clamp(-1, 1)) - torch.acos(cosang[0, 0].clamp(-1, 1))).abs().max().item()
+    assert ang_err <= 1e-4, ang_err
+    tot = counts.sum(1)
+    for b in (0, B // 2, B - 1):
+        assert torch.all(coords[b, 3 * int(tot[b]):] == 0)
+    # a 16-chain slice against the FP64 form
+    sl = slice(0, 16)
+    c64 = torch.empty(16, 3 * maxA, dtype=torch.float64, device=dev)
+    fm.Angles2Coords_forward(seq[sl], ang[sl].double(), c64, e, e)
+    d = (coords[sl].double() - c64).view(16, maxA, 3).norm(dim=-1).max().item()
+    assert d <= COORD_TOL_F32, d
