@@ -97,3 +97,38 @@ def test_host_num_atoms_reused_and_refreshed(built):
     r3 = layer(x, y, n)
     ref, _, _ = oracle.rmsd(src, dst, n.numpy())
     assert np.allclose(r3.cpu().numpy(), ref, rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_small_and_degenerate_chains(built, dtype):
+    """Chains of 0, 1, 2 and 3 atoms, collinear and planar chains (repeated
+    eigenvalues of the key matrix), identical structures (rmsd 0) and a mirrored copy:
+    rmsd against the oracle, finite gradients everywhere and zero gradient past each
+    chain.  rmsd = sqrt((R2 - 2 lambda + 1e-10) / N) cancels for near-identical
+    structures, so its absolute resolution is about sqrt(eps R2 / N): the tolerance is
+    2e-2 A in float32 and 1e-5 A in float64 (coordinates of about 10 A here)."""
+    from torchproteinlibrary_gb300.RMSD import Coords2RMSD
+    rng = np.random.default_rng(77)
+    N = 40
+    src = rng.standard_normal((10, N, 3)) * 8
+    dst = rng.standard_normal((10, N, 3)) * 8
+    na = np.array([0, 1, 2, 3, N, N, N, N, N, N], np.int32)
+    line = np.linspace(-20, 20, N)[:, None] * np.array([0.3, 0.5, 0.8])
+    src[4], dst[4] = line, line[::-1] + 5.0                      # collinear
+    src[5, :, 2] = 0.0
+    dst[5] = src[5] @ random_rotation(rng).T + 3.0                # planar, rigid copy
+    dst[6] = src[6]                                               # identical
+    dst[7] = src[7] * np.array([-1.0, 1.0, 1.0])                  # mirror image
+    src[8, :, 2] = 0.0
+    dst[8, :, 2] = 0.0                                            # both planar
+    x = torch.tensor(src.reshape(10, -1), dtype=dtype, device="cuda", requires_grad=True)
+    y = torch.tensor(dst.reshape(10, -1), dtype=dtype, device="cuda")
+    r = Coords2RMSD()(x, y, torch.tensor(na, device="cuda"))
+    r.sum().backward()
+    ro, _, _ = oracle.rmsd(src.reshape(10, -1), dst.reshape(10, -1), na)
+    atol = 2e-2 if dtype == torch.float32 else 1e-5
+    np.testing.assert_allclose(r.detach().double().cpu().numpy(), ro, atol=atol, rtol=0)
+    g = x.grad.double().cpu().numpy()
+    assert np.isfinite(g).all()
+    for b in range(10):
+        assert np.all(g[b, 3 * na[b]:] == 0.0)

@@ -78,6 +78,58 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
+// Largest eigenpair of the symmetric 4x4 K by cyclic Jacobi rotations in FP64, on one
+// thread: the fallback of key_eigen_warp for a near-multiple largest root (collinear
+// or otherwise degenerate structures, two-atom chains), where Newton on the quartic
+// converges only linearly and stalls at about the square root of the rounding error.
+// Rotation (p, r) with t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)),
+// theta = (a_rr - a_pp) / (2 a_pr), zeroes a_pr (A' = J^T A J, V' = V J).  a and v
+// are 16 doubles of shared scratch each, so that the rare path adds no registers to
+// the kernel.
+__device__ __forceinline__ void jacobi_top_eigenpair(const double *K, double *a, double *v, double &lam,
+                                                  double (&q)[4]) {
+    for (int i = 0; i < 16; i++) {
+        a[i] = K[i];
+        v[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    }
+    for (int sweep = 0; sweep < 16; sweep++) {
+        double off = 0.0, dg = 0.0;
+        for (int i = 0; i < 4; i++) {
+            dg += a[5 * i] * a[5 * i];
+            for (int j = i + 1; j < 4; j++) off += a[4 * i + j] * a[4 * i + j];
+        }
+        if (!(off > 1e-30 * (dg + off))) break;
+        for (int p = 0; p < 3; p++)
+            for (int r = p + 1; r < 4; r++) {
+                const double apr = a[4 * p + r];
+                if (!(fabs(apr) > 1e-300)) continue;
+                const double theta = (a[5 * r] - a[5 * p]) / (2.0 * apr);
+                const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < 4; k++) {  // A J
+                    const double akp = a[4 * k + p], akr = a[4 * k + r];
+                    a[4 * k + p] = c * akp - sn * akr;
+                    a[4 * k + r] = sn * akp + c * akr;
+                }
+                for (int k = 0; k < 4; k++) {  // J^T (A J)
+                    const double apk = a[4 * p + k], ark = a[4 * r + k];
+                    a[4 * p + k] = c * apk - sn * ark;
+                    a[4 * r + k] = sn * apk + c * ark;
+                }
+                for (int k = 0; k < 4; k++) {  // V J
+                    const double vkp = v[4 * k + p], vkr = v[4 * k + r];
+                    v[4 * k + p] = c * vkp - sn * vkr;
+                    v[4 * k + r] = sn * vkp + c * vkr;
+                }
+            }
+    }
+    int best = 0;
+    for (int i = 1; i < 4; i++)
+        if (a[5 * i] > a[5 * best]) best = i;
+    lam = a[5 * best];
+    for (int k = 0; k < 4; k++) q[k] = v[4 * k + best];
+}
+
 // The eigenvector for lam of key_eigen_warp<true>, in FP32: the largest row of the
 // cofactor matrix of K / e0 - (lam / e0) I (entries of order one), one cofactor per
 // lane.  The root itself stays FP64: when the top two eigenvalues nearly meet it is
@@ -141,7 +193,7 @@ __device__ void eigvec_f32(const double *sK, double e0, double l, double (&q)[4]
 // Executed by a full warp; every lane returns lam and the unit q (q = 1, 0, 0, 0
 // when every cofactor vanishes).
 template <bool F32_VEC>
-__device__ void key_eigen_warp(const double *sK, double e0, double &lam, double (&q)[4]) {
+__device__ void key_eigen_warp(const double *sK, double e0, double &lam, double (&q)[4], double *s_jac) {
     const int lane = threadIdx.x & 31;
     double t2 = 0.0, t3 = 0.0, c0 = 0.0;
     if (lane < 16) {
@@ -166,6 +218,7 @@ __device__ void key_eigen_warp(const double *sK, double e0, double &lam, double 
     double l = 0.0;
     if (e0 > 0.0) {
         const double ie = 1.0 / e0, ie2 = ie * ie;
+        const float ief = (float)ie;
         const float a2 = (float)(c2 * ie2), a1 = (float)(c1 * ie2 * ie), a0 = (float)(c0 * ie2 * ie2);
         float s = 1.f;
         for (int it = 0; it < 64; it++) {
@@ -177,12 +230,29 @@ __device__ void key_eigen_warp(const double *sK, double e0, double &lam, double 
             if (fabsf(d) <= 1e-6f) break;
         }
         l = (double)s * e0;
+        float corr = INFINITY;  // the last polish step, relative to e0
         for (int it = 0; it < 3; it++) {
             const double P = fma(fma(fma(l, l, c2), l, c1), l, c0);
             const double dP = fma(fma(4.0 * l, l, 2.0 * c2), l, c1);
             const float dPf = (float)dP;
-            if (!(dPf != 0.f) || !isfinite(dPf)) break;
-            l -= P * (double)(1.f / dPf);
+            if (!(dPf != 0.f) || !isfinite(dPf)) {
+                corr = INFINITY;
+                break;
+            }
+            const double d = P * (double)(1.f / dPf);
+            l -= d;
+            corr = (float)d * ief;
+        }
+        // a simple root has converged by the third polish step (each gains about
+        // seven digits); a near-multiple one (the top eigenvalues of K nearly or
+        // exactly equal) converges only linearly: a last step above 1e-10 of e0 sends
+        // the chain to the Jacobi solve (the same decision on every lane)
+        if (!(fabsf(corr) <= 1e-10f)) {
+            double lj = 0.0, qj[4] = {1.0, 0.0, 0.0, 0.0};
+            if (lane == 0) jacobi_top_eigenpair(sK, s_jac, s_jac + 16, lj, qj);
+            lam = __shfl_sync(0xffffffffu, lj, 0);
+            for (int k = 0; k < 4; k++) q[k] = __shfl_sync(0xffffffffu, qj[k], 0);
+            return;
         }
     }
     lam = l;
@@ -230,7 +300,7 @@ __device__ void key_eigen_warp(const double *sK, double e0, double &lam, double 
 // largest root is ill-conditioned in FP32 when the top two eigenvalues nearly meet),
 // then UT and rmsd in FP32.
 __device__ void rmsd_finish_f32(const RmsdArgs<float> &a, int b, int n, const double *s_out, double *s_K,
-                                const double *s_c) {
+                                const double *s_c, double *s_jac) {
     const int tid = threadIdx.x;
     if (tid == 0) {
         const double *R = s_out;
@@ -243,7 +313,7 @@ __device__ void rmsd_finish_f32(const RmsdArgs<float> &a, int b, int n, const do
     __syncwarp();
     const double r2 = s_out[9];
     double lam, qd[4];
-    key_eigen_warp<true>(s_K, 0.5 * r2, lam, qd);
+    key_eigen_warp<true>(s_K, 0.5 * r2, lam, qd, s_jac);
     if (tid != 0) return;
     const float q[4] = {(float)qd[0], (float)qd[1], (float)qd[2], (float)qd[3]};
     float U[9];
@@ -270,6 +340,7 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
     __shared__ double s_red[kRmsdWarps * 10];
     __shared__ double s_out[10];
     __shared__ double s_K[16];
+    __shared__ double s_jac[32];  // scratch of the Jacobi fallback
     __shared__ double s_c[6];  // centroids (src, dst)
     __shared__ T s_ct[6];
     const int b = blockIdx.x, tid = threadIdx.x;
@@ -315,7 +386,7 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
     }
     block_sums<T, 10>(acc, s_red, s_out);
     if constexpr (sizeof(T) == 4) {
-        if (tid < 32) rmsd_finish_f32(a, b, n, s_out, s_K, s_c);
+        if (tid < 32) rmsd_finish_f32(a, b, n, s_out, s_K, s_c, s_jac);
         return;
     }
     if (tid < 32) {
@@ -332,7 +403,7 @@ __global__ void __launch_bounds__(kRmsdThreads) rmsd_fwd_kernel(RmsdArgs<T> a) {
         }
         __syncwarp();
         double lam, q[4];
-        key_eigen_warp<false>(s_K, 0.5 * tot[9], lam, q);
+        key_eigen_warp<false>(s_K, 0.5 * tot[9], lam, q, s_jac);
         if (tid != 0) return;
         // rotation from the unit quaternion (coords2rmsd_interface.cpp:36-46)
         double U[9];
