@@ -194,6 +194,25 @@ def test_empty_inputs(rm):
     assert np.all(c == 0) and np.all(gi == 0)
 
 
+def test_layer_empty_batch_and_zero_lengths(rm):
+    """The float32 layer (its C++ autograd function) on an empty batch and on chains of
+    length 0: empty or all-zero coordinates, and a backward that returns zeros of the
+    angles' shape."""
+    from torchproteinlibrary_gb300.ReducedModel import Angles2Backbone
+    dev = torch.device("cuda")
+    layer = Angles2Backbone()
+    x = torch.zeros(0, 3, 16, device=dev, requires_grad=True)
+    out = layer(x, torch.zeros(0, dtype=torch.int32, device=dev))
+    assert out.shape == (0, 144)
+    out.sum().backward()
+    assert x.grad.shape == (0, 3, 16)
+    x = torch.rand(3, 3, 16, device=dev, requires_grad=True)
+    out = layer(x, torch.zeros(3, dtype=torch.int32, device=dev))
+    assert torch.all(out == 0)
+    out.backward(torch.ones_like(out))
+    assert torch.all(x.grad == 0)
+
+
 def test_errors_raise(rm):
     dev = torch.device("cuda")
     a = torch.zeros(2, 3, 8, device=dev)
