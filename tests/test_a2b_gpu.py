@@ -117,6 +117,31 @@ def test_tile_shapes_and_lookback(rm, rpt, cta):
     check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
 
 
+@pytest.mark.parametrize("rpt,cta", [(4, 32), (8, 32), (4, 4), (8, 4), (4, 1), (4, 128)])
+def test_angles_beyond_the_fast_sincos_range(rm, rpt, cta):
+    """Angles far outside [-pi, pi] (one in eight phi and psi moved by up to 1e5 turns)
+    send their four-residue groups down the rare path of the walk (sincosf instead of
+    the polynomial sin/cos): inlined in most forwards, a call in the one-warp C = 4
+    form.  Every scheme's forward and recomputing backward, and the backward from the
+    coordinates, against the oracle on the same float32 angles."""
+    B, L = 6, 600
+    ang, lengths, g = make_case(B, L, 61 + rpt, lengths=[600, 599, 257, 128, 33, 1])
+    rng = np.random.default_rng(7 + rpt + cta)
+    pick = rng.random((B, 2, L)) < 0.125
+    turns = rng.integers(-100000, 100001, (B, 2, L)) * (2 * np.pi)
+    ang[:, :2] = np.where(pick, ang[:, :2] + turns, ang[:, :2])
+    assert np.abs(ang).max() > 1e4
+    rm.set_options(rpt, 0, 0, 0, cta)
+    try:
+        c, gi = run_gpu(rm, ang, lengths, g, torch.float32)
+        c2, gi2 = run_gpu_coords_backward(rm, ang, lengths, g, 4)
+    finally:
+        rm.set_options(0, 0, 0, 0)
+    rc, rg = oracle_ref(ang, lengths, g, True)
+    check(c, gi, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+    check(c2, gi2, rc, rg, lengths, L, COORD_TOL_F32, GRAD_TOL_F32)
+
+
 def test_fp64_carry_threshold_and_renorm_off(rm):
     """FP32 inter-tile carries (fp64_carry_min_len=-1) or a threshold of 256 keep the
     1e-3 A bound; switching the Newton-Schulz renormalisation off is an ablation

@@ -511,3 +511,23 @@ def test_full_size_backbone_geometry(fm):
     fm.Angles2Coords_forward(seq[sl], ang[sl].double(), c64, e, e)
     d = (coords[sl].double() - c64).view(16, maxA, 3).norm(dim=-1).max().item()
     assert d <= COORD_TOL_F32, d
+
+
+def test_angles_beyond_the_fast_sincos_range(fm):
+    """One in eight of the eight angle rows moved by up to 1e5 turns: those residues take
+    sincosf instead of the polynomial sin/cos; the forward and both float32 backwards
+    against the oracle on the same float32 angles."""
+    seqs, ang, _, _, _ = coords_case(83)
+    rng = np.random.default_rng(83)
+    pick = rng.random(ang.shape) < 0.125
+    ang = np.where(pick, ang + rng.integers(-100000, 100001, ang.shape) * (2 * np.pi), ang)
+    ang = ang.astype(np.float32).astype(np.float64)
+    assert np.abs(ang).max() > 1e4
+    rc, _, _, na = oracle.a2c_forward(ang, seqs)
+    g = rng.standard_normal(rc.shape).astype(np.float32).astype(np.float64)
+    for b, n in enumerate(na):
+        g[b, 3 * n:] = 0
+    rg = oracle.a2c_backward(g, ang, seqs)
+    for from_coords in (True, False):
+        c, _, _, _, gi = run_gpu(fm, ang, seqs, g, torch.float32, from_coords=from_coords)
+        check(c, gi, rc, rg, na, COORD_TOL_F32, GRAD_TOL_F32)
